@@ -1,0 +1,305 @@
+#!/usr/bin/env python
+"""Headline benchmark: wall-Stokeslet kernel sum (fl.evaluate(WallStokeslet3D, ...)).
+
+Workload (one step): 262,144 targets uniform in [-1,1]^2 x [0.02,2] plus 16,384
+targets on the wall z = 0, 262,144 sources in the same box, i.i.d. N(0,1)
+FP64 forces, eps = 0.01, seeded (synthetic, the reference publishes no
+dataset).  One step = one mixed-precision sum (FP32 far field + FP64 near
+field for r < 4 eps) over all 278,528 x 262,144 pairs; inputs resident in HBM.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints ONE JSON line.  Timing: CUDA events on the launching stream around each
+step, L2 flushed (256 MB write) between timed steps, max over ranks; e2e goes
+through the public API with pinned host buffers (H2D + D2H inside the timed
+region).  The roofline of the dominant kernel (far_f32_kernel) uses the
+per-launch durations recorded by the library's CUDA events and the FP32 FFMA
+peak measured in the same process.  Multi-GPU: each rank sums its own
+independent workload (weak scaling, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N_SRC, N_TGT, N_WALL, EPS = 262144, 262144, 16384, 0.01
+FLOPS_PER_PAIR = 106          # WallStokeslet3D: canonical count (31 Stokeslet + 75 image)
+METRIC = "pair-interactions/s"
+WORKLOAD = "WallStokeslet3D sum, 278,528 targets (16,384 on z=0) x 262,144 sources, eps=0.01"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--cpu-sample", type=int, default=2048, help="targets in the CPU sample (x all sources)")
+    p.add_argument("--no-extras", action="store_true", help="skip the accuracy / FP64 / solve sections")
+    return p.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons every 200 ms while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_workload(seed):
+    from fluidlets_gb300.geometry import wall_sum_workload
+
+    return wall_sum_workload(N_SRC, N_TGT, N_WALL, EPS, seed=seed)
+
+
+def cpu_sample_rate(T, S, F, eps, n_targets):
+    """The oracle (C/OpenMP restatement of the reference loop) on all host cores."""
+    import oracle
+
+    threads = oracle.max_threads()
+    sub = T[:: max(1, len(T) // n_targets)][:n_targets]
+    t0 = time.perf_counter()
+    oracle.evaluate("wall", sub, S, F, eps)
+    dt = time.perf_counter() - t0
+    return len(sub) * len(S) / dt, threads, f"{len(sub)} targets x {len(S)} sources (WallStokeslet3D, FP64)"
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    T, S, F, eps = make_workload(0)
+    rates = []
+    import oracle
+
+    oracle.build()
+    for i in range(args.warmup + args.steps):
+        r, threads, sample = cpu_sample_rate(T[i % 7:], S, F, eps, args.cpu_sample)
+        if i >= args.warmup:
+            rates.append(r)
+    total_pairs = args.cpu_sample * N_SRC * args.steps
+    total_time = sum(args.cpu_sample * N_SRC / r for r in rates)
+    value = total_pairs / total_time
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_time / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)", "config": {"workload": WORKLOAD, "sample": sample},
+            "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import fluidlets_gb300 as fl
+    from fluidlets_gb300 import _lib
+
+    L = _lib.load()
+    dev = torch.device("cuda", local)
+    T, S, F, eps = make_workload(rank)
+    Td, Sd, Fd = (torch.from_numpy(a).to(dev) for a in (T, S, F))
+    ed = torch.full((N_SRC,), eps, dtype=torch.float64, device=dev)
+    kern = fl.WallStokeslet3D()
+    pairs = len(T) * len(S)
+    flush = torch.empty(256 * 2**20, dtype=torch.uint8, device=dev)
+
+    import ctypes
+
+    fp32_peak, fp64_peak = ctypes.c_double(0), ctypes.c_double(0)
+    _lib.check(L.flg_measure_peaks(ctypes.byref(fp32_peak), ctypes.byref(fp64_peak),
+                                   ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+
+    def step():
+        return fl.evaluate(kern, Td, Sd, Fd, ed, precision="mixed")
+
+    for _ in range(args.warmup):
+        out = step()
+    torch.cuda.synchronize()
+    L.flg_profile_enable(1)
+    launches0 = L.flg_launch_count()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            ev[k][0].record()
+            out = step()
+            ev[k][1].record()
+            flush.zero_()  # L2 flush between timed steps (outside the event pair)
+        torch.cuda.synchronize()
+    launches = L.flg_launch_count() - launches0
+    if dist:
+        dist.barrier()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = sum(step_ms)
+    far_ms, far_n = ctypes.c_double(0), ctypes.c_int64(0)
+    L.flg_profile_read(_lib.SLOT["far_f32"], ctypes.byref(far_ms), ctypes.byref(far_n))
+    near_ms, near_n = ctypes.c_double(0), ctypes.c_int64(0)
+    L.flg_profile_read(_lib.SLOT["near_f64"], ctypes.byref(near_ms), ctypes.byref(near_n))
+    L.flg_profile_enable(0)
+    if dist:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = pairs * args.steps * world / (total_ms * 1e-3)
+
+    # e2e through the public API: pinned host inputs, host output
+    Th, Sh, Fh = (torch.from_numpy(a).pin_memory() for a in (T, S, F))
+    out_h = None
+    for _ in range(1):
+        out_h = fl.evaluate(kern, Th, Sh, Fh, eps, precision="mixed")
+    torch.cuda.synchronize()
+    e2e_steps = max(1, min(args.steps, 5))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        out_h = fl.evaluate(kern, Th, Sh, Fh, eps, precision="mixed")
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    assert out_h.device.type == "cpu"
+    h2d = (T.nbytes + S.nbytes + F.nbytes)
+    d2h = out_h.numel() * out_h.element_size()
+    e2e_value = pairs * world / e2e_s
+    if dist:
+        t = torch.tensor([e2e_value], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MIN)
+        e2e_value = float(t.item()) * 1.0
+
+    far_avg_ms = far_ms.value / max(far_n.value, 1)
+    achieved = FLOPS_PER_PAIR * pairs / (far_avg_ms * 1e-3) / 1e12
+    traffic = None
+    prof = ROOT / "profiles" / "far_f32_wall_traffic.json"
+    if prof.exists():
+        try:
+            traffic = json.loads(prof.read_text()).get("bytes_per_launch_full_size")
+        except (ValueError, OSError):
+            traffic = None
+    line = {
+        "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 far field + f64 near field (r<4eps)",
+        "data": "synthetic (seeded uniform points, N(0,1) forces)",
+        "config": {"workload": WORKLOAD, "targets": len(T), "sources": len(S), "eps": eps,
+                   "precision": "mixed", "l2": "flushed (256 MB write) between timed steps",
+                   "parallelism": f"replicas x{world}"},
+        "clocks": clk.summary(),
+        "e2e": {"value": e2e_value, "unit": "pairs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak.value, "unit": "TFLOP/s",
+                     "frac": achieved / fp32_peak.value, "traffic": traffic,
+                     "kernel": "far_f32_kernel", "flops_per_pair": FLOPS_PER_PAIR,
+                     "peak_source": "FFMA microbenchmark measured in this run (of measured)",
+                     "far_ms_per_launch": far_avg_ms, "near_ms_per_launch": near_ms.value / max(near_n.value, 1)},
+        "fp64_peak_tflops": fp64_peak.value,
+    }
+    if rank == 0 and not args.no_extras:
+        # accuracy vs the plain FP64 GPU path on a sample of targets, and that path's rate
+        idx = np.r_[np.arange(0, N_TGT, 32), N_TGT + np.arange(0, N_WALL, 16)]
+        Ts = Td[torch.from_numpy(idx).to(dev)]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        u64 = fl.evaluate(kern, Ts, Sd, Fd, ed, precision="fp64")
+        torch.cuda.synchronize()
+        fp64_rate = len(idx) * N_SRC / (time.perf_counter() - t0)
+        um = out[torch.from_numpy(idx).to(dev)]
+        inter = torch.from_numpy(idx < N_TGT).to(dev)
+        err = float(torch.linalg.vector_norm(um[inter] - u64[inter]) / torch.linalg.vector_norm(u64[inter]))
+        line["accuracy"] = {"rel_l2_vs_fp64_gpu": err, "max_abs_u_on_wall_mixed": float(um[~inter].abs().max()),
+                            "max_abs_u_on_wall_fp64": float(u64[~inter].abs().max()),
+                            "sample_targets": int(len(idx))}
+        line["fp64_gpu_path"] = {"value": fp64_rate, "unit": "pairs/s",
+                                 "sample": f"{len(idx)} targets x {N_SRC} sources",
+                                 "mixed_speedup": value / world / fp64_rate}
+        rate, threads, sample = cpu_sample_rate(T, S, F, eps, args.cpu_sample)
+        line["cpu_baseline"] = {"value": rate, "unit": "pairs/s", "cores": threads, "kind": "port",
+                                "sample": sample}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

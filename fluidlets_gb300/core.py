@@ -1,0 +1,323 @@
+"""The reference's operator API on the GPU: evaluate, assemble, resistance.
+
+Signatures, defaults, dtype rules and exceptions follow the reference package
+``fluidlets`` (``core/_common.py``, ``core/matvec.py``, ``core/assemble.py``,
+``core/solve.py``); the O(MN) loops, the dense LU and GMRES run in
+``libfluidlets_gb300.so`` on the current CUDA device.
+
+NumPy in gives NumPy out (host <-> device copies at this boundary); torch CUDA
+tensors in give torch CUDA tensors out with no host round trip.
+
+Extensions, all keyword-only with defaults that reproduce the reference:
+``precision="fp64" | "mixed"`` (FP32 far field + FP64 near field for sums;
+TF32/BF16 tensor-core LU + FP64 GMRES iterative refinement for solves).
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _device as dv
+from ._lib import BF16, C128, F32, F64, LU_MODE, PREC, check, load
+from .kernels import kernel_params
+
+#: above this many unknowns, method="auto" switches from dense LU to GMRES (core/solve.py:20)
+DENSE_MAX = 6000
+
+
+# ---- input normalization (core/_common.py:7-23) ---------------------------
+def _points(a, dim=3) -> torch.Tensor:
+    if isinstance(a, torch.Tensor):
+        t = a.to(dtype=torch.float64)
+        if t.dim() == 1:
+            t = t.reshape(1, -1)
+        if t.dim() != 2 or t.shape[1] != dim:
+            raise ValueError(f"expected points of shape (N, {dim}), got {tuple(a.shape)}")
+        return dv.to_dev(t, torch.float64)
+    arr = np.atleast_2d(np.asarray(a, dtype=np.float64))
+    if arr.ndim != 2 or arr.shape[1] != dim:
+        raise ValueError(f"expected points of shape (N, {dim}), got {arr.shape}")
+    return dv.to_dev(arr, torch.float64)
+
+
+def _blob_widths(eps, n) -> torch.Tensor:
+    if isinstance(eps, torch.Tensor):
+        e = eps.to(dtype=torch.float64)
+        return dv.to_dev(torch.broadcast_to(e, (n,)), torch.float64)
+    e = np.asarray(eps, dtype=np.float64)
+    return dv.to_dev(np.broadcast_to(e, (n,)), torch.float64)
+
+
+def _prec(precision) -> int:
+    if precision not in PREC:
+        raise ValueError(f"unknown precision {precision!r} (expected 'fp64' or 'mixed')")
+    return PREC[precision]
+
+
+def _mu(mu):
+    m = complex(mu.item() if isinstance(mu, torch.Tensor) else mu)
+    if m == 0:
+        raise ValueError("mu must be non-zero")
+    return m, dv.is_complex_value(mu)
+
+
+def _out(t: torch.Tensor, where):
+    """NumPy for NumPy callers; a torch tensor on the inputs' device otherwise."""
+    if where is None:
+        return dv.to_host(t)
+    return t if where == "cuda" else t.cpu()
+
+
+# ---- core/matvec.py:24-49 ---------------------------------------------------
+def _evaluate_dev(kernel, X, Y, f, e, mu, precision, out=None):
+    """Device-level sum: X (M,3), Y (N,3), f (N,3) f64/c128, e (N,) -> (M,3)."""
+    kind, are, aim = kernel_params(kernel)
+    m, mu_c = _mu(mu)
+    M, N = X.shape[0], Y.shape[0]
+    fc = f.is_complex()
+    lib_complex = fc or aim != 0.0 or m.imag != 0.0
+    want_complex = lib_complex or mu_c
+    if out is None:
+        out = torch.empty((M, 3), dtype=torch.complex128 if lib_complex else torch.float64, device=X.device)
+    prec = _prec(precision)
+    L = load()
+    nbytes = L.flg_evaluate_workspace(kind, M, N, int(fc), aim, prec)
+    ws = dv.workspace(nbytes)
+    st = L.flg_evaluate(kind, are, aim, dv.ptr(X), M, dv.ptr(Y), dv.ptr(e), N, dv.ptr(f), int(fc), m.real, m.imag,
+                        dv.ptr(out), prec, dv.ptr(ws), nbytes, dv.stream())
+    check(st, "evaluate")
+    if want_complex and not out.is_complex():
+        out = out.to(torch.complex128)
+    return out
+
+
+def evaluate(kernel, targets, sources, strengths, eps, mu=1.0, *, precision="fp64"):
+    """Field at targets from regularized sources, without storing the matrix.
+
+    Same contract as the reference's ``fluidlets.evaluate``
+    (``core/matvec.py:24-49``): (M, 3) array, complex if mu, the strengths or
+    the kernel (complex Brinkman alpha) are complex.
+    """
+    as_torch = dv.home(targets, sources, strengths)
+    X = _points(targets, kernel.dim)
+    Y = _points(sources, kernel.dim)
+    N = Y.shape[0]
+    e = _blob_widths(eps, N)
+    fc = dv.is_complex_value(strengths)
+    f = dv.to_dev(strengths, torch.complex128 if fc else torch.float64).reshape(N, 3)
+    return _out(_evaluate_dev(kernel, X, Y, f, e, mu, precision), as_torch)
+
+
+# ---- core/assemble.py:27-101 ------------------------------------------------
+def _assemble_dev(kernel, X, Y, e, mu, out_dtype=torch.float64, out=None, ld=None):
+    kind, are, aim = kernel_params(kernel)
+    m, mu_c = _mu(mu)
+    M, N = X.shape[0], Y.shape[0]
+    complex_out = aim != 0.0 or m.imag != 0.0
+    if complex_out:
+        out_dtype = torch.complex128
+    code = {torch.float64: F64, torch.complex128: C128, torch.float32: F32, torch.bfloat16: BF16}[out_dtype]
+    if out is None:
+        out = torch.empty((3 * M, 3 * N), dtype=out_dtype, device=X.device)
+        ld = 3 * N
+    st = load().flg_assemble(kind, are, aim, dv.ptr(X), M, dv.ptr(Y), dv.ptr(e), N, m.real, m.imag, dv.ptr(out),
+                             code, ld, dv.stream())
+    check(st, "assemble")
+    if mu_c and not out.is_complex():
+        out = out.to(torch.complex128)
+    return out
+
+
+def assemble(kernel, targets, sources, eps, mu=1.0):
+    """Dense (3M) x (3N) matrix of ``kernel`` from N sources to M targets (``core/assemble.py:27-46``)."""
+    as_torch = dv.home(targets, sources)
+    X = _points(targets, kernel.dim)
+    Y = _points(sources, kernel.dim)
+    e = _blob_widths(eps, Y.shape[0])
+    return _out(_assemble_dev(kernel, X, Y, e, mu), as_torch)
+
+
+def nearest_neighbors(quad_points, force_points) -> np.ndarray:
+    """Index of the nearest force point for every quadrature point, shape (Q,) (``core/assemble.py:61-65``).
+
+    Host-side k-d tree (SciPy), as in the reference.
+    """
+    from scipy.spatial import cKDTree
+
+    return cKDTree(np.asarray(force_points, float)).query(np.asarray(quad_points, float))[1]
+
+
+def _assemble_nearest_dev(kernel, X, Xq, nn, n_force, e, mu, out_dtype=torch.float64, out=None, ld=None):
+    kind, are, aim = kernel_params(kernel)
+    m, mu_c = _mu(mu)
+    M, Q = X.shape[0], Xq.shape[0]
+    if aim != 0.0 or m.imag != 0.0:
+        out_dtype = torch.complex128
+    code = {torch.float64: F64, torch.complex128: C128, torch.float32: F32}[out_dtype]
+    if out is None:
+        out = torch.empty((3 * M, 3 * n_force), dtype=out_dtype, device=X.device)
+        ld = 3 * n_force
+    L = load()
+    nbytes = L.flg_assemble_nearest_workspace(Q, n_force)
+    ws = dv.workspace(nbytes)
+    st = L.flg_assemble_nearest(kind, are, aim, dv.ptr(X), M, dv.ptr(Xq), dv.ptr(nn), dv.ptr(e), Q, n_force,
+                                m.real, m.imag, dv.ptr(out), code, ld, dv.ptr(ws), nbytes, dv.stream())
+    check(st, "assemble_nearest")
+    if mu_c and not out.is_complex():
+        out = out.to(torch.complex128)
+    return out
+
+
+def assemble_nearest(kernel, targets, quad_points, nearest, n_force, eps, mu=1.0):
+    """Nearest-neighbour kernel matrix of Gallagher & Smith (2018) (``core/assemble.py:68-101``).
+
+    K[:, j] = sum over k with nearest[k] = j of G(x_i, X_k) / mu.
+    """
+    as_torch = dv.home(targets, quad_points)
+    X = _points(targets, kernel.dim)
+    Xq = _points(quad_points, kernel.dim)
+    e = _blob_widths(eps, Xq.shape[0])
+    nn = dv.to_dev(np.asarray(nearest) if not isinstance(nearest, torch.Tensor) else nearest, torch.int64)
+    if nn.numel() != Xq.shape[0]:
+        raise ValueError("nearest must have one entry per quadrature point")
+    n_force = int(n_force)
+    if nn.numel() and (int(nn.min()) < 0 or int(nn.max()) >= n_force):
+        raise ValueError("nearest indices must lie in [0, n_force)")
+    return _out(_assemble_nearest_dev(kernel, X, Xq, nn, n_force, e, mu), as_torch)
+
+
+# ---- core/solve.py:23-84 ----------------------------------------------------
+@dataclass
+class SolveInfo:
+    """``core/solve.py:23-27``, plus how the solve was computed."""
+
+    method: str
+    iterations: int
+    residual: float          # ||K f - U|| / ||U||, FP64 operator
+    precision: str = "fp64"
+    ir_steps: int = 0        # FP64 refinement steps of the mixed-precision path
+
+
+def _lu_solve_dev(K: torch.Tensor, U: torch.Tensor) -> torch.Tensor:
+    """Dense FP64 LU with partial pivoting (getrf + getrs) on the device; K is overwritten."""
+    n = K.shape[0]
+    L = load()
+    if K.is_complex():
+        # complex system through its real 2n x 2n form [[Re, -Im], [Im, Re]]
+        R = torch.empty((2 * n, 2 * n), dtype=torch.float64, device=K.device)
+        R[:n, :n] = K.real
+        R[:n, n:] = -K.imag
+        R[n:, :n] = K.imag
+        R[n:, n:] = K.real
+        b = torch.cat([U.real, U.imag]).to(torch.float64).contiguous() if U.is_complex() else \
+            torch.cat([U, torch.zeros_like(U)]).contiguous()
+        x = _lu_solve_dev(R, b)
+        return torch.complex(x[:n], x[n:])
+    piv = torch.empty(n, dtype=torch.int32, device=K.device)
+    nbytes = L.flg_lu_factor_f64_workspace(n)
+    ws = dv.workspace(nbytes)
+    info = ctypes.c_int(0)
+    check(L.flg_lu_factor_f64(n, dv.ptr(K), n, dv.ptr(piv), ctypes.byref(info), dv.ptr(ws), nbytes, dv.stream()),
+          "LU factorization")
+    B = U.reshape(n, -1).to(torch.float64).contiguous() if not U.is_complex() else None
+    if B is None:  # real matrix, complex right-hand side: two real columns
+        B = torch.stack([U.real, U.imag], 1).contiguous()
+        check(L.flg_lu_solve_f64(n, 2, dv.ptr(K), n, dv.ptr(piv), dv.ptr(B), 2, dv.stream()), "LU solve")
+        return torch.complex(B[:, 0], B[:, 1])
+    check(L.flg_lu_solve_f64(n, 1, dv.ptr(K), n, dv.ptr(piv), dv.ptr(B), 1, dv.stream()), "LU solve")
+    return B.reshape(-1)
+
+
+def _mixed_lu_solve_dev(K: torch.Tensor, U: torch.Tensor, rtol, restart, maxiter, lu_mode):
+    """TF32/BF16 tensor-core LU of K (no pivoting) + FP64 GMRES iterative refinement."""
+    n = K.shape[0]
+    L = load()
+    K32 = torch.empty((n, n), dtype=torch.float32, device=K.device)
+    check(L.flg_convert_f64_f32(n, n, dv.ptr(K), n, dv.ptr(K32), n, dv.stream()), "convert")
+    mode = LU_MODE[lu_mode]
+    nbytes = L.flg_lu_factor_lowp_workspace(n, mode)
+    ws = dv.workspace(nbytes)
+    info = ctypes.c_int(0)
+    check(L.flg_lu_factor_lowp(n, dv.ptr(K32), n, mode, ctypes.byref(info), dv.ptr(ws), nbytes, dv.stream()),
+          "low-precision LU")
+    del ws
+    b = U.reshape(-1).to(torch.float64).contiguous()
+    x = torch.zeros_like(b)
+    nbytes = L.flg_gmres_ir_dense_workspace(n, restart)
+    ws = dv.workspace(nbytes)
+    iters, outer, resid = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_double(0.0)
+    check(L.flg_gmres_ir_dense(n, dv.ptr(K), n, dv.ptr(K32), n, dv.ptr(b), dv.ptr(x), rtol, restart, maxiter,
+                               ctypes.byref(iters), ctypes.byref(outer), ctypes.byref(resid), dv.ptr(ws), nbytes,
+                               dv.stream()), "GMRES-IR")
+    return x, iters.value, outer.value, resid.value
+
+
+def _gmres_dev(kernel, X, e, mu, b, rtol, restart, maxiter, precision, inner_rtol=1e-6):
+    kind, are, aim = kernel_params(kernel)
+    m, _ = _mu(mu)
+    N = X.shape[0]
+    is_c = b.is_complex()
+    prec = _prec(precision)
+    L = load()
+    x = torch.zeros_like(b)
+    nbytes = L.flg_gmres_workspace(N, restart, int(is_c), prec)
+    ws = dv.workspace(nbytes)
+    iters, outer, resid = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_double(0.0)
+    st = L.flg_gmres(kind, are, aim, dv.ptr(X), dv.ptr(e), N, m.real, m.imag, dv.ptr(b), dv.ptr(x), int(is_c), rtol,
+                     restart, maxiter, prec, inner_rtol, ctypes.byref(iters), ctypes.byref(outer),
+                     ctypes.byref(resid), dv.ptr(ws), nbytes, dv.stream())
+    check(st, "GMRES")
+    return x, iters.value, outer.value, resid.value
+
+
+def resistance(kernel, points, velocities, eps, mu=1.0, method="auto", rtol=1e-10, restart=60, maxiter=200, *,
+               precision="fp64", lu="tf32"):
+    """Forces that produce the given velocities at the given points (``core/solve.py:30-84``).
+
+    Returns ``(forces (N, 3), SolveInfo)``.  ``method`` is "auto" (LU up to
+    ``DENSE_MAX`` unknowns, GMRES above), "lu" or "gmres"; GMRES follows
+    ``scipy.sparse.linalg.gmres`` (rtol relative to ||U||, atol 0, ``restart``
+    inner iterations per cycle, ``maxiter`` cycles) and raises RuntimeError if
+    it does not converge.
+
+    ``precision="mixed"``: LU runs as a TF32 (``lu="tf32"``) or BF16
+    (``lu="bf16"``) tensor-core factorization refined by FP64 GMRES to
+    ``rtol``; GMRES runs FP32-far/FP64-near matvecs inside FP64 iterative
+    refinement.  The residual reported is always that of the FP64 operator.
+    """
+    as_torch = dv.home(points, velocities)
+    X = _points(points, kernel.dim)
+    n = X.shape[0]
+    e = _blob_widths(eps, n)
+    Uc = dv.is_complex_value(velocities)
+    m, mu_c = _mu(mu)
+    kc = kernel_params(kernel)[2] != 0.0
+    cplx = Uc or mu_c or kc
+    U = dv.to_dev(velocities, torch.complex128 if Uc else torch.float64).reshape(-1)
+    if method == "auto":
+        method = "lu" if U.numel() <= DENSE_MAX else "gmres"
+    prec = _prec(precision)
+    ir_steps = 0
+    if method == "lu":
+        K = _assemble_dev(kernel, X, X, e, mu)
+        if prec == PREC["mixed"] and not K.is_complex() and not Uc:
+            f, iterations, ir_steps, _ = _mixed_lu_solve_dev(K, U, rtol, restart, maxiter, lu)
+        else:
+            f = _lu_solve_dev(K, U.to(K.dtype) if K.is_complex() else U)
+            iterations = 1
+        del K
+    elif method == "gmres":
+        b = U.to(torch.complex128) if cplx else U
+        f, iterations, ir_steps, _ = _gmres_dev(kernel, X, e, mu, b, rtol, restart, maxiter, precision)
+    else:
+        raise ValueError(f"unknown method {method!r}")
+    if cplx and not f.is_complex():
+        f = f.to(torch.complex128)
+    F = f.reshape(n, -1)
+    # final FP64 residual, one more O(N^2) sum as in core/solve.py:83
+    Kf = _evaluate_dev(kernel, X, X, F.contiguous(), e, mu, "fp64").reshape(-1)
+    resid = float(torch.linalg.vector_norm(Kf - U) / torch.linalg.vector_norm(U))
+    return _out(F, as_torch), SolveInfo(method, int(iterations), resid, precision, int(ir_steps))

@@ -1,0 +1,458 @@
+// assemble.cu -- dense mobility matrices and dense helpers.
+//
+//  flg_assemble            fluidlets.assemble (core/assemble.py:27-46, _fill 15-24)
+//  flg_assemble_nearest    fluidlets.assemble_nearest (core/assemble.py:68-101,
+//                          _fill_nearest 49-58), deterministic segmented sum
+//  flg_swimmer_constraints the rows/columns of swimming.py:90-99
+//  flg_gemv_f64, flg_convert_f64_f32
+//
+// Assembly writes K / mu once, directly in the requested element type (the
+// reference makes two extra full copies, core/assemble.py:46).  Each thread
+// computes one 3x3 block G(x_i, y_j) in FP64 and stores its nine entries;
+// consecutive threads take consecutive sources j, so a warp writes three
+// contiguous 96-element row segments.
+#include <cuda_bf16.h>
+
+#include "flg_common.cuh"
+#include "pair_math.cuh"
+#include "sum_plan.cuh"
+
+namespace flg {
+
+struct AsmArgs {
+    const double *tg;
+    int64_t M;
+    const double *src;
+    const double *eps;
+    int64_t N;
+    double are, aim;
+    double scale;  // global kernel scale
+    // 1/mu as a complex number
+    double imu_re, imu_im;
+    void *out;
+    int out_type;
+    int64_t ld;
+    int64_t col_off;  // first column written (nearest: group index scale)
+};
+
+// 3x3 block (row-major, before scale / mu); complex part only for complex alpha
+template <int KIND, bool CK>
+__device__ __forceinline__ void block_f64(double tx, double ty, double tz, double sx, double sy, double sz,
+                                          double e2, double are, double aim, double G[9], double Gi[9]) {
+    if constexpr (KIND == FLG_WALL) {
+        WallGeo<double> g = wall_geo<double, false>(tx, ty, tz, 2.0 * tz, sx, sy, sz, e2, 0.0);
+        const double W = g.W2, Zs = g.Z3 + g.s5x3;
+        const double dd[2] = {g.d0, g.d1};
+        for (int j = 0; j < 2; j++) {
+            G[3 * j + 0] = W * fma(dd[j] * g.d0, Zs, j == 0 ? g.cxy : 0.0);
+            G[3 * j + 1] = W * fma(dd[j] * g.d1, Zs, j == 1 ? g.cxy : 0.0);
+            G[3 * j + 2] = W * dd[j] * fma(g.Z3, g.dm, -g.s5x3 * g.dp);
+        }
+        const double c2 = fma(g.dm, g.Z3, g.s5x3 * g.dp);
+        G[6] = W * g.d0 * c2;
+        G[7] = W * g.d1 * c2;
+        G[8] = W * fma(g.dm * g.dm, g.Z3, fma(-g.s5x3 * g.dp, g.dp, g.cz));
+    } else {
+        const double d[3] = {tx - sx, ty - sy, tz - sz};
+        const double Q = fma(d[2], d[2], fma(d[1], d[1], fma(d[0], d[0], e2)));
+        const double s = rsq(Q);
+        if constexpr (CK) {
+            cpx<double> A, B;
+            brink_AB_c<double>(s, Q, e2, are, aim, A, B);
+            for (int a = 0; a < 3; a++)
+                for (int b = 0; b < 3; b++) {
+                    G[3 * a + b] = fma(B.re * d[a], d[b], a == b ? A.re : 0.0);
+                    Gi[3 * a + b] = fma(B.im * d[a], d[b], a == b ? A.im : 0.0);
+                }
+            return;
+        } else {
+            double A, B;
+            if constexpr (KIND == FLG_STOKESLET) stokeslet_AB(s, e2, A, B);
+            else brink_AB<double>(s, Q, e2, are, A, B);
+            for (int a = 0; a < 3; a++)
+                for (int b = 0; b < 3; b++) G[3 * a + b] = fma(B * d[a], d[b], a == b ? A : 0.0);
+        }
+    }
+    if constexpr (CK == false)
+        for (int k = 0; k < 9; k++) Gi[k] = 0.0;
+}
+
+__device__ __forceinline__ void store_block(const AsmArgs &a, int64_t i, int64_t col, const double G[9],
+                                            const double Gi[9], bool cplx) {
+    for (int r = 0; r < 3; r++) {
+        const int64_t row = 3 * i + r;
+        for (int c = 0; c < 3; c++) {
+            const int64_t off = row * a.ld + col + c;
+            // (G + i Gi) * scale * (1/mu)
+            const double gr = G[3 * r + c] * a.scale, gi = cplx ? Gi[3 * r + c] * a.scale : 0.0;
+            const double vr = gr * a.imu_re - gi * a.imu_im;
+            const double vi = gr * a.imu_im + gi * a.imu_re;
+            switch (a.out_type) {
+                case FLG_F64: ((double *)a.out)[off] = vr; break;
+                case FLG_C128:
+                    ((double *)a.out)[2 * off] = vr;
+                    ((double *)a.out)[2 * off + 1] = vi;
+                    break;
+                case FLG_F32: ((float *)a.out)[off] = (float)vr; break;
+                default: ((__nv_bfloat16 *)a.out)[off] = __double2bfloat16(vr); break;
+            }
+        }
+    }
+}
+
+template <int KIND, bool CK>
+__global__ void __launch_bounds__(128) assemble_kernel(AsmArgs a) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= a.N) return;
+    const double sx = a.src[3 * j], sy = a.src[3 * j + 1], sz = a.src[3 * j + 2];
+    const double e = a.eps[j], e2 = e * e;
+    const bool cplx = CK || a.imu_im != 0.0;
+    for (int64_t i = blockIdx.y; i < a.M; i += gridDim.y) {
+        double G[9], Gi[9];
+        block_f64<KIND, CK>(a.tg[3 * i], a.tg[3 * i + 1], a.tg[3 * i + 2], sx, sy, sz, e2, a.are, a.aim, G, Gi);
+        store_block(a, i, 3 * j, G, Gi, cplx);
+    }
+}
+
+// nearest-neighbour assembly: thread per (target i, force group j), members of
+// group j (ascending quadrature index) summed in FP64
+struct NearestArgs {
+    AsmArgs a;
+    const int *grp_off;   // [n_force + 1]
+    const int *grp_idx;   // [Q] quadrature indices grouped by nearest
+};
+
+template <int KIND, bool CK>
+__global__ void __launch_bounds__(128) assemble_nearest_kernel(NearestArgs na) {
+    const AsmArgs &a = na.a;
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;  // force point
+    if (j >= a.N) return;
+    const int b = na.grp_off[j], e = na.grp_off[j + 1];
+    const bool cplx = CK || a.imu_im != 0.0;
+    for (int64_t i = blockIdx.y; i < a.M; i += gridDim.y) {
+        const double tx = a.tg[3 * i], ty = a.tg[3 * i + 1], tz = a.tg[3 * i + 2];
+        double G[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, Gi[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        for (int m = b; m < e; m++) {
+            const int k = na.grp_idx[m];
+            const double ek = a.eps[k];
+            double g[9], gi[9];
+            block_f64<KIND, CK>(tx, ty, tz, a.src[3 * k], a.src[3 * k + 1], a.src[3 * k + 2], ek * ek, a.are, a.aim,
+                                g, gi);
+            for (int q = 0; q < 9; q++) {
+                G[q] += g[q];
+                Gi[q] += gi[q];
+            }
+        }
+        store_block(a, i, 3 * j, G, Gi, cplx);
+    }
+}
+
+// ---- grouping of quadrature points by nearest force point -------------------
+__global__ void group_count_kernel(const int64_t *nearest, int64_t Q, int64_t nf, int *counts, int *bad) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= Q) return;
+    const int64_t j = nearest[k];
+    if (j < 0 || j >= nf) {
+        atomicExch(bad, 1);
+        return;
+    }
+    atomicAdd(&counts[j], 1);
+}
+
+// single-block exclusive scan of n ints (loops over 1024-element chunks)
+__global__ void scan_small_kernel(const int *in, int *out, int64_t n) {
+    __shared__ int sm[1024];
+    __shared__ int carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int64_t base = 0; base < n; base += 1024) {
+        const int64_t i = base + threadIdx.x;
+        const int v = i < n ? in[i] : 0;
+        sm[threadIdx.x] = v;
+        __syncthreads();
+        for (int w = 1; w < 1024; w <<= 1) {
+            int t = (int)threadIdx.x >= w ? sm[threadIdx.x - w] : 0;
+            __syncthreads();
+            sm[threadIdx.x] += t;
+            __syncthreads();
+        }
+        if (i < n) out[i] = carry + sm[threadIdx.x] - v;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry += sm[1023];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[n] = carry;
+}
+
+__global__ void group_scatter_kernel(const int64_t *nearest, int64_t Q, int64_t nf, const int *off, int *cursor,
+                                     int *idx) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= Q) return;
+    const int64_t j = nearest[k];
+    if (j < 0 || j >= nf) return;
+    idx[off[j] + atomicAdd(&cursor[j], 1)] = (int)k;
+}
+
+__global__ void group_sort_kernel(const int *off, int64_t nf, int *idx) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nf) return;
+    const int b = off[j], e = off[j + 1];
+    for (int k = b + 1; k < e; k++) {
+        int v = idx[k], m = k - 1;
+        while (m >= b && idx[m] > v) {
+            idx[m + 1] = idx[m];
+            m--;
+        }
+        idx[m + 1] = v;
+    }
+}
+
+// ---- swimmer rows / columns (swimming.py:90-99) ------------------------------
+struct SwimArgs {
+    const double *x;
+    int64_t N;
+    double x0[3];
+    const double *X;
+    const int64_t *nearest;
+    int64_t Q;
+    void *A;
+    int out_type;
+    int64_t ld;
+};
+
+__device__ __forceinline__ void put(const SwimArgs &s, int64_t r, int64_t c, double v) {
+    if (s.out_type == FLG_F64) ((double *)s.A)[r * s.ld + c] = v;
+    else ((float *)s.A)[r * s.ld + c] = (float)v;
+}
+
+// thread per force point m: its 3 rows of the [-I | r x] columns, and its
+// 3 columns of the net-force / net-torque rows
+__global__ void swimmer_kernel(SwimArgs s) {
+    const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t n3 = 3 * s.N;
+    if (m < s.N) {
+        const double r0 = s.x[3 * m] - s.x0[0], r1 = s.x[3 * m + 1] - s.x0[1], r2 = s.x[3 * m + 2] - s.x0[2];
+        // cross matrix C(v): C @ w = v x w  (swimming.py:33-40)
+        const double C[9] = {0.0, -r2, r1, r2, 0.0, -r0, -r1, r0, 0.0};
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) {
+                put(s, 3 * m + a, n3 + b, a == b ? -1.0 : 0.0);
+                put(s, 3 * m + a, n3 + 3 + b, C[3 * a + b]);
+            }
+        // count and sum of the quadrature points of group m, ascending k
+        double cnt = 0.0, X0 = 0.0, X1 = 0.0, X2 = 0.0;
+        for (int64_t k = 0; k < s.Q; k++)
+            if (s.nearest[k] == m) {
+                cnt += 1.0;
+                X0 += s.X[3 * k];
+                X1 += s.X[3 * k + 1];
+                X2 += s.X[3 * k + 2];
+            }
+        const double D[9] = {0.0, -X2, X1, X2, 0.0, -X0, -X1, X0, 0.0};
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) {
+                put(s, n3 + a, 3 * m + b, a == b ? cnt : 0.0);
+                put(s, n3 + 3 + a, 3 * m + b, D[3 * a + b]);
+            }
+    }
+    if (m < 36) put(s, n3 + m / 6, n3 + m % 6, 0.0);
+}
+
+// ---- FP64 GEMV (row-major): warp per row ------------------------------------
+__global__ void __launch_bounds__(256) gemv_f64_kernel(int64_t nr, int64_t nc, const double *A, int64_t ld,
+                                                       const double *x, double *y) {
+    const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (row >= nr) return;
+    const double *a = A + row * ld;
+    double acc = 0.0;
+    if ((ld % 2 == 0) && (((uintptr_t)A & 15) == 0) && (((uintptr_t)x & 15) == 0)) {
+        const double2 *a2 = (const double2 *)a;
+        const double2 *x2 = (const double2 *)x;
+        const int64_t nc2 = nc / 2;
+        for (int64_t c = lane; c < nc2; c += 32) {
+            const double2 av = __ldcs(a2 + c), xv = x2[c];
+            acc = fma(av.x, xv.x, acc);
+            acc = fma(av.y, xv.y, acc);
+        }
+        if ((nc & 1) && lane == 0) acc = fma(a[nc - 1], x[nc - 1], acc);
+    } else {
+        for (int64_t c = lane; c < nc; c += 32) acc = fma(a[c], x[c], acc);
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) y[row] = acc;
+}
+
+__global__ void convert_f64_f32_kernel(int64_t nr, int64_t nc, const double *src, int64_t lds, float *dst,
+                                       int64_t ldd) {
+    const int64_t r = blockIdx.y;
+    for (int64_t rr = r; rr < nr; rr += gridDim.y)
+        for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += (int64_t)gridDim.x * blockDim.x)
+            dst[rr * ldd + c] = (float)src[rr * lds + c];
+}
+
+// ---- host side ----------------------------------------------------------------
+static int prepare(int kind, double are, double aim, double mu_re, double mu_im, int out_type, AsmArgs &a) {
+    FLG_TRY(check_kernel_args(kind, are, aim));
+    FLG_REQUIRE(!(mu_re == 0.0 && mu_im == 0.0), "mu must be non-zero");
+    FLG_REQUIRE(out_type >= FLG_F64 && out_type <= FLG_BF16, "unknown out_type %d", out_type);
+    const bool cplx = (kind == FLG_BRINKMANLET && aim != 0.0) || mu_im != 0.0;
+    FLG_REQUIRE(!cplx || out_type == FLG_C128, "a complex kernel or viscosity needs out_type FLG_C128");
+    a.are = are;
+    a.aim = aim;
+    a.scale = kind == FLG_BRINKMANLET ? 1.0 / (4.0 * kPi) : 1.0 / (8.0 * kPi);
+    const double d = mu_re * mu_re + mu_im * mu_im;
+    a.imu_re = mu_im == 0.0 ? 1.0 / mu_re : mu_re / d;
+    a.imu_im = mu_im == 0.0 ? 0.0 : -mu_im / d;
+    a.out_type = out_type;
+    return FLG_OK;
+}
+
+template <template <int, bool> class Launch, typename Arg>
+static void dispatch(int kind, bool ck, dim3 grid, int threads, cudaStream_t st, const Arg &arg) {
+    if (kind == FLG_STOKESLET) Launch<FLG_STOKESLET, false>::go(grid, threads, st, arg);
+    else if (kind == FLG_WALL) Launch<FLG_WALL, false>::go(grid, threads, st, arg);
+    else if (ck) Launch<FLG_BRINKMANLET, true>::go(grid, threads, st, arg);
+    else Launch<FLG_BRINKMANLET, false>::go(grid, threads, st, arg);
+}
+
+template <int K, bool C>
+struct LaunchAsm {
+    static void go(dim3 g, int t, cudaStream_t st, const AsmArgs &a) { assemble_kernel<K, C><<<g, t, 0, st>>>(a); }
+};
+template <int K, bool C>
+struct LaunchNearest {
+    static void go(dim3 g, int t, cudaStream_t st, const NearestArgs &a) {
+        assemble_nearest_kernel<K, C><<<g, t, 0, st>>>(a);
+    }
+};
+
+static dim3 asm_grid(int64_t M, int64_t N) {
+    return dim3((unsigned)ceil_div(N, 128), (unsigned)std::min<int64_t>(M, 65535));
+}
+
+}  // namespace flg
+
+using namespace flg;
+
+extern "C" int flg_assemble(int kind, double alpha_re, double alpha_im, const double *targets, int64_t M,
+                            const double *sources, const double *eps, int64_t N, double mu_re, double mu_im,
+                            void *out, int out_type, int64_t ld, void *stream) {
+    AsmArgs a{};
+    FLG_TRY(prepare(kind, alpha_re, alpha_im, mu_re, mu_im, out_type, a));
+    FLG_REQUIRE(M >= 0 && N >= 0, "negative sizes");
+    FLG_REQUIRE(ld >= 3 * N, "ld (%lld) < 3N (%lld)", (long long)ld, (long long)(3 * N));
+    if (M == 0 || N == 0) return FLG_OK;
+    FLG_REQUIRE(targets && sources && eps && out, "null pointer");
+    a.tg = targets;
+    a.M = M;
+    a.src = sources;
+    a.eps = eps;
+    a.N = N;
+    a.out = out;
+    a.ld = ld;
+    cudaStream_t st = as_stream(stream);
+    prof_begin(FLG_SLOT_ASSEMBLE, st);
+    dispatch<LaunchAsm>(kind, kind == FLG_BRINKMANLET && alpha_im != 0.0, asm_grid(M, N), 128, st, a);
+    FLG_LAUNCH_CHECK();
+    prof_end(FLG_SLOT_ASSEMBLE, st);
+    return FLG_OK;
+}
+
+extern "C" size_t flg_assemble_nearest_workspace(int64_t Q, int64_t n_force) {
+    CountingArena c;
+    c.take<int>(n_force + 1);  // counts / cursor
+    c.take<int>(n_force + 1);  // offsets
+    c.take<int>(Q + 1);        // grouped indices
+    c.take<int>(1);            // bad-index flag
+    return c.bytes();
+}
+
+extern "C" int flg_assemble_nearest(int kind, double alpha_re, double alpha_im, const double *targets, int64_t M,
+                                    const double *quad, const int64_t *nearest, const double *eps, int64_t Q,
+                                    int64_t n_force, double mu_re, double mu_im, void *out, int out_type, int64_t ld,
+                                    void *work, size_t work_bytes, void *stream) {
+    AsmArgs a{};
+    FLG_TRY(prepare(kind, alpha_re, alpha_im, mu_re, mu_im, out_type, a));
+    FLG_REQUIRE(out_type != FLG_BF16, "assemble_nearest writes FLG_F64, FLG_C128 or FLG_F32");
+    FLG_REQUIRE(M >= 0 && Q >= 0 && n_force >= 0, "negative sizes");
+    FLG_REQUIRE(Q < (1LL << 31) && n_force < (1LL << 31), "at most 2^31 - 1 quadrature / force points");
+    FLG_REQUIRE(ld >= 3 * n_force, "ld < 3 n_force");
+    if (M == 0 || n_force == 0) return FLG_OK;
+    FLG_REQUIRE(targets && out && (Q == 0 || (quad && nearest && eps)), "null pointer");
+    Arena ar(work, work_bytes);
+    int *counts = ar.take<int>(n_force + 1);
+    int *off = ar.take<int>(n_force + 1);
+    int *idx = ar.take<int>(Q + 1);
+    int *bad = ar.take<int>(1);
+    FLG_REQUIRE(counts && off && idx && bad, "workspace too small (%zu bytes)", work_bytes);
+    cudaStream_t st = as_stream(stream);
+    FLG_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * (n_force + 1), st));
+    FLG_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), st));
+    if (Q > 0) {
+        group_count_kernel<<<(unsigned)ceil_div(Q, 256), 256, 0, st>>>(nearest, Q, n_force, counts, bad);
+        FLG_LAUNCH_CHECK();
+    }
+    scan_small_kernel<<<1, 1024, 0, st>>>(counts, off, n_force);
+    FLG_LAUNCH_CHECK();
+    FLG_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * (n_force + 1), st));
+    if (Q > 0) {
+        group_scatter_kernel<<<(unsigned)ceil_div(Q, 256), 256, 0, st>>>(nearest, Q, n_force, off, counts, idx);
+        FLG_LAUNCH_CHECK();
+        group_sort_kernel<<<(unsigned)ceil_div(n_force, 256), 256, 0, st>>>(off, n_force, idx);
+        FLG_LAUNCH_CHECK();
+    }
+    a.tg = targets;
+    a.M = M;
+    a.src = quad;
+    a.eps = eps;
+    a.N = n_force;
+    a.out = out;
+    a.ld = ld;
+    NearestArgs na{a, off, idx};
+    prof_begin(FLG_SLOT_ASSEMBLE, st);
+    dispatch<LaunchNearest>(kind, kind == FLG_BRINKMANLET && alpha_im != 0.0, asm_grid(M, n_force), 128, st, na);
+    FLG_LAUNCH_CHECK();
+    prof_end(FLG_SLOT_ASSEMBLE, st);
+    int hbad = 0;
+    FLG_CUDA(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+    FLG_CUDA(cudaStreamSynchronize(st));
+    FLG_REQUIRE(hbad == 0, "nearest indices must lie in [0, n_force)");
+    return FLG_OK;
+}
+
+extern "C" int flg_swimmer_constraints(const double *x, int64_t N, const double *x0_host, const double *X,
+                                       const int64_t *nearest, int64_t Q, void *A, int out_type, int64_t ld,
+                                       void *stream) {
+    FLG_REQUIRE(N >= 0 && Q >= 0, "negative sizes");
+    FLG_REQUIRE(out_type == FLG_F64 || out_type == FLG_F32, "swimmer system is FLG_F64 or FLG_F32");
+    FLG_REQUIRE(ld >= 3 * N + 6, "ld < 3N + 6");
+    FLG_REQUIRE(x0_host && A && (N == 0 || x) && (Q == 0 || (X && nearest)), "null pointer");
+    SwimArgs s{x, N, {x0_host[0], x0_host[1], x0_host[2]}, X, nearest, Q, A, out_type, ld};
+    const int64_t threads = std::max<int64_t>(N, 36);
+    swimmer_kernel<<<(unsigned)ceil_div(threads, 128), 128, 0, as_stream(stream)>>>(s);
+    FLG_LAUNCH_CHECK();
+    return FLG_OK;
+}
+
+extern "C" int flg_gemv_f64(int64_t n_rows, int64_t n_cols, const double *A, int64_t ld, const double *x, double *y,
+                            void *stream) {
+    FLG_REQUIRE(n_rows >= 0 && n_cols >= 0 && ld >= n_cols, "bad GEMV shape");
+    if (n_rows == 0) return FLG_OK;
+    cudaStream_t st = as_stream(stream);
+    prof_begin(FLG_SLOT_GEMV, st);
+    gemv_f64_kernel<<<(unsigned)ceil_div(n_rows * 32, 256), 256, 0, st>>>(n_rows, n_cols, A, ld, x, y);
+    FLG_LAUNCH_CHECK();
+    prof_end(FLG_SLOT_GEMV, st);
+    return FLG_OK;
+}
+
+extern "C" int flg_convert_f64_f32(int64_t n_rows, int64_t n_cols, const double *src, int64_t lds, float *dst,
+                                   int64_t ldd, void *stream) {
+    FLG_REQUIRE(n_rows >= 0 && n_cols >= 0 && lds >= n_cols && ldd >= n_cols, "bad conversion shape");
+    if (n_rows == 0 || n_cols == 0) return FLG_OK;
+    dim3 grid((unsigned)std::min<int64_t>(ceil_div(n_cols, 256), 64), (unsigned)std::min<int64_t>(n_rows, 65535));
+    convert_f64_f32_kernel<<<grid, 256, 0, as_stream(stream)>>>(n_rows, n_cols, src, lds, dst, ldd);
+    FLG_LAUNCH_CHECK();
+    return FLG_OK;
+}

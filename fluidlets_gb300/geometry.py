@@ -1,0 +1,64 @@
+"""Point sets used to build the benchmark and test workloads.
+
+``fibonacci_sphere`` is the golden-angle spiral of the reference's
+``geometry/spheres.py:7-13``; ``cube_sphere`` its six-patch sphere (33-52).
+``spheroid`` and ``workload_*`` generate the synthetic, seeded inputs of the
+benchmark configurations.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def fibonacci_sphere(n: int, radius: float = 1.0, center=(0.0, 0.0, 0.0)) -> np.ndarray:
+    """n nearly uniform points on a sphere (golden-angle spiral), shape (n, 3)."""
+    k = np.arange(n) + 0.5
+    phi = np.arccos(1 - 2 * k / n)
+    theta = np.pi * (1 + np.sqrt(5)) * k
+    unit = np.c_[np.cos(theta) * np.sin(phi), np.sin(theta) * np.sin(phi), np.cos(phi)]
+    return radius * unit + np.asarray(center, float)
+
+
+def cube_sphere(n: int, radius: float = 1.0, center=(0.0, 0.0, 0.0)) -> np.ndarray:
+    """Six n x n cell-centred patches of the cube projected onto the sphere: 6 n^2 points."""
+    s = np.linspace(-1.0 + 1.0 / n, 1.0 - 1.0 / n, n)
+    A, B = np.meshgrid(s, s, indexing="ij")
+    A, B, one = A.ravel(), B.ravel(), np.ones(n * n)
+    faces = []
+    for axis in range(3):
+        for sign in (-1.0, 1.0):
+            cols = [A, B]
+            cols.insert(axis, sign * one)
+            faces.append(np.c_[cols[0], cols[1], cols[2]])
+    cube = np.vstack(faces)
+    unit = cube / np.linalg.norm(cube, axis=1)[:, None]
+    return radius * unit + np.asarray(center, float)
+
+
+def mean_nn_spacing(points: np.ndarray) -> float:
+    """Mean nearest-neighbour distance (k-d tree)."""
+    from scipy.spatial import cKDTree
+
+    d, _ = cKDTree(points).query(points, k=2)
+    return float(d[:, 1].mean())
+
+
+def spheroid(n: int, aspect: float, rotation: np.ndarray | None = None, center=(0.0, 0.0, 0.0)) -> np.ndarray:
+    """Prolate spheroid with semi-axes (aspect, 1, 1) from a Fibonacci lattice, rotated then shifted."""
+    p = fibonacci_sphere(n) * np.array([aspect, 1.0, 1.0])
+    if rotation is not None:
+        p = p @ np.asarray(rotation).T
+    return p + np.asarray(center, float)
+
+
+def wall_sum_workload(n_src: int = 262144, n_tgt: int = 262144, n_wall: int = 16384, eps: float = 0.01,
+                      seed: int = 0):
+    """Wall-Stokeslet sum workload: sources and targets uniform in [-1,1]^2 x [0.02,2]
+    above the wall z = 0, i.i.d. N(0,1) forces, plus n_wall targets on z = 0."""
+    rng = np.random.default_rng(seed)
+    lo, hi = [-1.0, -1.0, 0.02], [1.0, 1.0, 2.0]
+    src = rng.uniform(lo, hi, (n_src, 3))
+    tgt = rng.uniform(lo, hi, (n_tgt, 3))
+    wall = np.c_[rng.uniform(-1, 1, (n_wall, 2)), np.zeros(n_wall)]
+    f = rng.normal(size=(n_src, 3))
+    return np.r_[tgt, wall], src, f, eps

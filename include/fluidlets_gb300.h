@@ -1,0 +1,232 @@
+/*
+ * fluidlets_gb300.h -- C ABI of libfluidlets_gb300.so (GB300, sm_103a).
+ *
+ * The regularized-Stokeslet hot path of the reference package `fluidlets`
+ * (pure Python + Numba + SciPy): kernel sums, dense mobility-matrix assembly,
+ * dense LU and matrix-free GMRES for resistance and free-swimming solves.
+ *
+ * Conventions (all entry points):
+ *   - every pointer is a DEVICE pointer unless stated otherwise; the caller
+ *     owns all memory, the library never frees caller memory;
+ *   - points are (n, 3) row-major float64 ([point, component], the
+ *     reference's layout, core/assemble.py:1-5); forces/velocities likewise;
+ *     complex arrays are interleaved (re, im) float64 (numpy complex128);
+ *   - dense matrices are row-major with a leading dimension `ld` (elements);
+ *     row 3*i + a is component a of target i, column 3*j + b is component b
+ *     of source j (core/assemble.py:3-5);
+ *   - scratch memory is caller-provided: each entry point that needs any has
+ *     a *_workspace() query returning the byte count, and takes
+ *     (void* work, size_t work_bytes); a too-small workspace is FLG_ERR_INVALID;
+ *   - work is enqueued on `stream` (a cudaStream_t; NULL = legacy default
+ *     stream).  Entry points are asynchronous unless their comment says they
+ *     synchronize (the iterative solvers read scalars back every iteration);
+ *   - the return value is a status code (FLG_OK = 0).  Device code never
+ *     traps; argument errors are detected on the host before any launch.
+ *
+ * Kernel kinds mirror the reference's kernel classes:
+ *   FLG_STOKESLET      Stokeslet3D        kernels/stokeslet3d.py:53-64
+ *   FLG_WALL           WallStokeslet3D    kernels/images.py:92-104
+ *   FLG_BRINKMANLET    Brinkmanlet3D(a)   kernels/brinkmanlet3d.py:107-122
+ *                      (alpha_im != 0 is the complex-alpha extension, which
+ *                      the reference rejects at brinkmanlet3d.py:116-117)
+ */
+#ifndef FLUIDLETS_GB300_H
+#define FLUIDLETS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+#define FLG_OK 0
+#define FLG_ERR_INVALID 1        /* bad argument: Python raises ValueError   */
+#define FLG_ERR_CUDA 2           /* CUDA runtime error (see flg_last_error)  */
+#define FLG_ERR_NOT_CONVERGED 3  /* iterative solver hit maxiter: RuntimeError */
+#define FLG_ERR_SINGULAR 4       /* zero / non-finite pivot: LinAlgError     */
+#define FLG_ERR_NOMEM 5          /* request exceeds the caller's budget      */
+
+/* ---- kernel kinds, precisions, element types ---------------------------- */
+#define FLG_STOKESLET 0
+#define FLG_WALL 1
+#define FLG_BRINKMANLET 2
+
+#define FLG_PREC_FP64 0   /* plain FP64 everywhere: the drop-in path         */
+#define FLG_PREC_MIXED 1  /* FP32 far field + FP64 near field (r < 4 eps)    */
+
+#define FLG_F64 0
+#define FLG_C128 1
+#define FLG_F32 2
+#define FLG_BF16 3
+
+#define FLG_LU_TF32 0     /* tcgen05 kind::tf32, FP32 accumulate in TMEM     */
+#define FLG_LU_BF16 1     /* tcgen05 kind::f16 (bf16 operands), FP32 accum   */
+#define FLG_LU_FP32 2     /* FP32 CUDA cores (no tensor cores)               */
+
+/* ---- library ------------------------------------------------------------ */
+int flg_version(void);                          /* major*10000 + minor*100 + patch */
+const char *flg_last_error(void);               /* thread-local message of the last failure */
+
+/* ---- kernel sums --------------------------------------------------------
+ * Replaces fluidlets.evaluate (core/matvec.py:24-49) and its Numba loop
+ * _apply (core/matvec.py:10-21):  out_i = sum_j G(x_i, y_j; eps_j) f_j / mu.
+ *
+ *   targets (M,3) f64; sources (N,3) f64; eps (N,) f64 (a scalar eps is
+ *   broadcast by the caller, core/_common.py:15-18); strengths (N,3) f64, or
+ *   complex128 when strengths_complex; out (M,3) f64 or complex128 -- complex
+ *   iff strengths_complex || mu_im != 0 || alpha_im != 0 (core/_common.py:21-23).
+ *   precision FLG_PREC_FP64 follows the reference's FP64 arithmetic;
+ *   FLG_PREC_MIXED sums pairs with r >= 4 eps_j in FP32 (per-tile FP64
+ *   accumulation) and pairs with r < 4 eps_j in FP64.
+ */
+size_t flg_evaluate_workspace(int kind, int64_t M, int64_t N, int strengths_complex, double alpha_im,
+                              int precision);
+int flg_evaluate(int kind, double alpha_re, double alpha_im,
+                 const double *targets, int64_t M,
+                 const double *sources, const double *eps, int64_t N,
+                 const double *strengths, int strengths_complex,
+                 double mu_re, double mu_im,
+                 double *out, int precision,
+                 void *work, size_t work_bytes, void *stream);
+
+/* ---- dense assembly -----------------------------------------------------
+ * Replaces fluidlets.assemble (core/assemble.py:27-46) and _fill (15-24):
+ * K (3M x 3N) = G(x_i, y_j; eps_j) / mu written once, directly in out_type
+ * (FLG_F64 | FLG_C128 | FLG_F32 | FLG_BF16; complex kernels/mu need C128),
+ * row-major with leading dimension ld >= 3N.
+ */
+int flg_assemble(int kind, double alpha_re, double alpha_im,
+                 const double *targets, int64_t M,
+                 const double *sources, const double *eps, int64_t N,
+                 double mu_re, double mu_im,
+                 void *out, int out_type, int64_t ld, void *stream);
+
+/* Replaces fluidlets.assemble_nearest (core/assemble.py:68-101) and
+ * _fill_nearest (49-58): K[:, group j] = sum_{k: nearest[k] = j} G(x_i, X_k)/mu.
+ * nearest (Q,) int64 in [0, n_force).  The grouping is a deterministic
+ * segmented sum (quadrature points of a group are added in ascending k).
+ * out_type FLG_F64 | FLG_C128 | FLG_F32.  K is fully overwritten. */
+size_t flg_assemble_nearest_workspace(int64_t Q, int64_t n_force);
+int flg_assemble_nearest(int kind, double alpha_re, double alpha_im,
+                         const double *targets, int64_t M,
+                         const double *quad, const int64_t *nearest, const double *eps, int64_t Q,
+                         int64_t n_force, double mu_re, double mu_im,
+                         void *out, int out_type, int64_t ld,
+                         void *work, size_t work_bytes, void *stream);
+
+/* ---- free-swimmer system (swimming.py:66-102) ----------------------------
+ * Fills the (3N+6) x (3N+6) system of Gallagher & Smith (2018) Eq. 8 around an
+ * already assembled nearest-neighbour block A[:3N,:3N] (flg_assemble_nearest
+ * with ld = 3N+6): the -U and r x Omega columns (swimming.py:92-93) and the
+ * net-force / net-torque rows (95-99).  x (N,3) lab force points, x0 (3,)
+ * frame origin (host pointer), X (Q,3) lab quadrature points, nearest (Q,).
+ * out_type FLG_F64 | FLG_F32. */
+int flg_swimmer_constraints(const double *x, int64_t N, const double *x0_host,
+                            const double *X, const int64_t *nearest, int64_t Q,
+                            void *A, int out_type, int64_t ld, void *stream);
+
+/* ---- dense LU ------------------------------------------------------------
+ * Replaces the LU branch of fluidlets.resistance (core/solve.py:64-67,
+ * scipy.linalg.solve = LAPACK getrf/getrs) and np.linalg.solve in
+ * swimming.py:101.  Row-major A (n x n, ld), in place.
+ *
+ * flg_lu_factor_f64: right-looking blocked LU with partial pivoting
+ * (P A = L U, unit L).  ipiv (n,) int32 device array of 0-based row swaps
+ * (row k was exchanged with ipiv[k], applied in order).  info (host
+ * pointer): 0, or 1 + index of the first zero pivot (then FLG_ERR_SINGULAR).
+ * Synchronizes `stream`. */
+size_t flg_lu_factor_f64_workspace(int64_t n);
+int flg_lu_factor_f64(int64_t n, double *A, int64_t ld, int32_t *ipiv, int *info,
+                      void *work, size_t work_bytes, void *stream);
+/* Solves A X = B with the factors of flg_lu_factor_f64; B is (n x nrhs)
+ * row-major with leading dimension ldb, overwritten by X. */
+int flg_lu_solve_f64(int64_t n, int64_t nrhs, const double *LU, int64_t ld, const int32_t *ipiv,
+                     double *B, int64_t ldb, void *stream);
+
+/* Low-precision LU without pivoting for the mixed-precision path: A is FP32
+ * (n x n, ld), factored in place with tcgen05 tensor-core trailing updates
+ * (mode FLG_LU_TF32 or FLG_LU_BF16; FLG_LU_FP32 uses CUDA cores).  Only used
+ * as a preconditioner of FP64 GMRES iterative refinement, so accuracy is
+ * recovered in FP64.  info as above.  Synchronizes `stream`. */
+size_t flg_lu_factor_lowp_workspace(int64_t n, int mode);
+int flg_lu_factor_lowp(int64_t n, float *A, int64_t ld, int mode, int *info,
+                       void *work, size_t work_bytes, void *stream);
+/* x = (L U)^{-1} b in FP32 for one FP64 right-hand side (converted on the
+ * fly), result written as FP64. */
+size_t flg_lu_solve_lowp_workspace(int64_t n);
+int flg_lu_solve_lowp(int64_t n, const float *LU, int64_t ld, const double *b, double *x,
+                      void *work, size_t work_bytes, void *stream);
+
+/* ---- GMRES ---------------------------------------------------------------
+ * Restarted GMRES with the semantics of scipy.sparse.linalg.gmres as called
+ * by fluidlets.resistance (core/solve.py:68-79): rtol relative to ||b||,
+ * atol = 0, `restart` inner iterations, `maxiter` restart cycles, adaptive
+ * inner tolerance (scipy gh-8400), iteration count = number of inner
+ * iterations (callback_type "pr_norm").  Orthogonalization is classical
+ * Gram-Schmidt with one re-orthogonalization (CGS2).
+ *
+ * Matrix-free operator: A v = evaluate(kind, X, X, v, eps, mu) (n = 3N
+ * unknowns, real or complex).  precision:
+ *   FLG_PREC_FP64  plain FP64 matvec throughout;
+ *   FLG_PREC_MIXED iterative refinement: FP64 outer residual b - A x, inner
+ *                  GMRES on FLG_PREC_MIXED matvecs to inner_rtol.
+ * x (3N) in/out (initial guess; zero for the reference's behaviour).
+ * iters/outer/resid are host pointers: inner iterations, outer refinement
+ * steps, final ||b - A x|| / ||b|| (FP64 operator).  Synchronizes `stream`. */
+size_t flg_gmres_workspace(int64_t N, int restart, int is_complex, int precision);
+int flg_gmres(int kind, double alpha_re, double alpha_im,
+              const double *X, const double *eps, int64_t N,
+              double mu_re, double mu_im,
+              const double *b, double *x, int is_complex,
+              double rtol, int restart, int maxiter, int precision, double inner_rtol,
+              int *iters, int *outer, double *resid,
+              void *work, size_t work_bytes, void *stream);
+
+/* Dense GMRES-IR: solves A x = b (n x n FP64 row-major, ld) to rtol with an
+ * FP64 residual and FP64 GEMV matvecs, preconditioned (left) by the
+ * low-precision factors of flg_lu_factor_lowp (LU32, ld32).  Real only.
+ * iters = total inner iterations, outer = refinement steps. Synchronizes. */
+size_t flg_gmres_ir_dense_workspace(int64_t n, int restart);
+int flg_gmres_ir_dense(int64_t n, const double *A, int64_t ld, const float *LU32, int64_t ld32,
+                       const double *b, double *x, double rtol, int restart, int maxiter,
+                       int *iters, int *outer, double *resid,
+                       void *work, size_t work_bytes, void *stream);
+
+/* ---- dense helpers --------------------------------------------------------
+ * y = A x (FP64, row-major n_rows x n_cols, ld); used for residuals. */
+int flg_gemv_f64(int64_t n_rows, int64_t n_cols, const double *A, int64_t ld, const double *x, double *y,
+                 void *stream);
+/* dst (FP32, ldd) = (float) src (FP64, lds), n_rows x n_cols */
+int flg_convert_f64_f32(int64_t n_rows, int64_t n_cols, const double *src, int64_t lds, float *dst, int64_t ldd,
+                        void *stream);
+
+/* ---- measurement ----------------------------------------------------------
+ * Throughput microbenchmarks used as roofline denominators (FFMA FP32, DFMA
+ * FP64), in TFLOP/s, timed with CUDA events on `stream`.  Synchronizes. */
+int flg_measure_peaks(double *fp32_tflops, double *fp64_tflops, void *stream);
+
+/* Kernel timing and launch counting (measurement aid; off by default).
+ * While enabled, the library records a CUDA event pair on the launching
+ * stream around every launch of the profiled kernels below, and counts every
+ * kernel it launches.  flg_profile_enable(1) resets the records.
+ * flg_profile_read synchronizes the recorded events and returns the total
+ * milliseconds and launch count of one slot.  Process-wide state: enable it
+ * only around a measurement. */
+#define FLG_SLOT_FAR_F32 0      /* far_f32_kernel (mixed-precision far field)  */
+#define FLG_SLOT_NEAR_F64 1     /* near_f64_kernel (near field + combine)       */
+#define FLG_SLOT_SUM_F64 2      /* sum_f64_kernel (plain FP64 sum)              */
+#define FLG_SLOT_ASSEMBLE 3     /* dense assembly kernels                       */
+#define FLG_SLOT_LU_UPDATE 4    /* LU trailing updates (tensor-core GEMM)       */
+#define FLG_SLOT_LU_PANEL 5     /* LU panel / diagonal-block kernels            */
+#define FLG_SLOT_GEMV 6         /* FP64 GEMV (residuals)                        */
+#define FLG_NUM_SLOTS 8
+int flg_profile_enable(int enable);
+int flg_profile_read(int slot, double *total_ms, int64_t *launches);
+int64_t flg_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FLUIDLETS_GB300_H */

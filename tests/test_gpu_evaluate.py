@@ -1,0 +1,157 @@
+"""CUDA kernel sums vs the oracle and the reference's golden vectors."""
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import assert_close, rel_err
+
+pytestmark = pytest.mark.gpu
+
+fl = pytest.importorskip("fluidlets_gb300")
+KERNELS = {"stokeslet": fl.Stokeslet3D(), "wall": fl.WallStokeslet3D()}
+
+
+def kern(kind, alpha=0.0):
+    return fl.Brinkmanlet3D(alpha) if kind == "brinkman" else KERNELS[kind]
+
+
+@pytest.mark.parametrize("name,kind,alpha", [("stokeslet", "stokeslet", 0.0), ("wall", "wall", 0.0),
+                                             ("brinkman_0", "brinkman", 0.0), ("brinkman_0.5", "brinkman", 0.5),
+                                             ("brinkman_3", "brinkman", 3.0), ("brinkman_20", "brinkman", 20.0)])
+def test_fp64_matches_reference_golden(golden, name, kind, alpha):
+    g = golden
+    u = fl.evaluate(kern(kind, alpha), g["ev_targets"], g["ev_sources"], g["ev_forces"], g["ev_eps"])
+    assert u.dtype == np.float64 and u.shape == (33, 3)
+    assert_close(u, g[f"ev_{name}"], rtol=1e-12, atol_rel=1e-14)
+
+
+def test_legacy_matlab_vectors(legacy_kernels):
+    d = legacy_kernels
+    u = fl.evaluate(fl.Stokeslet3D(), d["targets"], d["sources"], d["strengths"], d["deltas"])
+    assert np.allclose(u, d["V_stokeslet"], rtol=1e-13, atol=1e-15)
+    u = fl.evaluate(fl.WallStokeslet3D(), d["targets"], d["sources"], d["strengths"], d["deltas"])
+    assert np.allclose(u, d["V_stokeslet"] + d["V_image"], rtol=1e-13, atol=1e-15)
+    u = fl.evaluate(fl.WallStokeslet3D(), d["wall"], d["sources"], d["strengths"], d["deltas"])
+    assert np.allclose(u, d["V_wall_total"], atol=1e-15)
+
+
+def test_complex_viscosity_and_strengths(golden):
+    g = golden
+    X, Y, F, e = g["ev_targets"], g["ev_sources"], g["ev_forces"], g["ev_eps"]
+    u = fl.evaluate(fl.Stokeslet3D(), X, Y, F, e, mu=2 - 0.5j)
+    assert u.dtype == np.complex128
+    assert_close(u, g["ev_stokeslet_mu"], rtol=1e-12, atol_rel=1e-14)
+    assert_close(fl.evaluate(fl.WallStokeslet3D(), X, Y, g["ev_forces_c"], e, mu=0.7), g["ev_wall_fc"], 1e-12, 1e-14)
+    assert_close(fl.evaluate(fl.Brinkmanlet3D(3.0), X, Y, g["ev_forces_c"], e, mu=2 - 0.5j), g["ev_brinkman_fc"],
+                 1e-12, 1e-14)
+    u = fl.evaluate(fl.Stokeslet3D(), X, Y, F, e, mu=2.0 + 0j)
+    assert u.dtype == np.complex128
+
+
+def test_wall_velocity_vanishes(golden):
+    g = golden
+    u = fl.evaluate(fl.WallStokeslet3D(), g["ev_wall_targets"], g["ev_sources"], g["ev_forces"], g["ev_eps"])
+    assert np.abs(u).max() < 1e-14
+    u = fl.evaluate(fl.WallStokeslet3D(), g["ev_wall_targets"], g["ev_sources"], g["ev_forces"], g["ev_eps"],
+                    precision="mixed")
+    assert np.abs(u).max() < 1e-14
+
+
+@pytest.mark.parametrize("alpha", [0.7 + 0.7j, 2.236 + 2.236j, 0.05 + 0.2j])
+@pytest.mark.parametrize("fc", [False, True])
+def test_complex_alpha_vs_oracle(alpha, fc):
+    rng = np.random.default_rng(5)
+    X, Y = rng.normal(size=(37, 3)), rng.normal(size=(53, 3))
+    F = rng.normal(size=(53, 3)) + (1j * rng.normal(size=(53, 3)) if fc else 0)
+    e = rng.uniform(0.05, 0.3, 53)
+    u = fl.evaluate(fl.Brinkmanlet3D(alpha), X, Y, F, e, mu=1.3)
+    ref = O.evaluate("brinkman", X, Y, F, e, mu=1.3, alpha=alpha)
+    assert u.dtype == np.complex128
+    assert_close(u, ref, rtol=1e-12, atol_rel=1e-14)
+    um = fl.evaluate(fl.Brinkmanlet3D(alpha), X, Y, F, e, mu=1.3, precision="mixed")
+    assert rel_err(um, ref) < 1e-5
+
+
+SIZES = [(1, 1), (31, 33), (33, 31), (257, 129), (1000, 3001), (4096, 255)]
+
+
+@pytest.mark.parametrize("kind,alpha", [("stokeslet", 0.0), ("wall", 0.0), ("brinkman", 1.5), ("brinkman", 12.0)])
+@pytest.mark.parametrize("M,N", SIZES)
+def test_ragged_sizes_fp64_and_mixed(kind, alpha, M, N):
+    rng = np.random.default_rng(M * 7919 + N)
+    X = np.c_[rng.uniform(-1, 1, (M, 2)), rng.uniform(0.0, 1.5, M)]
+    Y = np.c_[rng.uniform(-1, 1, (N, 2)), rng.uniform(0.01, 1.5, N)]
+    F = rng.normal(size=(N, 3))
+    e = rng.uniform(0.01, 0.08, N)
+    ref = O.evaluate(kind, X, Y, F, e, alpha=alpha)
+    k = kern(kind, alpha)
+    assert_close(fl.evaluate(k, X, Y, F, e), ref, rtol=1e-11, atol_rel=1e-13)
+    um = fl.evaluate(k, X, Y, F, e, precision="mixed")
+    assert np.linalg.norm(um - ref) / np.linalg.norm(ref) < 2e-6
+
+
+def test_self_interaction_and_near_pairs_mixed():
+    """Targets == sources (the resistance matvec): every target has its own source at r = 0."""
+    rng = np.random.default_rng(11)
+    X = fl.geometry.fibonacci_sphere(3000) if hasattr(fl, "geometry") else None
+    from fluidlets_gb300.geometry import fibonacci_sphere
+    X = fibonacci_sphere(3000) + [0, 0, 1.2]
+    F = rng.normal(size=X.shape)
+    e = 0.3 * np.sqrt(4 * np.pi / 3000)
+    for kind in ("stokeslet", "wall"):
+        ref = O.evaluate(kind, X, X, F, e)
+        assert_close(fl.evaluate(kern(kind), X, X, F, e), ref, rtol=1e-11, atol_rel=1e-13)
+        um = fl.evaluate(kern(kind), X, X, F, e, precision="mixed")
+        assert np.linalg.norm(um - ref) / np.linalg.norm(ref) < 1e-6
+
+
+def test_empty_inputs():
+    X = np.zeros((0, 3))
+    Y = np.random.default_rng(0).normal(size=(5, 3))
+    assert fl.evaluate(fl.Stokeslet3D(), X, Y, Y, 0.1).shape == (0, 3)
+    u = fl.evaluate(fl.Stokeslet3D(), Y, np.zeros((0, 3)), np.zeros((0, 3)), 0.1)
+    assert u.shape == (5, 3) and not u.any()
+
+
+def test_bad_shapes_raise():
+    with pytest.raises(ValueError):
+        fl.evaluate(fl.Stokeslet3D(), np.zeros((4, 2)), np.zeros((3, 3)), np.zeros((3, 3)), 0.1)
+    with pytest.raises(ValueError):
+        fl.Brinkmanlet3D(-1.0)
+    with pytest.raises(ValueError):
+        fl.evaluate(fl.Stokeslet3D(), np.zeros((4, 3)), np.zeros((3, 3)), np.zeros((3, 3)), 0.1, precision="fp16")
+
+
+def test_deterministic_bitwise():
+    rng = np.random.default_rng(2)
+    X, Y, F = rng.normal(size=(5000, 3)), rng.normal(size=(7000, 3)), rng.normal(size=(7000, 3))
+    Y[:, 2] = np.abs(Y[:, 2]) + 0.01
+    for prec in ("fp64", "mixed"):
+        a = fl.evaluate(fl.WallStokeslet3D(), X, Y, F, 0.02, precision=prec)
+        b = fl.evaluate(fl.WallStokeslet3D(), X, Y, F, 0.02, precision=prec)
+        assert np.array_equal(a, b)
+
+
+def test_torch_tensors_pass_through():
+    import torch
+    rng = np.random.default_rng(4)
+    X, Y, F = rng.normal(size=(100, 3)), rng.normal(size=(80, 3)), rng.normal(size=(80, 3))
+    u = fl.evaluate(fl.Stokeslet3D(), torch.tensor(X, device="cuda"), torch.tensor(Y, device="cuda"),
+                    torch.tensor(F, device="cuda"), 0.1)
+    assert isinstance(u, torch.Tensor) and u.is_cuda
+    assert_close(u.cpu().numpy(), O.evaluate("stokeslet", X, Y, F, 0.1), 1e-12, 1e-14)
+
+
+def test_config2_density_mixed_accuracy_sample():
+    """Wall-Stokeslet sum at the benchmark's source density (262,144 sources, eps = 0.01): a
+    sample of interior and on-wall targets, mixed precision vs the FP64 oracle."""
+    from fluidlets_gb300.geometry import wall_sum_workload
+    T, S, F, eps = wall_sum_workload(seed=1)
+    idx = np.r_[np.arange(0, 262144, 4096), 262144 + np.arange(0, 16384, 1024)]
+    ref = O.evaluate("wall", T[idx], S, F, eps)
+    um = fl.evaluate(fl.WallStokeslet3D(), T[idx], S, F, eps, precision="mixed")
+    interior = idx < 262144
+    assert np.linalg.norm(um[interior] - ref[interior]) / np.linalg.norm(ref[interior]) < 2e-6
+    assert np.abs(um[~interior]).max() < 1e-12
+    u64 = fl.evaluate(fl.WallStokeslet3D(), T[idx], S, F, eps)
+    assert_close(u64, ref, rtol=1e-11, atol_rel=1e-13)
