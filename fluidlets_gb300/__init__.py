@@ -8,6 +8,7 @@ in ``libfluidlets_gb300.so``.
 from .core import DENSE_MAX, SolveInfo, assemble, assemble_nearest, evaluate, nearest_neighbors, resistance
 from .kernels import Brinkmanlet3D, Kernel, Stokeslet3D, VectorKernel, WallStokeslet3D
 from .stokeslet3d import stokeslet3d_velocity
+from .swimming import SwimmerShape, SwimState, Trajectory, swim, swimming_problem
 
 __version__ = "1.0.0"
 __all__ = [
@@ -24,4 +25,9 @@ __all__ = [
     "resistance",
     "SolveInfo",
     "DENSE_MAX",
+    "SwimmerShape",
+    "SwimState",
+    "Trajectory",
+    "swimming_problem",
+    "swim",
 ]

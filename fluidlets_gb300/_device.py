@@ -43,6 +43,8 @@ def to_dev(a, dtype: torch.dtype) -> torch.Tensor:
     if isinstance(a, torch.Tensor):
         return a.to(device=dev, dtype=dtype).contiguous()
     arr = np.ascontiguousarray(np.asarray(a), dtype=torch_to_numpy(dtype))
+    if not arr.flags.writeable:
+        arr = arr.copy()
     return torch.from_numpy(arr).to(dev)
 
 

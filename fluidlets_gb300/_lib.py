@@ -36,16 +36,20 @@ SIGNATURES = {
     "flg_lu_factor_f64_workspace": (c_size_t, [c_int64]),
     "flg_lu_factor_f64": (c_int, [c_int64, _P, c_int64, _P, POINTER(c_int), _P, c_size_t, _P]),
     "flg_lu_solve_f64": (c_int, [c_int64, c_int64, _P, c_int64, _P, _P, c_int64, _P]),
+    "flg_lu_lowp_dinv_elems": (c_int64, [c_int64]),
     "flg_lu_factor_lowp_workspace": (c_size_t, [c_int64, c_int]),
-    "flg_lu_factor_lowp": (c_int, [c_int64, _P, c_int64, c_int, POINTER(c_int), _P, c_size_t, _P]),
+    "flg_lu_factor_lowp": (c_int, [c_int64, _P, c_int64, c_int, _P, POINTER(c_int), _P, c_size_t, _P]),
     "flg_lu_solve_lowp_workspace": (c_size_t, [c_int64]),
-    "flg_lu_solve_lowp": (c_int, [c_int64, _P, c_int64, _P, _P, _P, c_size_t, _P]),
+    "flg_lu_solve_lowp": (c_int, [c_int64, _P, c_int64, _P, _P, _P, _P, c_size_t, _P]),
+    "flg_tc_rank_update_workspace": (c_size_t, [c_int64, c_int64, c_int]),
+    "flg_tc_rank_update": (c_int, [_P, c_int64, _P, c_int64, _P, c_int64, c_int64, c_int64, c_int, _P, c_size_t,
+                                   _P]),
     "flg_gmres_workspace": (c_size_t, [c_int64, c_int, c_int, c_int]),
     "flg_gmres": (c_int, [c_int, c_double, c_double, _P, _P, c_int64, c_double, c_double, _P, _P, c_int,
                           c_double, c_int, c_int, c_int, c_double, POINTER(c_int), POINTER(c_int),
                           POINTER(c_double), _P, c_size_t, _P]),
     "flg_gmres_ir_dense_workspace": (c_size_t, [c_int64, c_int]),
-    "flg_gmres_ir_dense": (c_int, [c_int64, _P, c_int64, _P, c_int64, _P, _P, c_double, c_int, c_int,
+    "flg_gmres_ir_dense": (c_int, [c_int64, _P, c_int64, _P, c_int64, _P, _P, _P, c_double, c_int, c_int,
                                    POINTER(c_int), POINTER(c_int), POINTER(c_double), _P, c_size_t, _P]),
     "flg_gemv_f64": (c_int, [c_int64, c_int64, _P, c_int64, _P, _P, _P]),
     "flg_convert_f64_f32": (c_int, [c_int64, c_int64, _P, c_int64, _P, c_int64, _P]),

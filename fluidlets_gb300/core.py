@@ -222,7 +222,8 @@ def _lu_solve_dev(K: torch.Tensor, U: torch.Tensor) -> torch.Tensor:
     info = ctypes.c_int(0)
     check(L.flg_lu_factor_f64(n, dv.ptr(K), n, dv.ptr(piv), ctypes.byref(info), dv.ptr(ws), nbytes, dv.stream()),
           "LU factorization")
-    B = U.reshape(n, -1).to(torch.float64).contiguous() if not U.is_complex() else None
+    # the solve overwrites its right-hand side: always work on a copy of U
+    B = U.reshape(n, -1).to(torch.float64).clone() if not U.is_complex() else None
     if B is None:  # real matrix, complex right-hand side: two real columns
         B = torch.stack([U.real, U.imag], 1).contiguous()
         check(L.flg_lu_solve_f64(n, 2, dv.ptr(K), n, dv.ptr(piv), dv.ptr(B), 2, dv.stream()), "LU solve")
@@ -231,28 +232,43 @@ def _lu_solve_dev(K: torch.Tensor, U: torch.Tensor) -> torch.Tensor:
     return B.reshape(-1)
 
 
-def _mixed_lu_solve_dev(K: torch.Tensor, U: torch.Tensor, rtol, restart, maxiter, lu_mode):
-    """TF32/BF16 tensor-core LU of K (no pivoting) + FP64 GMRES iterative refinement."""
+def _lowp_factor_dev(K: torch.Tensor, lu_mode: str):
+    """FP32 copy of K (leading dimension padded to 32) factored without pivoting
+    on the tensor cores; returns (K32, ld32, dinv)."""
     n = K.shape[0]
     L = load()
-    K32 = torch.empty((n, n), dtype=torch.float32, device=K.device)
-    check(L.flg_convert_f64_f32(n, n, dv.ptr(K), n, dv.ptr(K32), n, dv.stream()), "convert")
+    ld32 = (n + 31) // 32 * 32
+    K32 = torch.empty((n, ld32), dtype=torch.float32, device=K.device)
+    check(L.flg_convert_f64_f32(n, n, dv.ptr(K), K.stride(0), dv.ptr(K32), ld32, dv.stream()), "convert")
+    dinv = torch.empty(L.flg_lu_lowp_dinv_elems(n), dtype=torch.float32, device=K.device)
     mode = LU_MODE[lu_mode]
     nbytes = L.flg_lu_factor_lowp_workspace(n, mode)
     ws = dv.workspace(nbytes)
     info = ctypes.c_int(0)
-    check(L.flg_lu_factor_lowp(n, dv.ptr(K32), n, mode, ctypes.byref(info), dv.ptr(ws), nbytes, dv.stream()),
-          "low-precision LU")
-    del ws
-    b = U.reshape(-1).to(torch.float64).contiguous()
+    check(L.flg_lu_factor_lowp(n, dv.ptr(K32), ld32, mode, dv.ptr(dinv), ctypes.byref(info), dv.ptr(ws), nbytes,
+                               dv.stream()), "low-precision LU")
+    return K32, ld32, dinv
+
+
+def _gmres_ir_dense_dev(K, K32, ld32, dinv, b, rtol, restart, maxiter):
+    """FP64 GMRES-IR on the dense FP64 K, preconditioned by the low-precision factors."""
+    n = K.shape[0]
+    L = load()
     x = torch.zeros_like(b)
     nbytes = L.flg_gmres_ir_dense_workspace(n, restart)
     ws = dv.workspace(nbytes)
     iters, outer, resid = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_double(0.0)
-    check(L.flg_gmres_ir_dense(n, dv.ptr(K), n, dv.ptr(K32), n, dv.ptr(b), dv.ptr(x), rtol, restart, maxiter,
-                               ctypes.byref(iters), ctypes.byref(outer), ctypes.byref(resid), dv.ptr(ws), nbytes,
-                               dv.stream()), "GMRES-IR")
+    check(L.flg_gmres_ir_dense(n, dv.ptr(K), K.stride(0), dv.ptr(K32), ld32, dv.ptr(dinv), dv.ptr(b), dv.ptr(x), rtol,
+                               restart, maxiter, ctypes.byref(iters), ctypes.byref(outer), ctypes.byref(resid),
+                               dv.ptr(ws), nbytes, dv.stream()), "GMRES-IR")
     return x, iters.value, outer.value, resid.value
+
+
+def _mixed_lu_solve_dev(K: torch.Tensor, U: torch.Tensor, rtol, restart, maxiter, lu_mode):
+    """TF32/BF16 tensor-core LU of K (no pivoting) + FP64 GMRES iterative refinement."""
+    K32, ld32, dinv = _lowp_factor_dev(K, lu_mode)
+    b = U.reshape(-1).to(torch.float64).contiguous()
+    return _gmres_ir_dense_dev(K, K32, ld32, dinv, b, rtol, restart, maxiter)
 
 
 def _gmres_dev(kernel, X, e, mu, b, rtol, restart, maxiter, precision, inner_rtol=1e-6):

@@ -1,0 +1,776 @@
+// lu.cu -- dense LU factorizations and triangular solves.
+//
+// FP64 (the drop-in for scipy.linalg.solve, core/solve.py:64-67, and
+// np.linalg.solve, swimming.py:101): right-looking blocked LU with partial
+// pivoting, row-major storage, block width kPanel = 64.
+//   panel_f64_kernel  cooperative launch over up to one CTA per SM; each CTA
+//                     keeps a slab of panel rows in shared memory; one grid
+//                     barrier per column (pivot search is a grid-wide argmax,
+//                     first index on ties as LAPACK's idamax).
+//   laswp_kernel      the panel's row swaps on the other columns.
+//   trsm_f64_kernel   U12 = L11^-1 A12.
+//   dgemm_update      A22 -= L21 U12 (FP64 CUDA cores).
+//
+// Low precision (preconditioner of FP64 GMRES-IR): blocked LU WITHOUT
+// pivoting in FP32 storage, block FLG_LU_LOWP_BLOCK = 128; the diagonal block
+// is factored by one CTA, which also writes the inverses of its L and U
+// factors (kept in `dinv` for the solves); the panels are GEMMs with those
+// inverses; the trailing update runs on the tensor cores (tc_gemm.cu) or on
+// CUDA cores (FLG_LU_FP32).
+//
+// Every spin-wait (the grid barrier) is bounded by a clock64 limit and
+// reports FLG_ERR_CUDA-style failure through a device flag instead of hanging.
+#include <cooperative_groups.h>
+
+#include <algorithm>
+
+#include "flg_common.cuh"
+
+namespace flg {
+
+constexpr int kPanel = 64;                    // FP64 LU block width
+constexpr int kNB = FLG_LU_LOWP_BLOCK;        // low-precision LU block
+constexpr long long kSpinLimit = 4000000000LL;  // ~2 s of SM clock
+
+// ---- bounded grid barrier ------------------------------------------------------
+struct GridBar {
+    unsigned int count;
+    unsigned int gen;
+    int err;   // a wait ran out
+    int info;  // 1 + first zero pivot
+};
+
+__device__ bool grid_sync(GridBar *b, unsigned nblocks) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned int *vgen = &b->gen;
+        const unsigned g = *vgen;
+        __threadfence();
+        const unsigned arrived = atomicAdd(&b->count, 1u);
+        if (arrived == nblocks - 1) {
+            atomicExch(&b->count, 0u);
+            __threadfence();
+            atomicAdd(&b->gen, 1u);
+        } else {
+            const long long t0 = clock64();
+            while (*vgen == g) {
+                if (clock64() - t0 > kSpinLimit) {
+                    atomicExch(&b->err, 1);
+                    break;
+                }
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return *(volatile int *)&b->err == 0;
+}
+
+// ---- FP64 panel ------------------------------------------------------------------
+struct PanelArgs {
+    double *A;
+    int64_t ld, n, k0;
+    int kb, rpc;
+    int32_t *ipiv;
+    GridBar *bar;
+    double *slot_val;  // [2][nblk]
+    long long *slot_row;
+    double *rowbuf;   // [2][nblk][kb]
+    double *diagbuf;  // [2][kb]
+};
+
+__global__ void __launch_bounds__(256) panel_f64_kernel(PanelArgs a) {
+    extern __shared__ double P[];  // [rpc][kb]
+    __shared__ double s_piv[kPanel];
+    __shared__ double red_v[8];
+    __shared__ long long red_r[8];
+    __shared__ long long s_p;
+    __shared__ int s_wc, s_lb;
+    const int nblk = gridDim.x, c = blockIdx.x, kb = a.kb;
+    const int64_t r0 = a.k0 + (int64_t)c * a.rpc;
+    const int nr = (int)max((int64_t)0, min((int64_t)a.rpc, a.n - r0));
+    for (int e = threadIdx.x; e < nr * kb; e += blockDim.x) {
+        const int lr = e / kb, j = e - lr * kb;
+        P[e] = a.A[(r0 + lr) * a.ld + a.k0 + j];
+    }
+    __syncthreads();
+    for (int j = 0; j < kb; j++) {
+        const int64_t g = a.k0 + j;
+        const int buf = j & 1;
+        // local argmax of |P[., j]| over rows >= g (first index on ties)
+        double best = -1.0;
+        long long brow = LLONG_MAX;
+        for (int lr = threadIdx.x; lr < nr; lr += blockDim.x) {
+            const int64_t gr = r0 + lr;
+            if (gr < g) continue;
+            const double v = fabs(P[lr * kb + j]);
+            if (v > best) {
+                best = v;
+                brow = gr;
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const double ov = __shfl_xor_sync(0xffffffffu, best, o);
+            const long long orow = __shfl_xor_sync(0xffffffffu, brow, o);
+            if (ov > best || (ov == best && orow < brow)) {
+                best = ov;
+                brow = orow;
+            }
+        }
+        if ((threadIdx.x & 31) == 0) {
+            red_v[threadIdx.x >> 5] = best;
+            red_r[threadIdx.x >> 5] = brow;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int w = 1; w < (int)(blockDim.x >> 5); w++)
+                if (red_v[w] > red_v[0] || (red_v[w] == red_v[0] && red_r[w] < red_r[0])) {
+                    red_v[0] = red_v[w];
+                    red_r[0] = red_r[w];
+                }
+            a.slot_val[buf * nblk + c] = red_v[0];
+            a.slot_row[buf * nblk + c] = red_r[0];
+            s_lb = red_r[0] == LLONG_MAX ? -1 : (int)(red_r[0] - r0);
+        }
+        __syncthreads();
+        if (s_lb >= 0)
+            for (int q = threadIdx.x; q < kb; q += blockDim.x)
+                a.rowbuf[((int64_t)buf * nblk + c) * kb + q] = P[s_lb * kb + q];
+        if (g >= r0 && g < r0 + nr)
+            for (int q = threadIdx.x; q < kb; q += blockDim.x) a.diagbuf[buf * kb + q] = P[(g - r0) * kb + q];
+        __threadfence();
+        if (!grid_sync(a.bar, nblk)) return;
+        // global argmax
+        if (threadIdx.x == 0) {
+            double bv = -1.0;
+            long long br = LLONG_MAX;
+            int wc = -1;
+            for (int q = 0; q < nblk; q++) {
+                const double v = ((volatile double *)a.slot_val)[buf * nblk + q];
+                const long long r = ((volatile long long *)a.slot_row)[buf * nblk + q];
+                if (r == LLONG_MAX) continue;
+                if (v > bv || (v == bv && r < br)) {
+                    bv = v;
+                    br = r;
+                    wc = q;
+                }
+            }
+            if (wc < 0) {  // no finite candidate: keep row g
+                br = g;
+                wc = -1;
+            }
+            s_p = br;
+            s_wc = wc;
+            if (c == 0) a.ipiv[g] = (int32_t)br;
+        }
+        __syncthreads();
+        const long long p = s_p;
+        for (int q = threadIdx.x; q < kb; q += blockDim.x)
+            s_piv[q] = s_wc >= 0 ? ((volatile double *)a.rowbuf)[((int64_t)buf * nblk + s_wc) * kb + q]
+                                 : ((volatile double *)a.diagbuf)[buf * kb + q];
+        __syncthreads();
+        if (p != g) {
+            if (p >= r0 && p < r0 + nr)
+                for (int q = threadIdx.x; q < kb; q += blockDim.x)
+                    P[(p - r0) * kb + q] = ((volatile double *)a.diagbuf)[buf * kb + q];
+            if (g >= r0 && g < r0 + nr)
+                for (int q = threadIdx.x; q < kb; q += blockDim.x) P[(g - r0) * kb + q] = s_piv[q];
+        }
+        __syncthreads();
+        const double piv = s_piv[j];
+        if (piv == 0.0 || !isfinite(piv)) {
+            if (threadIdx.x == 0) atomicCAS(&a.bar->info, 0, (int)(g + 1));
+        } else {
+            const double rp = 1.0 / piv;
+            for (int lr = threadIdx.x; lr < nr; lr += blockDim.x)
+                if (r0 + lr > g) P[lr * kb + j] *= rp;
+            __syncthreads();
+            const int w = kb - j - 1;
+            for (int e = threadIdx.x; e < nr * w; e += blockDim.x) {
+                const int lr = e / w, q = j + 1 + (e - lr * w);
+                if (r0 + lr > g) P[lr * kb + q] = fma(-P[lr * kb + j], s_piv[q], P[lr * kb + q]);
+            }
+        }
+        __syncthreads();
+    }
+    for (int e = threadIdx.x; e < nr * kb; e += blockDim.x) {
+        const int lr = e / kb, j = e - lr * kb;
+        a.A[(r0 + lr) * a.ld + a.k0 + j] = P[e];
+    }
+}
+
+// row swaps of rows k0 .. k0+kb-1 on columns [c0, c1)
+__global__ void laswp_kernel(double *A, int64_t ld, const int32_t *ipiv, int64_t k0, int kb, int64_t c0, int64_t c1) {
+    const int64_t c = c0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= c1) return;
+    for (int q = 0; q < kb; q++) {
+        const int64_t r = k0 + q, p = ipiv[r];
+        if (p != r) {
+            const double t = A[r * ld + c];
+            A[r * ld + c] = A[p * ld + c];
+            A[p * ld + c] = t;
+        }
+    }
+}
+
+// U12 = L11^-1 A12 (unit lower L11 = A[k0:k0+64, k0:k0+64]), thread per column;
+// the column lives in registers (the panel width is always kPanel here)
+__global__ void __launch_bounds__(128) trsm_f64_kernel(double *A, int64_t ld, int64_t k0, int64_t c0, int64_t c1) {
+    __shared__ double L[kPanel][kPanel + 1];
+    for (int e = threadIdx.x; e < kPanel * kPanel; e += blockDim.x) {
+        const int r = e / kPanel, q = e - r * kPanel;
+        L[r][q] = A[(k0 + r) * ld + k0 + q];
+    }
+    const int64_t c = c0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    __syncthreads();
+    if (c >= c1) return;
+    double x[kPanel];
+#pragma unroll
+    for (int r = 0; r < kPanel; r++) {
+        double v = A[(k0 + r) * ld + c];
+#pragma unroll
+        for (int q = 0; q < r; q++) v = fma(-L[r][q], x[q], v);
+        x[r] = v;
+    }
+#pragma unroll
+    for (int r = 0; r < kPanel; r++) A[(k0 + r) * ld + c] = x[r];
+}
+
+// C (m x nc) -= L (m x kb) * U (kb x nc); FP64, 64x64 tiles, 4x4 per thread,
+// K in chunks of 16
+constexpr int DG_BK = 16;
+__global__ void __launch_bounds__(256) dgemm_update_kernel(double *C, const double *Lp, const double *Up, int64_t ld,
+                                                           int64_t m, int64_t nc, int kb) {
+    __shared__ double As[DG_BK][64];  // As[k][row]
+    __shared__ double Bs[DG_BK][64];  // Bs[k][col]
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int64_t row0 = (int64_t)blockIdx.y * 64, col0 = (int64_t)blockIdx.x * 64;
+    double acc[4][4] = {};
+    for (int k0 = 0; k0 < kb; k0 += DG_BK) {
+        for (int e = threadIdx.x; e < 64 * DG_BK; e += 256) {
+            const int r = e / DG_BK, k = e - r * DG_BK;
+            As[k][r] = (row0 + r < m && k0 + k < kb) ? Lp[(row0 + r) * ld + k0 + k] : 0.0;
+            const int k2 = e >> 6, cc = e & 63;
+            Bs[k2][cc] = (col0 + cc < nc && k0 + k2 < kb) ? Up[(int64_t)(k0 + k2) * ld + col0 + cc] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < DG_BK; k++) {
+            double av[4], bv[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++) av[i] = As[k][ty * 4 + i];
+#pragma unroll
+            for (int j = 0; j < 4; j++) bv[j] = Bs[k][tx * 4 + j];
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int j = 0; j < 4; j++) acc[i][j] = fma(av[i], bv[j], acc[i][j]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const int64_t r = row0 + ty * 4 + i;
+        if (r >= m) continue;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int64_t cc = col0 + tx * 4 + j;
+            if (cc < nc) C[r * ld + cc] -= acc[i][j];
+        }
+    }
+}
+
+// ---- FP64 triangular solves (getrs) ------------------------------------------------
+__global__ void apply_pivots_kernel(double *B, int64_t ldb, int64_t nrhs, const int32_t *ipiv, int64_t n) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nrhs) return;
+    for (int64_t r = 0; r < n; r++) {
+        const int64_t p = ipiv[r];
+        if (p != r) {
+            const double t = B[r * ldb + c];
+            B[r * ldb + c] = B[p * ldb + c];
+            B[p * ldb + c] = t;
+        }
+    }
+}
+
+// solve the diagonal block [b0, b0+bs) in place (lower unit, or upper) for each rhs column
+template <bool UPPER>
+__global__ void trsv_block_kernel(const double *LU, int64_t ld, double *B, int64_t ldb, int64_t nrhs, int64_t b0,
+                                  int bs) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nrhs) return;
+    if (!UPPER) {
+        for (int r = 0; r < bs; r++) {
+            double x = B[(b0 + r) * ldb + c];
+            for (int q = 0; q < r; q++) x = fma(-LU[(b0 + r) * ld + b0 + q], B[(b0 + q) * ldb + c], x);
+            B[(b0 + r) * ldb + c] = x;
+        }
+    } else {
+        for (int r = bs - 1; r >= 0; r--) {
+            double x = B[(b0 + r) * ldb + c];
+            for (int q = r + 1; q < bs; q++) x = fma(-LU[(b0 + r) * ld + b0 + q], B[(b0 + q) * ldb + c], x);
+            B[(b0 + r) * ldb + c] = x / LU[(b0 + r) * ld + b0 + r];
+        }
+    }
+}
+
+// B[rows r in [r0, r1)] -= LU[r, b0:b0+bs] * B[b0:b0+bs]; warp per (row, rhs)
+__global__ void trsv_update_kernel(const double *LU, int64_t ld, double *B, int64_t ldb, int64_t nrhs, int64_t b0,
+                                   int bs, int64_t r0, int64_t r1) {
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const int64_t rows = r1 - r0;
+    if (w >= rows * nrhs) return;
+    const int64_t r = r0 + w / nrhs, c = w % nrhs;
+    double acc = 0.0;
+    for (int q = lane; q < bs; q += 32) acc = fma(LU[r * ld + b0 + q], B[(b0 + q) * ldb + c], acc);
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) B[r * ldb + c] -= acc;
+}
+
+// ---- low precision (FP32) no-pivot LU ----------------------------------------------
+// One CTA factors the nb x nb diagonal block in shared memory and writes L, U
+// back plus Linv (unit lower) and Uinv (upper) to dinv.
+__global__ void __launch_bounds__(1024) diag_lowp_kernel(float *A, int64_t ld, int64_t k0, int nb, float *Linv,
+                                                         float *Uinv, int *info) {
+    extern __shared__ float sm[];
+    float *D = sm;                     // nb x nb factors
+    float *Li = sm + kNB * kNB;        // nb x nb
+    float *Ui = sm + 2 * kNB * kNB;    // nb x nb
+    __shared__ int bad;
+    if (threadIdx.x == 0) bad = 0;
+    for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+        const int r = e / nb, c = e - r * nb;
+        D[r * kNB + c] = A[(k0 + r) * ld + k0 + c];
+    }
+    __syncthreads();
+    for (int j = 0; j < nb; j++) {
+        const float piv = D[j * kNB + j];
+        const bool ok = piv != 0.0f && isfinite(piv);
+        if (!ok) {
+            if (threadIdx.x == 0 && !bad) {
+                bad = 1;
+                atomicCAS(info, 0, (int)(k0 + j + 1));
+            }
+        }
+        const float rp = ok ? 1.0f / piv : 0.0f;
+        for (int r = j + 1 + threadIdx.x; r < nb; r += blockDim.x) D[r * kNB + j] *= rp;
+        __syncthreads();
+        const int w = nb - j - 1;
+        for (int e = threadIdx.x; e < w * w; e += blockDim.x) {
+            const int r = j + 1 + e / w, c = j + 1 + e % w;
+            D[r * kNB + c] = fmaf(-D[r * kNB + j], D[j * kNB + c], D[r * kNB + c]);
+        }
+        __syncthreads();
+    }
+    // inverses: thread per column k
+    for (int k = threadIdx.x; k < nb; k += blockDim.x) {
+        // L X = I (unit lower): X[i][k] = delta - sum_{q<i} L[i][q] X[q][k]
+        for (int i = 0; i < nb; i++) {
+            float x = (i == k) ? 1.0f : 0.0f;
+            if (i > k)
+                for (int q = k; q < i; q++) x = fmaf(-D[i * kNB + q], Li[q * kNB + k], x);
+            Li[i * kNB + k] = (i < k) ? 0.0f : x;
+        }
+        // U X = I (upper): back substitution for column k
+        for (int i = nb - 1; i >= 0; i--) {
+            if (i > k) {
+                Ui[i * kNB + k] = 0.0f;
+                continue;
+            }
+            float x = (i == k) ? 1.0f : 0.0f;
+            for (int q = i + 1; q <= k; q++) x = fmaf(-D[i * kNB + q], Ui[q * kNB + k], x);
+            Ui[i * kNB + k] = x / D[i * kNB + i];
+        }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+        const int r = e / nb, c = e - r * nb;
+        A[(k0 + r) * ld + k0 + c] = D[r * kNB + c];
+        Linv[r * kNB + c] = Li[r * kNB + c];
+        Uinv[r * kNB + c] = Ui[r * kNB + c];
+    }
+}
+
+// C = alpha A B + beta C (row-major FP32, CUDA cores); 128x128 tiles, 8x8 per thread
+constexpr int SG_BM = 128, SG_BN = 128, SG_BK = 8;
+__global__ void __launch_bounds__(256) sgemm_kernel(int64_t M, int64_t N, int64_t K, float alpha, const float *A,
+                                                    int64_t lda, const float *B, int64_t ldb, float beta, float *C,
+                                                    int64_t ldc) {
+    __shared__ float As[SG_BK][SG_BM];
+    __shared__ float Bs[SG_BK][SG_BN];
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int64_t row0 = (int64_t)blockIdx.y * SG_BM, col0 = (int64_t)blockIdx.x * SG_BN;
+    float acc[8][8] = {};
+    for (int64_t k0 = 0; k0 < K; k0 += SG_BK) {
+        for (int e = threadIdx.x; e < SG_BM * SG_BK; e += 256) {
+            const int r = e / SG_BK, k = e % SG_BK;
+            As[k][r] = (row0 + r < M && k0 + k < K) ? A[(row0 + r) * lda + k0 + k] : 0.0f;
+            const int k2 = e / SG_BN, cc = e % SG_BN;
+            Bs[k2][cc] = (k0 + k2 < K && col0 + cc < N) ? B[(k0 + k2) * ldb + col0 + cc] : 0.0f;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < SG_BK; k++) {
+            float av[8], bv[8];
+#pragma unroll
+            for (int i = 0; i < 8; i++) av[i] = As[k][ty * 8 + i];
+#pragma unroll
+            for (int j = 0; j < 8; j++) bv[j] = Bs[k][tx * 8 + j];
+#pragma unroll
+            for (int i = 0; i < 8; i++)
+#pragma unroll
+                for (int j = 0; j < 8; j++) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const int64_t r = row0 + ty * 8 + i;
+        if (r >= M) continue;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const int64_t c = col0 + tx * 8 + j;
+            if (c < N) C[r * ldc + c] = alpha * acc[i][j] + (beta == 0.0f ? 0.0f : beta * C[r * ldc + c]);
+        }
+    }
+}
+
+__global__ void copy2d_f32_kernel(const float *src, int64_t lds, float *dst, int64_t ldd, int64_t rows, int64_t cols) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (int64_t r = blockIdx.y; r < rows; r += gridDim.y)
+        if (c < cols) dst[r * ldd + c] = src[r * lds + c];
+}
+
+// dst (cols x rows, ldd) = src^T (rows x cols, lds)
+__global__ void transpose_f32_kernel(const float *src, int64_t lds, float *dst, int64_t ldd, int64_t rows,
+                                     int64_t cols) {
+    __shared__ float t[32][33];
+    const int64_t r0 = (int64_t)blockIdx.y * 32, c0 = (int64_t)blockIdx.x * 32;
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const int64_t r = r0 + i, c = c0 + threadIdx.x;
+        t[i][threadIdx.x] = (r < rows && c < cols) ? src[r * lds + c] : 0.0f;
+    }
+    __syncthreads();
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const int64_t c = c0 + i, r = r0 + threadIdx.x;
+        if (c < cols && r < rows) dst[c * ldd + r] = t[threadIdx.x][i];
+    }
+}
+
+// tensor-core trailing update (tc_gemm.cu): C (m x nc, ldc) -= Lp (m x nb, ldl) * Ut^T (nc x nb)
+size_t tc_update_bytes(int64_t m, int64_t nc, int mode);
+int tc_update(float *C, int64_t ldc, const float *Lp, int64_t ldl, const float *Ut, int64_t m, int64_t nc, int mode,
+              void *work, size_t work_bytes, cudaStream_t st);
+
+static int sgemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, float alpha, const float *A, int64_t lda,
+                 const float *B, int64_t ldb, float beta, float *C, int64_t ldc) {
+    if (M == 0 || N == 0) return FLG_OK;
+    dim3 grid((unsigned)ceil_div(N, SG_BN), (unsigned)ceil_div(M, SG_BM));
+    sgemm_kernel<<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
+    FLG_LAUNCH_CHECK();
+    return FLG_OK;
+}
+
+static int copy2d(cudaStream_t st, const float *src, int64_t lds, float *dst, int64_t ldd, int64_t rows, int64_t cols) {
+    if (rows == 0 || cols == 0) return FLG_OK;
+    dim3 grid((unsigned)ceil_div(cols, 256), (unsigned)std::min<int64_t>(rows, 65535));
+    copy2d_f32_kernel<<<grid, 256, 0, st>>>(src, lds, dst, ldd, rows, cols);
+    FLG_LAUNCH_CHECK();
+    return FLG_OK;
+}
+
+// ---- low precision triangular solve with the diagonal-block inverses ------------------
+// x_blk = Dinv (nb x nb) * y_blk ; one CTA, thread per row
+__global__ void blk_apply_kernel(const float *Dinv, float *y, int64_t b0, int bs) {
+    __shared__ float yb[kNB];
+    for (int q = threadIdx.x; q < bs; q += blockDim.x) yb[q] = y[b0 + q];
+    __syncthreads();
+    for (int r = threadIdx.x; r < bs; r += blockDim.x) {
+        float acc = 0.0f;
+        for (int q = 0; q < bs; q++) acc = fmaf(Dinv[r * kNB + q], yb[q], acc);
+        y[b0 + r] = acc;
+    }
+}
+
+// y[r] -= LU[r, b0:b0+bs] * y[b0:b0+bs] for r in [r0, r1); warp per row
+__global__ void blk_update_kernel(const float *LU, int64_t ld, float *y, int64_t b0, int bs, int64_t r0, int64_t r1) {
+    const int64_t r = r0 + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (r >= r1) return;
+    float acc = 0.0f;
+    const float *row = LU + r * ld + b0;
+    for (int q = lane; q < bs; q += 32) acc = fmaf(row[q], y[b0 + q], acc);
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) y[r] -= acc;
+}
+
+__global__ void d2f_kernel(const double *a, float *b, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = (float)a[i];
+}
+__global__ void f2d_kernel(const float *a, double *b, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = (double)a[i];
+}
+
+size_t lu_solve_lowp_bytes(int64_t n) {
+    CountingArena c;
+    c.take<float>(n);
+    return c.bytes();
+}
+
+int lu_solve_lowp_apply(int64_t n, const float *LU, int64_t ld, const float *dinv, const double *b, double *x,
+                        void *work, size_t work_bytes, cudaStream_t st) {
+    Arena ar(work, work_bytes);
+    float *y = ar.take<float>(n);
+    FLG_REQUIRE(y != nullptr, "workspace too small for the low-precision solve");
+    d2f_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(b, y, n);
+    FLG_LAUNCH_CHECK();
+    const int64_t nblk = ceil_div(n, kNB);
+    const float *Linv = dinv, *Uinv = dinv + nblk * kNB * kNB;
+    for (int64_t k = 0; k < nblk; k++) {  // forward: L y = b
+        const int64_t b0 = k * kNB;
+        const int bs = (int)std::min<int64_t>(kNB, n - b0);
+        blk_apply_kernel<<<1, kNB, 0, st>>>(Linv + k * kNB * kNB, y, b0, bs);
+        FLG_LAUNCH_CHECK();
+        if (b0 + bs < n) {
+            const int64_t rows = n - b0 - bs;
+            blk_update_kernel<<<(unsigned)ceil_div(rows * 32, 256), 256, 0, st>>>(LU, ld, y, b0, bs, b0 + bs, n);
+            FLG_LAUNCH_CHECK();
+        }
+    }
+    for (int64_t k = nblk - 1; k >= 0; k--) {  // backward: U x = y
+        const int64_t b0 = k * kNB;
+        const int bs = (int)std::min<int64_t>(kNB, n - b0);
+        blk_apply_kernel<<<1, kNB, 0, st>>>(Uinv + k * kNB * kNB, y, b0, bs);
+        FLG_LAUNCH_CHECK();
+        if (b0 > 0) {
+            blk_update_kernel<<<(unsigned)ceil_div(b0 * 32, 256), 256, 0, st>>>(LU, ld, y, b0, bs, 0, b0);
+            FLG_LAUNCH_CHECK();
+        }
+    }
+    f2d_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(y, x, n);
+    FLG_LAUNCH_CHECK();
+    return FLG_OK;
+}
+
+}  // namespace flg
+
+using namespace flg;
+
+// ---- FP64 LU entry points --------------------------------------------------------------
+static int panel_geometry(int64_t m, int &nblk, int &rpc) {
+    const int sms = sm_count();
+    nblk = (int)std::max<int64_t>(1, std::min<int64_t>(sms, ceil_div(m, 32)));
+    rpc = (int)ceil_div(m, nblk);
+    return rpc <= 384 ? FLG_OK : FLG_ERR_INVALID;
+}
+
+extern "C" size_t flg_lu_factor_f64_workspace(int64_t n) {
+    CountingArena c;
+    const int nblk = sm_count();
+    c.take<GridBar>(1);
+    c.take<double>(2 * nblk);
+    c.take<long long>(2 * nblk);
+    c.take<double>((size_t)2 * nblk * kPanel);
+    c.take<double>(2 * kPanel);
+    (void)n;
+    return c.bytes();
+}
+
+extern "C" int flg_lu_factor_f64(int64_t n, double *A, int64_t ld, int32_t *ipiv, int *info, void *work,
+                                 size_t work_bytes, void *stream) {
+    FLG_REQUIRE(n >= 0 && ld >= n && info, "bad LU arguments");
+    *info = 0;
+    if (n == 0) return FLG_OK;
+    FLG_REQUIRE(A && ipiv, "null pointer");
+    int nblk0, rpc0;
+    FLG_REQUIRE(panel_geometry(n, nblk0, rpc0) == FLG_OK, "FP64 dense LU supports n <= %d (use GMRES above)",
+                sm_count() * 384);
+    cudaStream_t st = as_stream(stream);
+    Arena ar(work, work_bytes);
+    const int maxblk = sm_count();
+    GridBar *bar = ar.take<GridBar>(1);
+    double *slot_val = ar.take<double>(2 * maxblk);
+    long long *slot_row = ar.take<long long>(2 * maxblk);
+    double *rowbuf = ar.take<double>((size_t)2 * maxblk * kPanel);
+    double *diagbuf = ar.take<double>(2 * kPanel);
+    FLG_REQUIRE(diagbuf != nullptr, "workspace too small for LU (%zu bytes)", work_bytes);
+    FLG_CUDA(cudaMemsetAsync(bar, 0, sizeof(GridBar), st));
+    FLG_CUDA(cudaFuncSetAttribute(panel_f64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  384 * kPanel * (int)sizeof(double)));
+    for (int64_t k0 = 0; k0 < n; k0 += kPanel) {
+        const int kb = (int)std::min<int64_t>(kPanel, n - k0);
+        const int64_t m = n - k0;
+        int nblk, rpc;
+        panel_geometry(m, nblk, rpc);
+        int per_sm = 0;
+        const size_t smem = (size_t)rpc * kb * sizeof(double);
+        FLG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, panel_f64_kernel, 256, smem));
+        FLG_REQUIRE(per_sm * sm_count() >= nblk, "panel grid (%d CTAs) cannot be co-resident", nblk);
+        PanelArgs pa{A, ld, n, k0, kb, rpc, ipiv, bar, slot_val, slot_row, rowbuf, diagbuf};
+        void *args[] = {&pa};
+        prof_begin(FLG_SLOT_LU_PANEL, st);
+        FLG_CUDA(cudaLaunchCooperativeKernel((void *)panel_f64_kernel, dim3(nblk), dim3(256), args, smem, st));
+        count_launch();
+        prof_end(FLG_SLOT_LU_PANEL, st);
+        if (k0 > 0) {
+            laswp_kernel<<<(unsigned)ceil_div(k0, 256), 256, 0, st>>>(A, ld, ipiv, k0, kb, 0, k0);
+            FLG_LAUNCH_CHECK();
+        }
+        const int64_t c0 = k0 + kb;
+        if (c0 < n) {
+            const int64_t nc = n - c0;
+            laswp_kernel<<<(unsigned)ceil_div(nc, 256), 256, 0, st>>>(A, ld, ipiv, k0, kb, c0, n);
+            FLG_LAUNCH_CHECK();
+            trsm_f64_kernel<<<(unsigned)ceil_div(nc, 128), 128, 0, st>>>(A, ld, k0, c0, n);
+            FLG_LAUNCH_CHECK();
+            dim3 grid((unsigned)ceil_div(nc, 64), (unsigned)ceil_div(nc, 64));
+            prof_begin(FLG_SLOT_LU_UPDATE, st);
+            dgemm_update_kernel<<<grid, 256, 0, st>>>(A + c0 * ld + c0, A + c0 * ld + k0, A + k0 * ld + c0, ld, nc, nc,
+                                                      kb);
+            FLG_LAUNCH_CHECK();
+            prof_end(FLG_SLOT_LU_UPDATE, st);
+        }
+    }
+    GridBar hb;
+    FLG_CUDA(cudaMemcpyAsync(&hb, bar, sizeof(GridBar), cudaMemcpyDeviceToHost, st));
+    FLG_CUDA(cudaStreamSynchronize(st));
+    if (hb.err) {
+        set_error("LU panel barrier timed out");
+        return FLG_ERR_CUDA;
+    }
+    *info = hb.info;
+    if (hb.info) {
+        set_error("Matrix is singular (zero pivot at row %d)", hb.info - 1);
+        return FLG_ERR_SINGULAR;
+    }
+    return FLG_OK;
+}
+
+extern "C" int flg_lu_solve_f64(int64_t n, int64_t nrhs, const double *LU, int64_t ld, const int32_t *ipiv, double *B,
+                                int64_t ldb, void *stream) {
+    FLG_REQUIRE(n >= 0 && nrhs >= 0 && ld >= n && ldb >= nrhs, "bad LU solve arguments");
+    if (n == 0 || nrhs == 0) return FLG_OK;
+    cudaStream_t st = as_stream(stream);
+    apply_pivots_kernel<<<(unsigned)ceil_div(nrhs, 32), 32, 0, st>>>(B, ldb, nrhs, ipiv, n);
+    FLG_LAUNCH_CHECK();
+    const int bsz = 64;
+    for (int64_t b0 = 0; b0 < n; b0 += bsz) {
+        const int bs = (int)std::min<int64_t>(bsz, n - b0);
+        trsv_block_kernel<false><<<(unsigned)ceil_div(nrhs, 32), 32, 0, st>>>(LU, ld, B, ldb, nrhs, b0, bs);
+        FLG_LAUNCH_CHECK();
+        if (b0 + bs < n) {
+            const int64_t rows = n - b0 - bs;
+            trsv_update_kernel<<<(unsigned)ceil_div(rows * nrhs * 32, 256), 256, 0, st>>>(LU, ld, B, ldb, nrhs, b0,
+                                                                                         bs, b0 + bs, n);
+            FLG_LAUNCH_CHECK();
+        }
+    }
+    for (int64_t b0 = ((n - 1) / bsz) * bsz; b0 >= 0; b0 -= bsz) {
+        const int bs = (int)std::min<int64_t>(bsz, n - b0);
+        trsv_block_kernel<true><<<(unsigned)ceil_div(nrhs, 32), 32, 0, st>>>(LU, ld, B, ldb, nrhs, b0, bs);
+        FLG_LAUNCH_CHECK();
+        if (b0 > 0) {
+            trsv_update_kernel<<<(unsigned)ceil_div(b0 * nrhs * 32, 256), 256, 0, st>>>(LU, ld, B, ldb, nrhs, b0, bs,
+                                                                                       0, b0);
+            FLG_LAUNCH_CHECK();
+        }
+    }
+    return FLG_OK;
+}
+
+// ---- low-precision LU entry points ----------------------------------------------------
+extern "C" int64_t flg_lu_lowp_dinv_elems(int64_t n) { return 2 * ceil_div(std::max<int64_t>(n, 1), kNB) * kNB * kNB; }
+
+template <class Ar>
+static void lowp_carve(Ar &ar, int64_t n, int mode, float **U12, float **L21, float **U12T, char **tcw,
+                       size_t *tcb) {
+    *U12 = ar.template take<float>((size_t)kNB * n);
+    *L21 = ar.template take<float>((size_t)n * kNB);
+    *U12T = ar.template take<float>((size_t)n * kNB);
+    *tcb = (mode == FLG_LU_FP32) ? 0 : tc_update_bytes(n, n, mode);
+    *tcw = ar.template take<char>(*tcb);
+}
+
+extern "C" size_t flg_lu_factor_lowp_workspace(int64_t n, int mode) {
+    CountingArena c;
+    float *a, *b, *d;
+    char *w;
+    size_t t;
+    lowp_carve(c, n, mode, &a, &b, &d, &w, &t);
+    return c.bytes();
+}
+
+extern "C" int flg_lu_factor_lowp(int64_t n, float *A, int64_t ld, int mode, float *dinv, int *info, void *work,
+                                  size_t work_bytes, void *stream) {
+    FLG_REQUIRE(n >= 0 && ld >= n && info, "bad LU arguments");
+    FLG_REQUIRE(mode == FLG_LU_TF32 || mode == FLG_LU_BF16 || mode == FLG_LU_FP32, "unknown LU mode %d", mode);
+    FLG_REQUIRE(ld % 4 == 0, "ld must be a multiple of 4 (16-byte rows)");
+    *info = 0;
+    if (n == 0) return FLG_OK;
+    FLG_REQUIRE(A && dinv, "null pointer");
+    cudaStream_t st = as_stream(stream);
+    Arena ar(work, work_bytes);
+    float *U12, *L21, *U12T;
+    char *tcw;
+    size_t tcb;
+    lowp_carve(ar, n, mode, &U12, &L21, &U12T, &tcw, &tcb);
+    int *dinfo = ar.take<int>(1);
+    FLG_REQUIRE(U12 && L21 && U12T && dinfo && (tcb == 0 || tcw), "workspace too small for LU (%zu bytes)",
+                work_bytes);
+    FLG_CUDA(cudaMemsetAsync(dinfo, 0, sizeof(int), st));
+    const size_t dsmem = 3 * (size_t)kNB * kNB * sizeof(float);
+    FLG_CUDA(cudaFuncSetAttribute(diag_lowp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem));
+    const int64_t nblk = ceil_div(n, kNB);
+    float *Linv = dinv, *Uinv = dinv + nblk * kNB * kNB;
+    for (int64_t k = 0; k < nblk; k++) {
+        const int64_t k0 = k * kNB;
+        const int nb = (int)std::min<int64_t>(kNB, n - k0);
+        prof_begin(FLG_SLOT_LU_PANEL, st);
+        diag_lowp_kernel<<<1, 1024, dsmem, st>>>(A, ld, k0, nb, Linv + k * kNB * kNB, Uinv + k * kNB * kNB, dinfo);
+        FLG_LAUNCH_CHECK();
+        const int64_t c0 = k0 + nb, nr = n - c0;
+        if (nr > 0) {
+            float *A12 = A + k0 * ld + c0, *A21 = A + c0 * ld + k0, *A22 = A + c0 * ld + c0;
+            // U12 = Linv A12 ; L21 = A21 Uinv (panel GEMMs on CUDA cores)
+            FLG_TRY(sgemm(st, nb, nr, nb, 1.0f, Linv + k * kNB * kNB, kNB, A12, ld, 0.0f, U12, nr));
+            FLG_TRY(copy2d(st, U12, nr, A12, ld, nb, nr));
+            FLG_TRY(sgemm(st, nr, nb, nb, 1.0f, A21, ld, Uinv + k * kNB * kNB, kNB, 0.0f, L21, kNB));
+            FLG_TRY(copy2d(st, L21, kNB, A21, ld, nr, nb));
+            prof_end(FLG_SLOT_LU_PANEL, st);
+            prof_begin(FLG_SLOT_LU_UPDATE, st);
+            if (mode == FLG_LU_FP32 || nb < kNB) {
+                FLG_TRY(sgemm(st, nr, nr, nb, -1.0f, A21, ld, A12, ld, 1.0f, A22, ld));
+            } else {
+                dim3 tb(32, 8), tg((unsigned)ceil_div(nr, 32), (unsigned)ceil_div(nb, 32));
+                transpose_f32_kernel<<<tg, tb, 0, st>>>(U12, nr, U12T, kNB, nb, nr);
+                FLG_LAUNCH_CHECK();
+                FLG_TRY(tc_update(A22, ld, A21, ld, U12T, nr, nr, mode, tcw, tcb, st));
+            }
+            prof_end(FLG_SLOT_LU_UPDATE, st);
+        } else {
+            prof_end(FLG_SLOT_LU_PANEL, st);
+        }
+    }
+    int hinfo = 0;
+    FLG_CUDA(cudaMemcpyAsync(&hinfo, dinfo, sizeof(int), cudaMemcpyDeviceToHost, st));
+    FLG_CUDA(cudaStreamSynchronize(st));
+    *info = hinfo;
+    if (hinfo) {
+        set_error("zero or non-finite pivot at row %d in the low-precision LU", hinfo - 1);
+        return FLG_ERR_SINGULAR;
+    }
+    return FLG_OK;
+}
+
+extern "C" size_t flg_lu_solve_lowp_workspace(int64_t n) { return lu_solve_lowp_bytes(n); }
+
+extern "C" int flg_lu_solve_lowp(int64_t n, const float *LU, int64_t ld, const float *dinv, const double *b, double *x,
+                                 void *work, size_t work_bytes, void *stream) {
+    FLG_REQUIRE(n >= 0 && ld >= n, "bad solve arguments");
+    if (n == 0) return FLG_OK;
+    return lu_solve_lowp_apply(n, LU, ld, dinv, b, x, work, work_bytes, as_stream(stream));
+}

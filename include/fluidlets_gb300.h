@@ -146,18 +146,34 @@ int flg_lu_solve_f64(int64_t n, int64_t nrhs, const double *LU, int64_t ld, cons
                      double *B, int64_t ldb, void *stream);
 
 /* Low-precision LU without pivoting for the mixed-precision path: A is FP32
- * (n x n, ld), factored in place with tcgen05 tensor-core trailing updates
- * (mode FLG_LU_TF32 or FLG_LU_BF16; FLG_LU_FP32 uses CUDA cores).  Only used
- * as a preconditioner of FP64 GMRES iterative refinement, so accuracy is
- * recovered in FP64.  info as above.  Synchronizes `stream`. */
+ * (n x n, ld; ld a multiple of 4 so every row starts on a 16-byte boundary),
+ * factored in place (unit L, U) in blocks of FLG_LU_LOWP_BLOCK with the
+ * trailing updates on the tcgen05 tensor cores (mode FLG_LU_TF32 or
+ * FLG_LU_BF16; FLG_LU_FP32 uses CUDA cores).  dinv (FP32, size
+ * flg_lu_lowp_dinv_elems(n)) receives the inverses of the diagonal blocks
+ * of L and U, used by flg_lu_solve_lowp.  Only used as a preconditioner of
+ * FP64 GMRES iterative refinement, so accuracy is recovered in FP64.
+ * info as above (a zero or non-finite pivot).  Synchronizes `stream`. */
+#define FLG_LU_LOWP_BLOCK 128
+int64_t flg_lu_lowp_dinv_elems(int64_t n);
 size_t flg_lu_factor_lowp_workspace(int64_t n, int mode);
-int flg_lu_factor_lowp(int64_t n, float *A, int64_t ld, int mode, int *info,
+int flg_lu_factor_lowp(int64_t n, float *A, int64_t ld, int mode, float *dinv, int *info,
                        void *work, size_t work_bytes, void *stream);
 /* x = (L U)^{-1} b in FP32 for one FP64 right-hand side (converted on the
  * fly), result written as FP64. */
 size_t flg_lu_solve_lowp_workspace(int64_t n);
-int flg_lu_solve_lowp(int64_t n, const float *LU, int64_t ld, const double *b, double *x,
+int flg_lu_solve_lowp(int64_t n, const float *LU, int64_t ld, const float *dinv, const double *b, double *x,
                       void *work, size_t work_bytes, void *stream);
+
+/* Tensor-core rank-128 update used by the trailing updates of
+ * flg_lu_factor_lowp, exposed as a building block:
+ *   C (m x nc, FP32, ldc)  -=  A (m x 128, FP32, lda) * Bt^T,  Bt (nc x 128, FP32, ldb = 128)
+ * mode FLG_LU_TF32 (kind::tf32) or FLG_LU_BF16 (operands rounded to BF16,
+ * kind::f16); FP32 accumulation in TMEM.  A and C rows must start on 16-byte
+ * boundaries (lda, ldc multiples of 4).  Synchronizes `stream`. */
+size_t flg_tc_rank_update_workspace(int64_t m, int64_t nc, int mode);
+int flg_tc_rank_update(float *C, int64_t ldc, const float *A, int64_t lda, const float *Bt, int64_t ldb,
+                       int64_t m, int64_t nc, int mode, void *work, size_t work_bytes, void *stream);
 
 /* ---- GMRES ---------------------------------------------------------------
  * Restarted GMRES with the semantics of scipy.sparse.linalg.gmres as called
@@ -186,11 +202,11 @@ int flg_gmres(int kind, double alpha_re, double alpha_im,
 
 /* Dense GMRES-IR: solves A x = b (n x n FP64 row-major, ld) to rtol with an
  * FP64 residual and FP64 GEMV matvecs, preconditioned (left) by the
- * low-precision factors of flg_lu_factor_lowp (LU32, ld32).  Real only.
+ * low-precision factors of flg_lu_factor_lowp (LU32, ld32, dinv).  Real only.
  * iters = total inner iterations, outer = refinement steps. Synchronizes. */
 size_t flg_gmres_ir_dense_workspace(int64_t n, int restart);
 int flg_gmres_ir_dense(int64_t n, const double *A, int64_t ld, const float *LU32, int64_t ld32,
-                       const double *b, double *x, double rtol, int restart, int maxiter,
+                       const float *dinv, const double *b, double *x, double rtol, int restart, int maxiter,
                        int *iters, int *outer, double *resid,
                        void *work, size_t work_bytes, void *stream);
 
