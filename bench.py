@@ -155,6 +155,62 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def solve_section(dev, n_points=1536, reps=5):
+    """Resistance solves on the sphere workload: unit sphere, N Fibonacci points, eps = 0.25 x mean
+    nearest-neighbour spacing, U = (1, 0, 0), free-space Stokeslet, dense LU (3N unknowns).
+    Plain FP64 GPU path vs mixed precision (tensor-core LU + FP64 GMRES-IR), with a cuSOLVER
+    FP64 solve (torch.linalg.solve) of the same assembled matrix as a reference point."""
+    import torch
+
+    import fluidlets_gb300 as fl
+    from fluidlets_gb300.core import _assemble_dev
+    from fluidlets_gb300.geometry import fibonacci_sphere, mean_nn_spacing
+
+    X = fibonacci_sphere(n_points)
+    eps = 0.25 * mean_nn_spacing(X)
+    Xd = torch.from_numpy(X).to(dev)
+    U = torch.zeros_like(Xd)
+    U[:, 0] = 1.0
+    ed = torch.full((n_points,), eps, dtype=torch.float64, device=dev)
+    kern = fl.Stokeslet3D()
+
+    def timed(fn):
+        out = fn()  # warm-up
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            out = fn()
+            torch.cuda.synchronize()
+            ms.append(1e3 * (time.perf_counter() - t0))
+        ms = np.array(ms)
+        return out, {"solves_per_s": float(1e3 / ms.mean()), "ms_mean": float(ms.mean()),
+                     "p50_ms": float(np.percentile(ms, 50)), "p99_ms": float(np.percentile(ms, 99))}
+
+    (F64, i64), t64 = timed(lambda: fl.resistance(kern, Xd, U, ed, method="lu"))
+    res = {"workload": f"resistance, free Stokeslet, unit sphere N={n_points} Fibonacci, eps={eps:.6f} "
+                       f"(0.25 x mean NN spacing), U=(1,0,0), dense LU on {3 * n_points} unknowns",
+           "fp64_gpu": dict(t64, residual=i64.residual),
+           "drag_over_6pi_a": float(F64[:, 0].sum().item() / (6 * np.pi))}
+    for lu in ("tf32", "bf16"):
+        (Fm, im), tm = timed(lambda: fl.resistance(kern, Xd, U, ed, method="lu", precision="mixed", lu=lu))
+        err = float(torch.linalg.vector_norm(Fm - F64) / torch.linalg.vector_norm(F64))
+        res[f"mixed_{lu}"] = dict(tm, rel_force_err_vs_fp64=err, residual=im.residual, ir_steps=im.ir_steps,
+                                  gmres_iterations=im.iterations, speedup_vs_fp64=t64["ms_mean"] / tm["ms_mean"])
+
+    def cusolver():
+        K = _assemble_dev(kern, Xd, Xd, ed, 1.0)
+        return torch.linalg.solve(K, U.reshape(-1))
+
+    _, tc = timed(cusolver)
+    res["cusolver_fp64_reference_point"] = tc
+    res["fp64_baseline_for_speedup"] = "fp64_gpu" if t64["ms_mean"] <= tc["ms_mean"] else "cusolver_fp64_reference_point"
+    base = min(t64["ms_mean"], tc["ms_mean"])
+    for lu in ("tf32", "bf16"):
+        res[f"mixed_{lu}"]["speedup_vs_faster_fp64"] = base / res[f"mixed_{lu}"]["ms_mean"]
+    return res
+
+
 def run_ours(args):
     import torch
 
@@ -284,6 +340,7 @@ def run_ours(args):
         line["fp64_gpu_path"] = {"value": fp64_rate, "unit": "pairs/s",
                                  "sample": f"{len(idx)} targets x {N_SRC} sources",
                                  "mixed_speedup": value / world / fp64_rate}
+        line["solves"] = solve_section(dev)
         rate, threads, sample = cpu_sample_rate(T, S, F, eps, args.cpu_sample)
         line["cpu_baseline"] = {"value": rate, "unit": "pairs/s", "cores": threads, "kind": "port",
                                 "sample": sample}
