@@ -26,6 +26,9 @@ SIGNATURES = {
     "flg_evaluate_workspace": (c_size_t, [c_int, c_int64, c_int64, c_int, c_double, c_int]),
     "flg_evaluate": (c_int, [c_int, c_double, c_double, _P, c_int64, _P, _P, c_int64, _P, c_int, c_double,
                              c_double, _P, c_int, _P, c_size_t, _P]),
+    "flg_evaluate_noalloc_max_bytes": (c_size_t, []),
+    "flg_evaluate_noalloc": (c_int, [c_int, c_double, c_double, _P, c_int64, _P, _P, c_int64, _P, c_int, c_double,
+                                     c_double, _P, _P]),
     "flg_assemble": (c_int, [c_int, c_double, c_double, _P, c_int64, _P, _P, c_int64, c_double, c_double, _P,
                              c_int, c_int64, _P]),
     "flg_assemble_nearest_workspace": (c_size_t, [c_int64, c_int64]),

@@ -17,6 +17,7 @@
 // still fill the 152 SMs; the per-split partial sums go to workspace and are
 // combined in a fixed order (bitwise deterministic results).
 #include <algorithm>
+#include <mutex>
 
 #include "flg_common.cuh"
 #include "pair_math.cuh"
@@ -814,4 +815,89 @@ extern "C" int flg_evaluate(int kind, double alpha_re, double alpha_im, const do
     r.out = out;
     r.out_complex = (strengths_complex || ck || mu_im != 0.0) ? 1 : 0;
     return sum_run(r, L, precision, &p, st);
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free FP64 sum (flg_evaluate_noalloc).
+//
+// Some callers cannot allocate device memory at all: a host application that
+// reserves the whole GPU for its own memory pool at start-up, or a plug-in
+// running inside a framework that forbids cudaMalloc once it is running.
+// They cannot provide the workspace flg_evaluate asks for either, so this
+// variant keeps the only scratch the FP64 sum needs -- the per-split partial
+// sums -- in the fixed-size device array below.  The array exists once per
+// GPU that loads the library and stays allocated until the process exits.
+// ---------------------------------------------------------------------------
+constexpr size_t kNoAllocScratchBytes = size_t(16) << 20;  // 16 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void *g_noalloc_addr[kMaxDevices] = {};
+}  // namespace
+
+// Device address of g_noalloc_scratch on the current device.  In host code the
+// array's name is only a host-side stand-in, so the address is looked up once
+// per device (with that device current) and cached.
+static int noalloc_scratch(void **addr) {
+    int dev = 0;
+    FLG_CUDA(cudaGetDevice(&dev));
+    FLG_REQUIRE(dev >= 0 && dev < kMaxDevices, "device ordinal %d out of range", dev);
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (g_noalloc_addr[dev] == nullptr) {
+        void *p = nullptr;
+        FLG_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        g_noalloc_addr[dev] = p;
+    }
+    *addr = g_noalloc_addr[dev];
+    return FLG_OK;
+}
+
+extern "C" size_t flg_evaluate_noalloc_max_bytes(void) { return kNoAllocScratchBytes; }
+
+extern "C" int flg_evaluate_noalloc(int kind, double alpha_re, double alpha_im, const double *targets, int64_t M,
+                                    const double *sources, const double *eps, int64_t N, const double *strengths,
+                                    int strengths_complex, double mu_re, double mu_im, double *out, void *stream) {
+    FLG_TRY(check_kernel_args(kind, alpha_re, alpha_im));
+    FLG_REQUIRE(M >= 0 && N >= 0, "negative sizes M=%lld N=%lld", (long long)M, (long long)N);
+    FLG_REQUIRE(M < (1LL << 31) && N < (1LL << 31), "at most 2^31 - 1 targets and sources");
+    FLG_REQUIRE(!(mu_re == 0.0 && mu_im == 0.0), "mu must be non-zero");
+    const bool ck = kind == FLG_BRINKMANLET && alpha_im != 0.0;
+    const int nf = strengths_complex ? 2 : 1;
+    SumLayout L;
+    sum_layout(kind, M, N, nf, ck, FLG_PREC_FP64, L);
+    // one partial sum per (split, target): shrink the number of source splits
+    // until they fit the fixed array; one split is the minimum
+    const size_t per_split = (size_t)M * L.outw * sizeof(double);
+    FLG_REQUIRE(per_split <= kNoAllocScratchBytes,
+                "flg_evaluate_noalloc: %lld targets need %zu bytes of scratch, more than its fixed %zu; "
+                "use flg_evaluate with a workspace",
+                (long long)M, per_split, kNoAllocScratchBytes);
+    if (M == 0) return FLG_OK;
+    FLG_REQUIRE(targets && out, "null targets/out");
+    FLG_REQUIRE(N == 0 || (sources && eps && strengths), "null sources/eps/strengths");
+    if (N > 0 && (size_t)L.S * per_split > kNoAllocScratchBytes) {
+        const int64_t smax = (int64_t)(kNoAllocScratchBytes / per_split);
+        L.split_len = ceil_div(ceil_div(N, smax), kF64Tile) * kF64Tile;
+        L.S = ceil_div(N, L.split_len);
+    }
+    SumPlan p{};
+    FLG_TRY(noalloc_scratch((void **)&p.partial));
+    SumRun r{};
+    r.kind = kind;
+    r.tg = targets;
+    r.M = M;
+    r.src = sources;
+    r.eps = eps;
+    r.f = strengths;
+    r.N = N;
+    r.alpha_re = alpha_re;
+    r.alpha_im = alpha_im;
+    r.mu_re = mu_re;
+    r.mu_im = mu_im;
+    r.out = out;
+    r.out_complex = (strengths_complex || ck || mu_im != 0.0) ? 1 : 0;
+    // every partial that is read is written earlier in the same call: nothing to clear
+    return sum_run(r, L, FLG_PREC_FP64, &p, as_stream(stream));
 }

@@ -91,6 +91,29 @@ int flg_evaluate(int kind, double alpha_re, double alpha_im,
                  double *out, int precision,
                  void *work, size_t work_bytes, void *stream);
 
+/* Allocation-free variant of flg_evaluate, FLG_PREC_FP64 only.  No
+ * counterpart in the reference: it exists for callers that cannot allocate
+ * device memory at all -- a host application that reserves the whole GPU for
+ * its own memory pool at start-up, or a plug-in whose framework forbids
+ * cudaMalloc once it is running -- and so cannot provide the workspace of
+ * flg_evaluate either.  It calls no cudaMalloc, cudaFree or other allocating
+ * routine: its scratch (the per-split partial sums) is a fixed array of
+ * flg_evaluate_noalloc_max_bytes() = 16 MiB of device memory that every GPU
+ * loading the library holds until the process exits.  Limit: the targets
+ * must satisfy M * 24 bytes (real output) or M * 48 bytes (complex) <= 16 MiB,
+ * i.e. M <= 699,050 real / 349,525 complex; larger M returns FLG_ERR_INVALID.
+ * The first call on each device looks up the array's device address (with
+ * that device current); make that first call before any stream capture.
+ * All calls share the one array, so calls whose work overlaps on the GPU
+ * (different streams, or different host threads) race: serialize them. */
+size_t flg_evaluate_noalloc_max_bytes(void);
+int flg_evaluate_noalloc(int kind, double alpha_re, double alpha_im,
+                         const double *targets, int64_t M,
+                         const double *sources, const double *eps, int64_t N,
+                         const double *strengths, int strengths_complex,
+                         double mu_re, double mu_im,
+                         double *out, void *stream);
+
 /* ---- dense assembly -----------------------------------------------------
  * Replaces fluidlets.assemble (core/assemble.py:27-46) and _fill (15-24):
  * K (3M x 3N) = G(x_i, y_j; eps_j) / mu written once, directly in out_type
