@@ -91,6 +91,6 @@ struct CountingArena {
 
 inline cudaStream_t as_stream(void *s) { return (cudaStream_t)s; }
 
-inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+__host__ __device__ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
 }  // namespace flg

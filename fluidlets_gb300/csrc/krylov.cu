@@ -282,7 +282,7 @@ struct Gmres {
         std::vector<double> gc(m);
         std::vector<H> gs(m);
         std::vector<T> hbuf(2 * (m + 2) + 2);
-        bool have_r = false;
+        bool have_r = false, r_is_b = false;
         for (int it = 0; it < maxiter; it++) {
             if (it == 0) {
                 int nz = 0;
@@ -296,6 +296,7 @@ struct Gmres {
                     FLG_TRY(residual(b, x));
                 } else {
                     FLG_CUDA(cudaMemcpyAsync(r, b, sizeof(T) * n, cudaMemcpyDeviceToDevice, st));
+                    r_is_b = true;
                 }
                 double rn0;
                 FLG_TRY(norm(r, &rn0));
@@ -306,8 +307,12 @@ struct Gmres {
                 have_r = true;
             }
             (void)have_r;
-            // v0 = M^-1 r / ||M^-1 r||
-            FLG_TRY(precond(r, V));
+            // v0 = M^-1 r / ||M^-1 r||  (r == b on the first cycle from x = 0: M^-1 b is in tmp)
+            if (it == 0 && M && r_is_b) {
+                FLG_CUDA(cudaMemcpyAsync(V, tmp, sizeof(T) * n, cudaMemcpyDeviceToDevice, st));
+            } else {
+                FLG_TRY(precond(r, V));
+            }
             double tmpn;
             FLG_TRY(norm(V, &tmpn));
             if (tmpn == 0.0) {  // r = 0 exactly: x solves the system

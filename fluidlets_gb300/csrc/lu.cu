@@ -33,34 +33,36 @@ constexpr int kNB = FLG_LU_LOWP_BLOCK;        // low-precision LU block
 constexpr long long kSpinLimit = 4000000000LL;  // ~2 s of SM clock
 
 // ---- bounded grid barrier ------------------------------------------------------
+// One atomic per CTA: CTA 0 adds 2^31 - (nblocks - 1), every other CTA adds 1,
+// so once all have arrived the counter has grown by exactly 2^31 and its top
+// bit has flipped (no reset needed between barriers); waiters spin on an
+// acquire load until the bit flips, for at most kSpinLimit cycles.
 struct GridBar {
     unsigned int count;
-    unsigned int gen;
+    unsigned int pad;
     int err;   // a wait ran out
     int info;  // 1 + first zero pivot
 };
 
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
 __device__ bool grid_sync(GridBar *b, unsigned nblocks) {
     __syncthreads();
     if (threadIdx.x == 0) {
-        volatile unsigned int *vgen = &b->gen;
-        const unsigned g = *vgen;
-        __threadfence();
-        const unsigned arrived = atomicAdd(&b->count, 1u);
-        if (arrived == nblocks - 1) {
-            atomicExch(&b->count, 0u);
-            __threadfence();
-            atomicAdd(&b->gen, 1u);
-        } else {
-            const long long t0 = clock64();
-            while (*vgen == g) {
-                if (clock64() - t0 > kSpinLimit) {
-                    atomicExch(&b->err, 1);
-                    break;
-                }
+        const unsigned inc = (blockIdx.x == 0) ? (0x80000000u - (nblocks - 1)) : 1u;
+        unsigned old;
+        asm volatile("atom.add.release.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(&b->count), "r"(inc) : "memory");
+        const long long t0 = clock64();
+        while (((old ^ ld_acquire_u32(&b->count)) & 0x80000000u) == 0) {
+            if (clock64() - t0 > kSpinLimit) {
+                atomicExch(&b->err, 1);
+                break;
             }
         }
-        __threadfence();
     }
     __syncthreads();
     return *(volatile int *)&b->err == 0;
@@ -330,66 +332,247 @@ __global__ void trsv_update_kernel(const double *LU, int64_t ld, double *B, int6
 }
 
 // ---- low precision (FP32) no-pivot LU ----------------------------------------------
-// One CTA factors the nb x nb diagonal block in shared memory and writes L, U
-// back plus Linv (unit lower) and Uinv (upper) to dinv.
-__global__ void __launch_bounds__(1024) diag_lowp_kernel(float *A, int64_t ld, int64_t k0, int nb, float *Linv,
-                                                         float *Uinv, int *info) {
+// One CTA factors the nb x nb diagonal block (nb <= 128, padded with the
+// identity to 128) in shared memory, blocked in 32 x 32 sub-blocks:
+//   per sub-block step s: warp 0 factors D[s][s]; warps solve the panels
+//   U[s][t] = L[s][s]^-1 D[s][t] and L[t][s] = D[t][s] U[s][s]^-1; all threads
+//   update the trailing sub-blocks.
+// Then the inverses of L (unit lower) and U (upper) by block recursion:
+//   diagonal 32 x 32 inverses by single warps, off-diagonal blocks level by
+//   level:  Linv[t][s] = -Linv[t][t] sum_{q=s}^{t-1} L[t][q] Linv[q][s],
+//           Uinv[s][t] = -Uinv[s][s] sum_{q=s+1}^{t} U[s][q] Uinv[q][t].
+// L, U go back to A; Linv, Uinv (full 128 x 128) to dinv.
+constexpr int kSB = 32;          // sub-block
+constexpr int kNS = kNB / kSB;   // sub-blocks per side (4)
+constexpr int kPD = kNB + 1;     // padded shared-memory row stride
+constexpr size_t kDiagSmem = (3 * (size_t)kNB * kPD + 2 * (kNS - 1) * kSB * kSB) * sizeof(float);
+
+__global__ void __launch_bounds__(512) diag_lowp_kernel(float *A, int64_t ld, int64_t k0, int nb, float *Linv,
+                                                        float *Uinv, int *info) {
     extern __shared__ float sm[];
-    float *D = sm;                     // nb x nb factors
-    float *Li = sm + kNB * kNB;        // nb x nb
-    float *Ui = sm + 2 * kNB * kNB;    // nb x nb
-    __shared__ int bad;
-    if (threadIdx.x == 0) bad = 0;
-    for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
-        const int r = e / nb, c = e - r * nb;
-        D[r * kNB + c] = A[(k0 + r) * ld + k0 + c];
+    float *D = sm, *Li = sm + kNB * kPD, *Ui = sm + 2 * kNB * kPD, *T = sm + 3 * kNB * kPD;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, nthr = blockDim.x, nwarp = nthr >> 5;
+    for (int e = tid; e < kNB * kNB; e += nthr) {
+        const int r = e / kNB, c = e - r * kNB;
+        D[r * kPD + c] = (r < nb && c < nb) ? A[(k0 + r) * ld + k0 + c] : (r == c ? 1.0f : 0.0f);
+        Li[r * kPD + c] = 0.0f;
+        Ui[r * kPD + c] = 0.0f;
     }
     __syncthreads();
-    for (int j = 0; j < nb; j++) {
-        const float piv = D[j * kNB + j];
-        const bool ok = piv != 0.0f && isfinite(piv);
-        if (!ok) {
-            if (threadIdx.x == 0 && !bad) {
-                bad = 1;
-                atomicCAS(info, 0, (int)(k0 + j + 1));
-            }
+    // ---- phase A: right-looking LU without pivoting over the whole block.
+    // Thread t owns two 4 x 4 tiles in registers: tile rows/cols (tr, tc) with
+    // tc = t % 32 and tr = t / 32 and t / 32 + 16.  Step j: the owners of
+    // column j form the multipliers (pivot row j published in shared memory by
+    // the previous step) and publish them; every thread updates its tiles; the
+    // owners of row j + 1 publish it.  Two barriers per column.
+    {
+        __shared__ float rowj[2][kNB], colj[kNB];
+        float a[2][4][4];
+        const int tc = tid & 31;
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int tr = (tid >> 5) + 16 * h;
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int c = 0; c < 4; c++) a[h][i][c] = D[(4 * tr + i) * kPD + 4 * tc + c];
         }
-        const float rp = ok ? 1.0f / piv : 0.0f;
-        for (int r = j + 1 + threadIdx.x; r < nb; r += blockDim.x) D[r * kNB + j] *= rp;
+        if (tid < kNB) rowj[0][tid] = D[tid];  // row 0
         __syncthreads();
-        const int w = nb - j - 1;
-        for (int e = threadIdx.x; e < w * w; e += blockDim.x) {
-            const int r = j + 1 + e / w, c = j + 1 + e % w;
-            D[r * kNB + c] = fmaf(-D[r * kNB + j], D[j * kNB + c], D[r * kNB + c]);
+        for (int j = 0; j < kNB; j++) {
+            const float *rj = rowj[j & 1];
+            const float piv = rj[j];
+            const bool ok = piv != 0.0f && isfinite(piv);
+            if (!ok && tid == 0 && j < nb) atomicCAS(info, 0, (int)(k0 + j + 1));
+            const float rp = ok ? 1.0f / piv : 0.0f;
+            // owners of column j: multipliers for rows below j
+            if (tc == (j >> 2)) {
+                const int cc = j & 3;
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const int tr = (tid >> 5) + 16 * h;
+#pragma unroll
+                    for (int i = 0; i < 4; i++) {
+                        const int r = 4 * tr + i;
+                        float v = cc == 0 ? a[h][i][0] : cc == 1 ? a[h][i][1] : cc == 2 ? a[h][i][2] : a[h][i][3];
+                        if (r > j) {
+                            v *= rp;
+                            if (cc == 0) a[h][i][0] = v;
+                            else if (cc == 1) a[h][i][1] = v;
+                            else if (cc == 2) a[h][i][2] = v;
+                            else a[h][i][3] = v;
+                        }
+                        colj[r] = (r > j) ? v : 0.0f;
+                    }
+                }
+            }
+            __syncthreads();
+            // rank-1 update of the trailing part: a[r][c] -= l_r u_c for r > j, c > j
+            float u[4];
+#pragma unroll
+            for (int c = 0; c < 4; c++) u[c] = (4 * tc + c > j) ? rj[4 * tc + c] : 0.0f;
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int tr = (tid >> 5) + 16 * h;
+                if (4 * tr + 3 <= j) continue;
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    const float l = colj[4 * tr + i];
+#pragma unroll
+                    for (int c = 0; c < 4; c++) a[h][i][c] = fmaf(-l, u[c], a[h][i][c]);
+                }
+            }
+            // publish row j + 1 (final after this update) into the other buffer
+            if (j + 1 < kNB) {
+                const int r = j + 1, tr_need = r >> 2, i = r & 3;
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    if ((tid >> 5) + 16 * h == tr_need) {
+#pragma unroll
+                        for (int c = 0; c < 4; c++) {
+                            const float v = i == 0 ? a[h][0][c] : i == 1 ? a[h][1][c] : i == 2 ? a[h][2][c] : a[h][3][c];
+                            rowj[(j + 1) & 1][4 * tc + c] = v;
+                        }
+                    }
+                }
+            }
+            __syncthreads();
+        }
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int tr = (tid >> 5) + 16 * h;
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int c = 0; c < 4; c++) D[(4 * tr + i) * kPD + 4 * tc + c] = a[h][i][c];
         }
         __syncthreads();
     }
-    // inverses: thread per column k
-    for (int k = threadIdx.x; k < nb; k += blockDim.x) {
-        // L X = I (unit lower): X[i][k] = delta - sum_{q<i} L[i][q] X[q][k]
-        for (int i = 0; i < nb; i++) {
-            float x = (i == k) ? 1.0f : 0.0f;
-            if (i > k)
-                for (int q = k; q < i; q++) x = fmaf(-D[i * kNB + q], Li[q * kNB + k], x);
-            Li[i * kNB + k] = (i < k) ? 0.0f : x;
-        }
-        // U X = I (upper): back substitution for column k
-        for (int i = nb - 1; i >= 0; i--) {
-            if (i > k) {
-                Ui[i * kNB + k] = 0.0f;
-                continue;
+    // ---- phase B: inverses; diagonal sub-blocks first (warp per block, lane = column)
+    for (int task = warp; task < 2 * kNS; task += nwarp) {
+        const int o = (task % kNS) * kSB, c = lane;
+        if (task < kNS) {  // unit lower: X[i][c] = delta - sum_{c<=q<i} L[i][q] X[q][c]
+            for (int i = 0; i < kSB; i++) {
+                float v = (i == c) ? 1.0f : 0.0f;
+                if (i > c) {
+#pragma unroll 4
+                    for (int q = c; q < i; q++) v = fmaf(-D[(o + i) * kPD + o + q], Li[(o + q) * kPD + o + c], v);
+                }
+                Li[(o + i) * kPD + o + c] = (i < c) ? 0.0f : v;
             }
-            float x = (i == k) ? 1.0f : 0.0f;
-            for (int q = i + 1; q <= k; q++) x = fmaf(-D[i * kNB + q], Ui[q * kNB + k], x);
-            Ui[i * kNB + k] = x / D[i * kNB + i];
+        } else {  // upper, bottom up
+            for (int ii = kSB - 1; ii >= 0; ii--) {
+                float v = 0.0f;
+                if (ii <= c) {
+                    v = (ii == c) ? 1.0f : 0.0f;
+#pragma unroll 4
+                    for (int q = ii + 1; q <= c; q++) v = fmaf(-D[(o + ii) * kPD + o + q], Ui[(o + q) * kPD + o + c], v);
+                    v = v / D[(o + ii) * kPD + o + ii];
+                }
+                Ui[(o + ii) * kPD + o + c] = v;
+            }
         }
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
-        const int r = e / nb, c = e - r * nb;
-        A[(k0 + r) * ld + k0 + c] = D[r * kNB + c];
-        Linv[r * kNB + c] = Li[r * kNB + c];
-        Uinv[r * kNB + c] = Ui[r * kNB + c];
+    for (int d = 1; d < kNS; d++) {
+        const int npair = kNS - d;  // pairs (s, s + d), for Linv and for Uinv
+        // T = sum_q L[t][q] Linv[q][s]   |   T = sum_q U[s][q] Uinv[q][t]
+        for (int e = tid; e < 2 * npair * kSB * kSB; e += nthr) {
+            const int p = e / (kSB * kSB), i = (e / kSB) % kSB, j = e % kSB;
+            const bool lower = p < npair;
+            const int s = lower ? p : p - npair, t = s + d;
+            float acc = 0.0f;
+            if (lower) {
+                for (int q = s * kSB; q < t * kSB; q++) acc = fmaf(D[(t * kSB + i) * kPD + q], Li[q * kPD + s * kSB + j], acc);
+            } else {
+                for (int q = (s + 1) * kSB; q < (t + 1) * kSB; q++)
+                    acc = fmaf(D[(s * kSB + i) * kPD + q], Ui[q * kPD + t * kSB + j], acc);
+            }
+            T[p * kSB * kSB + i * kSB + j] = acc;
+        }
+        __syncthreads();
+        // Linv[t][s] = -Linv[t][t] T   |   Uinv[s][t] = -Uinv[s][s] T
+        for (int e = tid; e < 2 * npair * kSB * kSB; e += nthr) {
+            const int p = e / (kSB * kSB), i = (e / kSB) % kSB, j = e % kSB;
+            const bool lower = p < npair;
+            const int s = lower ? p : p - npair, t = s + d;
+            float acc = 0.0f;
+            const float *Tp = T + p * kSB * kSB;
+            if (lower) {
+                for (int k = 0; k < kSB; k++) acc = fmaf(Li[(t * kSB + i) * kPD + t * kSB + k], Tp[k * kSB + j], acc);
+                Li[(t * kSB + i) * kPD + s * kSB + j] = -acc;
+            } else {
+                for (int k = 0; k < kSB; k++) acc = fmaf(Ui[(s * kSB + i) * kPD + s * kSB + k], Tp[k * kSB + j], acc);
+                Ui[(s * kSB + i) * kPD + t * kSB + j] = -acc;
+            }
+        }
+        __syncthreads();
+    }
+    for (int e = tid; e < kNB * kNB; e += nthr) {
+        const int r = e / kNB, c = e - r * kNB;
+        if (r < nb && c < nb) A[(k0 + r) * ld + k0 + c] = D[r * kPD + c];
+        Linv[r * kNB + c] = Li[r * kPD + c];
+        Uinv[r * kNB + c] = Ui[r * kPD + c];
+    }
+}
+
+// Panels of one LU step, in place, in one launch (CTA x < ntu: U tiles, else L tiles):
+//   U12[:, 32-col tile] = Linv (128 x 128) * A12[:, tile]  (all 128 rows per CTA; also
+//                         written transposed into Ut (nr x 128, K-major) for the tensor cores)
+//   L21[32-row tile, :] = A21[tile, :] * Uinv (128 x 128)  (all 128 columns per CTA)
+// Each CTA reads its whole input tile before writing it back, so in place is safe.
+__global__ void __launch_bounds__(256) lowp_panel_kernel(float *A, int64_t ld, int64_t k0, int64_t nr,
+                                                         const float *Linv, const float *Uinv, float *Ut, int ntu) {
+    __shared__ float tile[kNB][33];  // U: [row][col]; L: stored as [col][row]
+    const int64_t c0 = k0 + kNB;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    if ((int)blockIdx.x < ntu) {
+        const int64_t j0 = (int64_t)blockIdx.x * 32;
+        const int cols = (int)min((int64_t)32, nr - j0);
+        for (int e = t; e < kNB * 32; e += 256) {
+            const int r = e >> 5, c = e & 31;
+            tile[r][c] = c < cols ? A[(k0 + r) * ld + c0 + j0 + c] : 0.0f;
+        }
+        __syncthreads();
+        float acc[16];
+#pragma unroll
+        for (int k = 0; k < 16; k++) acc[k] = 0.0f;
+        for (int q = 0; q < kNB; q++) {
+            const float b = tile[q][lane];
+#pragma unroll
+            for (int k = 0; k < 16; k++) acc[k] = fmaf(Linv[(w + 8 * k) * kNB + q], b, acc[k]);
+        }
+        if (lane < cols) {
+#pragma unroll
+            for (int k = 0; k < 16; k++) {
+                const int r = w + 8 * k;
+                A[(k0 + r) * ld + c0 + j0 + lane] = acc[k];
+                Ut[(j0 + lane) * kNB + r] = acc[k];
+            }
+        }
+    } else {
+        const int64_t i0 = (int64_t)(blockIdx.x - ntu) * 32;
+        const int rows = (int)min((int64_t)32, nr - i0);
+        for (int e = t; e < 32 * kNB; e += 256) {
+            const int r = e >> 7, c = e & (kNB - 1);
+            tile[c][r] = r < rows ? A[(c0 + i0 + r) * ld + k0 + c] : 0.0f;
+        }
+        __syncthreads();
+        // thread: column c = t % 128, rows r = t / 128 + 2 k
+        const int c = t & (kNB - 1), rb = t >> 7;
+        float acc[16];
+#pragma unroll
+        for (int k = 0; k < 16; k++) acc[k] = 0.0f;
+        for (int q = 0; q < kNB; q++) {
+            const float u = Uinv[q * kNB + c];
+#pragma unroll
+            for (int k = 0; k < 16; k++) acc[k] = fmaf(tile[q][rb + 2 * k], u, acc[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < 16; k++) {
+            const int r = rb + 2 * k;
+            if (r < rows) A[(c0 + i0 + r) * ld + k0 + c] = acc[k];
+        }
     }
 }
 
@@ -462,7 +645,7 @@ __global__ void transpose_f32_kernel(const float *src, int64_t lds, float *dst, 
 // tensor-core trailing update (tc_gemm.cu): C (m x nc, ldc) -= Lp (m x nb, ldl) * Ut^T (nc x nb)
 size_t tc_update_bytes(int64_t m, int64_t nc, int mode);
 int tc_update(float *C, int64_t ldc, const float *Lp, int64_t ldl, const float *Ut, int64_t m, int64_t nc, int mode,
-              void *work, size_t work_bytes, cudaStream_t st);
+              void *work, size_t work_bytes, cudaStream_t st, int *err_dev);
 
 static int sgemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, float alpha, const float *A, int64_t lda,
                  const float *B, int64_t ldb, float beta, float *C, int64_t ldc) {
@@ -482,28 +665,105 @@ static int copy2d(cudaStream_t st, const float *src, int64_t lds, float *dst, in
 }
 
 // ---- low precision triangular solve with the diagonal-block inverses ------------------
-// x_blk = Dinv (nb x nb) * y_blk ; one CTA, thread per row
-__global__ void blk_apply_kernel(const float *Dinv, float *y, int64_t b0, int bs) {
-    __shared__ float yb[kNB];
-    for (int q = threadIdx.x; q < bs; q += blockDim.x) yb[q] = y[b0 + q];
-    __syncthreads();
-    for (int r = threadIdx.x; r < bs; r += blockDim.x) {
-        float acc = 0.0f;
-        for (int q = 0; q < bs; q++) acc = fmaf(Dinv[r * kNB + q], yb[q], acc);
-        y[b0 + r] = acc;
-    }
+// x = U^-1 L^-1 b for one right-hand side, FP32 factors, in ONE cooperative
+// launch: for each 128-row block b (forward, then backward) every CTA forms
+// x_b = Dinv_b y_b in shared memory (a 128 x 128 matvec, recomputed per CTA
+// instead of communicated), CTA 0 stores it, and the CTAs share out the rows
+// still to be updated, y[r] -= LU[r, block b] x_b (a warp per row); one bounded
+// grid barrier separates the blocks.
+struct ApplyArgs {
+    const float *LU;
+    int64_t ld, n;
+    const float *Linv, *Uinv;
+    float *y;  // working right-hand side (n)
+    float *z;  // solution blocks (n)
+    GridBar *bar;
+};
+
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
 }
 
-// y[r] -= LU[r, b0:b0+bs] * y[b0:b0+bs] for r in [r0, r1); warp per row
-__global__ void blk_update_kernel(const float *LU, int64_t ld, float *y, int64_t b0, int bs, int64_t r0, int64_t r1) {
-    const int64_t r = r0 + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    const int lane = threadIdx.x & 31;
-    if (r >= r1) return;
-    float acc = 0.0f;
-    const float *row = LU + r * ld + b0;
-    for (int q = lane; q < bs; q += 32) acc = fmaf(row[q], y[b0 + q], acc);
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0) y[r] -= acc;
+// stage one 128 x 128 block inverse into shared memory (asynchronous)
+__device__ __forceinline__ void stage_dinv(float *dst, const float *src) {
+    for (int e = threadIdx.x * 4; e < kNB * kNB; e += blockDim.x * 4) cp_async16(dst + e, src + e);
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+__global__ void __launch_bounds__(256) lowp_apply_kernel(ApplyArgs a) {
+    extern __shared__ float4 dyn4[];
+    float *Dbuf = (float *)dyn4;  // 2 x 128 x 128
+    __shared__ float yb[kNB], xb[kNB];
+    const int nblk = (int)ceil_div(a.n, kNB);
+    const int nwarp_tot = gridDim.x * (blockDim.x >> 5);
+    const int gwarp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    const int total = 2 * nblk;
+    // step t: forward block t (t < nblk), backward block 2 nblk - 1 - t
+    auto dinv_of = [&](int t) {
+        const int k = t < nblk ? t : 2 * nblk - 1 - t;
+        return (t < nblk ? a.Linv : a.Uinv) + (int64_t)k * kNB * kNB;
+    };
+    stage_dinv(Dbuf, dinv_of(0));
+    for (int t = 0; t < total; t++) {
+        const bool fwd = t < nblk;
+        const int k = fwd ? t : 2 * nblk - 1 - t;
+        const int64_t b0 = (int64_t)k * kNB;
+        const int bs = (int)min((int64_t)kNB, a.n - b0);
+        const float *src = fwd ? a.y : a.z;  // backward pass reads the forward result
+        for (int q = threadIdx.x; q < bs; q += blockDim.x) yb[q] = ((volatile float *)src)[b0 + q];
+        if (t + 1 < total) {
+            stage_dinv(Dbuf + ((t + 1) & 1) * kNB * kNB, dinv_of(t + 1));
+            asm volatile("cp.async.wait_group 1;" ::: "memory");
+        } else {
+            asm volatile("cp.async.wait_group 0;" ::: "memory");
+        }
+        __syncthreads();
+        const float *Dk = Dbuf + (t & 1) * kNB * kNB;
+        for (int r = threadIdx.x >> 5; r < bs; r += blockDim.x >> 5) {  // warp per row
+            float acc = 0.0f;
+            for (int q = lane; q < bs; q += 32) acc = fmaf(Dk[r * kNB + q], yb[q], acc);
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0) xb[r] = acc;
+        }
+        __syncthreads();
+        if (blockIdx.x == 0)
+            for (int q = threadIdx.x; q < bs; q += blockDim.x) (fwd ? a.z : a.y)[b0 + q] = xb[q];
+        // rows still to update: below (forward) / above (backward); a row may be
+        // updated by different CTAs in different steps, so bypass L1
+        const int64_t r0 = fwd ? b0 + bs : 0, r1 = fwd ? a.n : b0;
+        volatile float *tgt = fwd ? a.y : a.z;
+        // four rows per warp at a time, all loads issued before the reductions
+        for (int64_t rb = r0 + 4 * (int64_t)gwarp; rb < r1; rb += 4 * (int64_t)nwarp_tot) {
+            float v[4][4];
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const int64_t r = rb + i;
+                const float *row = a.LU + (r < r1 ? r : rb) * a.ld + b0;
+#pragma unroll
+                for (int c = 0; c < 4; c++) {
+                    const int q = lane + 32 * c;
+                    v[i][c] = (q < bs) ? row[q] : 0.0f;
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                float acc = 0.0f;
+#pragma unroll
+                for (int c = 0; c < 4; c++) {
+                    const int q = lane + 32 * c;
+                    acc = fmaf(v[i][c], q < bs ? xb[q] : 0.0f, acc);
+                }
+                for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+                // fire-and-forget reduction (RED): one update per row and step, steps ordered by the barrier
+                if (lane == 0 && rb + i < r1) atomicAdd((float *)&tgt[rb + i], -acc);
+            }
+        }
+        if (!grid_sync(a.bar, gridDim.x)) {
+            asm volatile("cp.async.wait_group 0;" ::: "memory");
+            return;
+        }
+    }
 }
 
 __global__ void d2f_kernel(const double *a, float *b, int64_t n) {
@@ -518,6 +778,8 @@ __global__ void f2d_kernel(const float *a, double *b, int64_t n) {
 size_t lu_solve_lowp_bytes(int64_t n) {
     CountingArena c;
     c.take<float>(n);
+    c.take<float>(n);
+    c.take<GridBar>(1);
     return c.bytes();
 }
 
@@ -525,32 +787,26 @@ int lu_solve_lowp_apply(int64_t n, const float *LU, int64_t ld, const float *din
                         void *work, size_t work_bytes, cudaStream_t st) {
     Arena ar(work, work_bytes);
     float *y = ar.take<float>(n);
-    FLG_REQUIRE(y != nullptr, "workspace too small for the low-precision solve");
+    float *z = ar.take<float>(n);
+    GridBar *bar = ar.take<GridBar>(1);
+    FLG_REQUIRE(y && z && bar, "workspace too small for the low-precision solve");
     d2f_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(b, y, n);
     FLG_LAUNCH_CHECK();
+    FLG_CUDA(cudaMemsetAsync(bar, 0, sizeof(GridBar), st));
     const int64_t nblk = ceil_div(n, kNB);
-    const float *Linv = dinv, *Uinv = dinv + nblk * kNB * kNB;
-    for (int64_t k = 0; k < nblk; k++) {  // forward: L y = b
-        const int64_t b0 = k * kNB;
-        const int bs = (int)std::min<int64_t>(kNB, n - b0);
-        blk_apply_kernel<<<1, kNB, 0, st>>>(Linv + k * kNB * kNB, y, b0, bs);
-        FLG_LAUNCH_CHECK();
-        if (b0 + bs < n) {
-            const int64_t rows = n - b0 - bs;
-            blk_update_kernel<<<(unsigned)ceil_div(rows * 32, 256), 256, 0, st>>>(LU, ld, y, b0, bs, b0 + bs, n);
-            FLG_LAUNCH_CHECK();
-        }
-    }
-    for (int64_t k = nblk - 1; k >= 0; k--) {  // backward: U x = y
-        const int64_t b0 = k * kNB;
-        const int bs = (int)std::min<int64_t>(kNB, n - b0);
-        blk_apply_kernel<<<1, kNB, 0, st>>>(Uinv + k * kNB * kNB, y, b0, bs);
-        FLG_LAUNCH_CHECK();
-        if (b0 > 0) {
-            blk_update_kernel<<<(unsigned)ceil_div(b0 * 32, 256), 256, 0, st>>>(LU, ld, y, b0, bs, 0, b0);
-            FLG_LAUNCH_CHECK();
-        }
-    }
+    ApplyArgs aa{LU, ld, n, dinv, dinv + nblk * kNB * kNB, y, z, bar};
+    const size_t smem = 2 * (size_t)kNB * kNB * sizeof(float);
+    FLG_CUDA(cudaFuncSetAttribute(lowp_apply_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    FLG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lowp_apply_kernel, 256, smem));
+    FLG_REQUIRE(per_sm >= 1, "preconditioner kernel does not fit on an SM");
+    const int grid = sm_count();
+    void *args[] = {&aa};
+    prof_begin(FLG_SLOT_LU_SOLVE, st);
+    FLG_CUDA(cudaLaunchCooperativeKernel((void *)lowp_apply_kernel, dim3(grid), dim3(256), args, smem, st));
+    count_launch();
+    prof_end(FLG_SLOT_LU_SOLVE, st);
+    // after the backward pass the solution is in y
     f2d_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(y, x, n);
     FLG_LAUNCH_CHECK();
     return FLG_OK;
@@ -701,6 +957,7 @@ extern "C" size_t flg_lu_factor_lowp_workspace(int64_t n, int mode) {
     char *w;
     size_t t;
     lowp_carve(c, n, mode, &a, &b, &d, &w, &t);
+    c.take<int>(2);
     return c.bytes();
 }
 
@@ -718,11 +975,11 @@ extern "C" int flg_lu_factor_lowp(int64_t n, float *A, int64_t ld, int mode, flo
     char *tcw;
     size_t tcb;
     lowp_carve(ar, n, mode, &U12, &L21, &U12T, &tcw, &tcb);
-    int *dinfo = ar.take<int>(1);
+    int *dinfo = ar.take<int>(2);  // [0] first bad pivot, [1] tensor-core wait timed out
     FLG_REQUIRE(U12 && L21 && U12T && dinfo && (tcb == 0 || tcw), "workspace too small for LU (%zu bytes)",
                 work_bytes);
-    FLG_CUDA(cudaMemsetAsync(dinfo, 0, sizeof(int), st));
-    const size_t dsmem = 3 * (size_t)kNB * kNB * sizeof(float);
+    FLG_CUDA(cudaMemsetAsync(dinfo, 0, 2 * sizeof(int), st));
+    const size_t dsmem = kDiagSmem;
     FLG_CUDA(cudaFuncSetAttribute(diag_lowp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem));
     const int64_t nblk = ceil_div(n, kNB);
     float *Linv = dinv, *Uinv = dinv + nblk * kNB * kNB;
@@ -730,34 +987,43 @@ extern "C" int flg_lu_factor_lowp(int64_t n, float *A, int64_t ld, int mode, flo
         const int64_t k0 = k * kNB;
         const int nb = (int)std::min<int64_t>(kNB, n - k0);
         prof_begin(FLG_SLOT_LU_PANEL, st);
-        diag_lowp_kernel<<<1, 1024, dsmem, st>>>(A, ld, k0, nb, Linv + k * kNB * kNB, Uinv + k * kNB * kNB, dinfo);
+        diag_lowp_kernel<<<1, 512, dsmem, st>>>(A, ld, k0, nb, Linv + k * kNB * kNB, Uinv + k * kNB * kNB, dinfo);
         FLG_LAUNCH_CHECK();
         const int64_t c0 = k0 + nb, nr = n - c0;
         if (nr > 0) {
             float *A12 = A + k0 * ld + c0, *A21 = A + c0 * ld + k0, *A22 = A + c0 * ld + c0;
-            // U12 = Linv A12 ; L21 = A21 Uinv (panel GEMMs on CUDA cores)
-            FLG_TRY(sgemm(st, nb, nr, nb, 1.0f, Linv + k * kNB * kNB, kNB, A12, ld, 0.0f, U12, nr));
-            FLG_TRY(copy2d(st, U12, nr, A12, ld, nb, nr));
-            FLG_TRY(sgemm(st, nr, nb, nb, 1.0f, A21, ld, Uinv + k * kNB * kNB, kNB, 0.0f, L21, kNB));
-            FLG_TRY(copy2d(st, L21, kNB, A21, ld, nr, nb));
+            if (nb == kNB) {
+                // U12 = Linv A12 (+ its K-major copy U12T), L21 = A21 Uinv: one launch, in place
+                const int ntu = (int)ceil_div(nr, 32), ntl = (int)ceil_div(nr, 32);
+                lowp_panel_kernel<<<ntu + ntl, 256, 0, st>>>(A, ld, k0, nr, Linv + k * kNB * kNB,
+                                                             Uinv + k * kNB * kNB, U12T, ntu);
+                FLG_LAUNCH_CHECK();
+            } else {  // (only reachable for a partial last block, which has no trailing part)
+                FLG_TRY(sgemm(st, nb, nr, nb, 1.0f, Linv + k * kNB * kNB, kNB, A12, ld, 0.0f, U12, nr));
+                FLG_TRY(copy2d(st, U12, nr, A12, ld, nb, nr));
+                FLG_TRY(sgemm(st, nr, nb, nb, 1.0f, A21, ld, Uinv + k * kNB * kNB, kNB, 0.0f, L21, kNB));
+                FLG_TRY(copy2d(st, L21, kNB, A21, ld, nr, nb));
+            }
             prof_end(FLG_SLOT_LU_PANEL, st);
             prof_begin(FLG_SLOT_LU_UPDATE, st);
             if (mode == FLG_LU_FP32 || nb < kNB) {
                 FLG_TRY(sgemm(st, nr, nr, nb, -1.0f, A21, ld, A12, ld, 1.0f, A22, ld));
             } else {
-                dim3 tb(32, 8), tg((unsigned)ceil_div(nr, 32), (unsigned)ceil_div(nb, 32));
-                transpose_f32_kernel<<<tg, tb, 0, st>>>(U12, nr, U12T, kNB, nb, nr);
-                FLG_LAUNCH_CHECK();
-                FLG_TRY(tc_update(A22, ld, A21, ld, U12T, nr, nr, mode, tcw, tcb, st));
+                FLG_TRY(tc_update(A22, ld, A21, ld, U12T, nr, nr, mode, tcw, tcb, st, dinfo + 1));
             }
             prof_end(FLG_SLOT_LU_UPDATE, st);
         } else {
             prof_end(FLG_SLOT_LU_PANEL, st);
         }
     }
-    int hinfo = 0;
-    FLG_CUDA(cudaMemcpyAsync(&hinfo, dinfo, sizeof(int), cudaMemcpyDeviceToHost, st));
+    int hflags[2] = {0, 0};
+    FLG_CUDA(cudaMemcpyAsync(hflags, dinfo, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
     FLG_CUDA(cudaStreamSynchronize(st));
+    if (hflags[1]) {
+        set_error("tensor-core update: an mbarrier wait timed out");
+        return FLG_ERR_CUDA;
+    }
+    const int hinfo = hflags[0];
     *info = hinfo;
     if (hinfo) {
         set_error("zero or non-finite pivot at row %d in the low-precision LU", hinfo - 1);

@@ -268,14 +268,18 @@ size_t tc_update_bytes(int64_t m, int64_t nc, int mode) {
     return c.bytes();
 }
 
+// err_dev: device flag raised on a timed-out wait.  When null, the flag lives in
+// the workspace and the call synchronizes to check it; the LU passes its own
+// flag and checks it once at the end of the factorization.
 int tc_update(float *C, int64_t ldc, const float *Lp, int64_t ldl, const float *Ut, int64_t m, int64_t nc, int mode,
-              void *work, size_t work_bytes, cudaStream_t st) {
+              void *work, size_t work_bytes, cudaStream_t st, int *err_dev) {
     FLG_REQUIRE(mode == FLG_LU_TF32 || mode == FLG_LU_BF16, "tensor-core mode must be TF32 or BF16");
     FLG_REQUIRE(m >= 0 && nc >= 0 && m < (1LL << 31) && nc < (1LL << 31), "bad tensor-core update shape");
     if (m == 0 || nc == 0) return FLG_OK;
     Arena ar(work, work_bytes);
-    int *err = ar.take<int>(1);
-    FLG_REQUIRE(err != nullptr, "workspace too small for the tensor-core update");
+    int *own = ar.take<int>(1);
+    int *err = err_dev ? err_dev : own;
+    FLG_REQUIRE(err != nullptr && own != nullptr, "workspace too small for the tensor-core update");
     CUtensorMap ma, mb;
     if (mode == FLG_LU_TF32) {
         FLG_TRY(make_map(&ma, Lp, m, ldl, mode));
@@ -291,7 +295,7 @@ int tc_update(float *C, int64_t ldc, const float *Lp, int64_t ldl, const float *
         FLG_TRY(make_map(&ma, La, m, TC_K, mode));
         FLG_TRY(make_map(&mb, Ub, nc, TC_K, mode));
     }
-    FLG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
+    if (!err_dev) FLG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
     const size_t smem = tc_smem_bytes();
     dim3 grid((unsigned)ceil_div(nc, TC_BN), (unsigned)ceil_div(m, TC_BM));
     FLG_REQUIRE(grid.y <= 65535, "too many row tiles");
@@ -305,6 +309,7 @@ int tc_update(float *C, int64_t ldc, const float *Lp, int64_t ldl, const float *
         tc_update_kernel<FLG_LU_BF16><<<grid, TC_THREADS, smem, st>>>(ma, mb, C, ldc, (int)m, (int)nc, err);
     }
     FLG_LAUNCH_CHECK();
+    if (err_dev) return FLG_OK;
     int herr = 0;
     FLG_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
     FLG_CUDA(cudaStreamSynchronize(st));
@@ -322,5 +327,5 @@ extern "C" int flg_tc_rank_update(float *C, int64_t ldc, const float *A, int64_t
                                   int64_t m, int64_t nc, int mode, void *work, size_t work_bytes, void *stream) {
     FLG_REQUIRE(ldb == flg::TC_K, "Bt must be compact (ldb == 128)");
     FLG_REQUIRE(lda >= flg::TC_K && ldc >= nc, "bad leading dimensions");
-    return flg::tc_update(C, ldc, A, lda, Bt, m, nc, mode, work, work_bytes, flg::as_stream(stream));
+    return flg::tc_update(C, ldc, A, lda, Bt, m, nc, mode, work, work_bytes, flg::as_stream(stream), nullptr);
 }

@@ -16,7 +16,7 @@ import torch
 
 def main(argv=None):
     p = argparse.ArgumentParser()
-    p.add_argument("op", choices=["sum", "assemble", "lu", "resistance"])
+    p.add_argument("op", choices=["sum", "assemble", "lu", "resistance", "breakdown"])
     p.add_argument("--kind", default="wall", choices=["stokeslet", "wall", "brinkman"])
     p.add_argument("--alpha", type=complex, default=0.0)
     p.add_argument("--targets", type=int, default=65536)
@@ -39,6 +39,8 @@ def main(argv=None):
         for _ in range(a.reps):
             fl.evaluate(kern, Td, Sd, Fd, eps, precision=a.precision)
         torch.cuda.synchronize()
+    elif a.op == "breakdown":
+        breakdown(a, kern)
     else:
         X = fibonacci_sphere(a.n) + (np.array([0, 0, 1.5]) if a.kind == "wall" else 0)
         eps = 0.25 * mean_nn_spacing(X)
@@ -55,6 +57,52 @@ def main(argv=None):
                 core.resistance(kern, Xd, U, eps, precision=a.precision, lu=a.lu)
             torch.cuda.synchronize()
             print(f"{a.op} n={a.n}: {1e3 * (time.perf_counter() - t0):.2f} ms")
+
+
+def breakdown(a, kern):
+    """Phase times of one mixed-precision dense resistance solve (assembly, FP32 copy,
+    tensor-core LU, FP64 GMRES-IR, final FP64 residual) and of the FP64 LU."""
+    import ctypes
+
+    from fluidlets_gb300 import _lib, core
+    from fluidlets_gb300.geometry import fibonacci_sphere, mean_nn_spacing
+
+    L = _lib.load()
+    dev = torch.device("cuda")
+    X = fibonacci_sphere(a.n) + (np.array([0, 0, 1.5]) if a.kind == "wall" else 0)
+    eps = 0.25 * mean_nn_spacing(X)
+    Xd = torch.from_numpy(X).to(dev)
+    e = torch.full((a.n,), eps, dtype=torch.float64, device=dev)
+    U = torch.zeros_like(Xd)
+    U[:, 0] = 1.0
+    b = U.reshape(-1).contiguous()
+
+    def t(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = fn()
+        torch.cuda.synchronize()
+        return out, 1e3 * (time.perf_counter() - t0)
+
+    for rep in range(a.reps):
+        L.flg_profile_enable(1)
+        K, t_asm = t(lambda: core._assemble_dev(kern, Xd, Xd, e, 1.0))
+        (K32, ld32, dinv), t_lu = t(lambda: core._lowp_factor_dev(K, a.lu))
+        (x, it, outer, res), t_ir = t(lambda: core._gmres_ir_dense_dev(K, K32, ld32, dinv, b, 1e-10, 60, 200))
+        _, t_res = t(lambda: core._evaluate_dev(kern, Xd, Xd, x.reshape(-1, 3), e, 1.0, "fp64"))
+        slots = {}
+        for name, k in _lib.SLOT.items():
+            ms, n = ctypes.c_double(0), ctypes.c_int64(0)
+            L.flg_profile_read(k, ctypes.byref(ms), ctypes.byref(n))
+            if n.value:
+                slots[name] = (round(ms.value, 3), n.value)
+        L.flg_profile_enable(0)
+        print(f"[mixed {a.lu}] n={3 * a.n}: assemble {t_asm:.2f} ms, convert+LU {t_lu:.2f} ms, GMRES-IR {t_ir:.2f} ms "
+              f"({it} it, {outer} IR, resid {res:.2e}), residual {t_res:.2f} ms; kernel slots (ms, launches): {slots}")
+    K = core._assemble_dev(kern, Xd, Xd, e, 1.0)
+    _, t64 = t(lambda: core._lu_solve_dev(K.clone(), b))
+    _, tcs = t(lambda: torch.linalg.solve(K, b))
+    print(f"[fp64] LU factor+solve {t64:.2f} ms; cuSOLVER (torch.linalg.solve) {tcs:.2f} ms")
 
 
 if __name__ == "__main__":

@@ -260,6 +260,7 @@ int flg_measure_peaks(double *fp32_tflops, double *fp64_tflops, void *stream);
 #define FLG_SLOT_LU_UPDATE 4    /* LU trailing updates (tensor-core GEMM)       */
 #define FLG_SLOT_LU_PANEL 5     /* LU panel / diagonal-block kernels            */
 #define FLG_SLOT_GEMV 6         /* FP64 GEMV (residuals)                        */
+#define FLG_SLOT_LU_SOLVE 7     /* low-precision triangular solves (preconditioner) */
 #define FLG_NUM_SLOTS 8
 int flg_profile_enable(int enable);
 int flg_profile_read(int slot, double *total_ms, int64_t *launches);
