@@ -48,6 +48,10 @@ def parse():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--cpu-sample", type=int, default=2048, help="targets in the CPU sample (x all sources)")
     p.add_argument("--no-extras", action="store_true", help="skip the accuracy / FP64 / solve sections")
+    p.add_argument("--workload", default="wall_sum", choices=["wall_sum", "brinkman_gmres", "wall_lu", "serve"],
+                   help="wall_sum (default, the headline) or one of the other benchmark configurations")
+    p.add_argument("--n-points", type=int, default=None, help="override the point count of brinkman_gmres / wall_lu")
+    p.add_argument("--fp64", action="store_true", help="also run the plain FP64 GPU solve (slow at full size)")
     return p.parse_args()
 
 
@@ -350,8 +354,121 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_brinkman_gmres(args):
+    """Sphere radius 1, N Fibonacci points (default 65,536), eps = 0.2 x mean NN spacing, Brinkmanlet
+    alpha in {0, 1, 10} and alpha = (1 + i) sqrt(omega / 2), omega in {1, 10}; rigid translation
+    (1, 0, 0) and rotation (0, 0, 1) x x; GMRES(restart 50) to 1e-10: FP32-far/FP64-near matvecs in
+    FP64 iterative refinement, and (with --fp64) the plain FP64-matvec GMRES."""
+    import torch
+
+    import fluidlets_gb300 as fl
+    from fluidlets_gb300.geometry import fibonacci_sphere, mean_nn_spacing
+
+    n = args.n_points or 65536
+    X = fibonacci_sphere(n)
+    eps = 0.2 * mean_nn_spacing(X)
+    dev = torch.device("cuda")
+    Xd = torch.from_numpy(X).to(dev)
+    ed = torch.full((n,), eps, dtype=torch.float64, device=dev)
+    Ut = torch.zeros_like(Xd)
+    Ut[:, 0] = 1.0
+    Ur = torch.stack([-Xd[:, 1], Xd[:, 0], torch.zeros_like(Xd[:, 0])], 1)  # (0, 0, 1) x x
+    out = {"workload": f"Brinkmanlet GMRES, unit sphere N={n} Fibonacci, eps={eps:.7f} (0.2 x mean NN spacing), "
+                       "restart 50, rtol 1e-10", "cases": []}
+    alphas = [0.0, 1.0, 10.0, (1 + 1j) * np.sqrt(0.5), (1 + 1j) * np.sqrt(5.0)]
+    # warm-up (module loading, kernel attributes) outside the timed solves
+    fl.resistance(fl.Brinkmanlet3D(1.0), Xd[:512], Ut[:512], ed[:512], method="gmres", precision="mixed")
+    for a in alphas:
+        k = fl.Brinkmanlet3D(a)
+        for motion, U in (("translate_x", Ut), ("rotate_z", Ur)):
+            case = {"alpha": str(a), "motion": motion}
+            for prec in (["mixed", "fp64"] if args.fp64 else ["mixed"]):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                F, info = fl.resistance(k, Xd, U, ed, method="gmres", restart=50, maxiter=200, precision=prec)
+                torch.cuda.synchronize()
+                dt = time.perf_counter() - t0
+                Fh = F.cpu().numpy()
+                drag = Fh[:, 0].sum()
+                torque = (X[:, 0] * Fh[:, 1] - X[:, 1] * Fh[:, 0]).sum()
+                case[prec] = {"seconds": dt, "iterations": info.iterations, "ir_steps": info.ir_steps,
+                              "residual": info.residual,
+                              "drag_x": complex(drag).real if np.iscomplexobj(drag) else float(drag),
+                              "torque_z": complex(torque).real if np.iscomplexobj(torque) else float(torque),
+                              "drag_x_imag": float(np.imag(drag)), "torque_z_imag": float(np.imag(torque))}
+                case[prec + "_forces"] = Fh
+            if args.fp64:
+                # accuracy against the FP64 solution converged to 1e-13 (the rtol = 1e-10 FP64 solve
+                # above is itself only accurate to ~ condition number x 1e-10)
+                Fc, ic = fl.resistance(k, Xd, U, ed, method="gmres", restart=50, maxiter=400, rtol=1e-13)
+                Fc = Fc.cpu().numpy()
+                for prec in ("mixed", "fp64"):
+                    case[f"rel_force_err_{prec}_vs_converged_fp64"] = float(
+                        np.linalg.norm(case[prec + "_forces"] - Fc) / np.linalg.norm(Fc))
+                case["speedup_mixed_vs_fp64"] = case["fp64"]["seconds"] / case["mixed"]["seconds"]
+            for key in [c for c in case if c.endswith("_forces")]:
+                del case[key]
+            out["cases"].append(case)
+            print(json.dumps(case), flush=True)
+    print(json.dumps(out), flush=True)
+
+
+def run_wall_lu(args):
+    """Sphere radius 1, N Fibonacci points (default 8,192), centre heights h/a in {1.05, 1.5, 3.0}
+    over the wall z = 0, eps = 0.25 x mean NN spacing, WallStokeslet3D, translation parallel (x)
+    and normal (z): TF32 and BF16 tensor-core LU + FP64 GMRES-IR to 1e-10, against the FP64 LU."""
+    import torch
+
+    import fluidlets_gb300 as fl
+    from fluidlets_gb300.geometry import fibonacci_sphere, mean_nn_spacing
+
+    n = args.n_points or 8192
+    S = fibonacci_sphere(n)
+    eps = 0.25 * mean_nn_spacing(S)
+    dev = torch.device("cuda")
+    ed = torch.full((n,), eps, dtype=torch.float64, device=dev)
+    k = fl.WallStokeslet3D()
+    out = {"workload": f"WallStokeslet3D dense LU, sphere N={n} ({3 * n} unknowns), eps={eps:.7f}", "cases": []}
+    for h in (1.05, 1.5, 3.0):
+        Xd = torch.from_numpy(S + [0, 0, h]).to(dev)
+        for motion, vec in (("parallel_x", [1.0, 0, 0]), ("normal_z", [0, 0, 1.0])):
+            U = torch.tensor(vec, dtype=torch.float64, device=dev).expand(n, 3).contiguous()
+            case = {"h_over_a": h, "motion": motion}
+            ref = None
+            if args.fp64:
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                F64, i64 = fl.resistance(k, Xd, U, ed, method="lu")
+                torch.cuda.synchronize()
+                case["fp64_lu"] = {"seconds": time.perf_counter() - t0, "residual": i64.residual,
+                                   "drag": float(F64[:, 0 if motion == "parallel_x" else 2].sum())}
+                ref = F64
+            for lu in ("tf32", "bf16"):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                Fm, im = fl.resistance(k, Xd, U, ed, method="lu", precision="mixed", lu=lu)
+                torch.cuda.synchronize()
+                c = {"seconds": time.perf_counter() - t0, "residual": im.residual, "ir_steps": im.ir_steps,
+                     "gmres_iterations": im.iterations,
+                     "drag": float(Fm[:, 0 if motion == "parallel_x" else 2].sum())}
+                if ref is not None:
+                    c["rel_force_err_vs_fp64"] = float(torch.linalg.vector_norm(Fm - ref) / torch.linalg.vector_norm(ref))
+                    c["speedup_vs_fp64"] = case["fp64_lu"]["seconds"] / c["seconds"]
+                case["mixed_" + lu] = c
+            out["cases"].append(case)
+            print(json.dumps(case), flush=True)
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
+    if args.impl != "reference" and args.workload == "brinkman_gmres":
+        return run_brinkman_gmres(args)
+    if args.impl != "reference" and args.workload == "wall_lu":
+        return run_wall_lu(args)
+    if args.impl != "reference" and args.workload == "serve":
+        from fluidlets_gb300.serve import bench_serving
+        return bench_serving(args)
     if args.impl == "reference":
         run_reference(args)
     else:

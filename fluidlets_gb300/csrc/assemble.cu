@@ -114,6 +114,38 @@ __global__ void __launch_bounds__(128) assemble_kernel(AsmArgs a) {
     }
 }
 
+// Bucket assembly for graph replay: points padded to n_cap, the real count
+// read from device memory; entries with i or j >= n_real form an identity block.
+template <int KIND>
+__global__ void __launch_bounds__(128) assemble_bucket_kernel(AsmArgs a, const int64_t *n_real_p) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= a.N) return;
+    const int64_t nr = *n_real_p;
+    const bool jr = j < nr;
+    double sx = 0, sy = 0, sz = 0, e2 = 0;
+    if (jr) {
+        sx = a.src[3 * j];
+        sy = a.src[3 * j + 1];
+        sz = a.src[3 * j + 2];
+        const double e = a.eps[j];
+        e2 = e * e;
+    }
+    for (int64_t i = blockIdx.y; i < a.M; i += gridDim.y) {
+        double G[9], Gi[9];
+        if (jr && i < nr) {
+            block_f64<KIND, false>(a.tg[3 * i], a.tg[3 * i + 1], a.tg[3 * i + 2], sx, sy, sz, e2, a.are, a.aim, G, Gi);
+            store_block(a, i, 3 * j, G, Gi, false);
+        } else {
+            for (int q = 0; q < 9; q++) G[q] = (i == j && (q == 0 || q == 4 || q == 8)) ? 1.0 : 0.0;
+            AsmArgs b = a;
+            b.scale = 1.0;
+            b.imu_re = 1.0;
+            b.imu_im = 0.0;
+            store_block(b, i, 3 * j, G, G, false);
+        }
+    }
+}
+
 // nearest-neighbour assembly: thread per (target i, force group j), members of
 // group j (ascending quadrature index) summed in FP64
 struct NearestArgs {
@@ -354,6 +386,34 @@ extern "C" int flg_assemble(int kind, double alpha_re, double alpha_im, const do
     cudaStream_t st = as_stream(stream);
     prof_begin(FLG_SLOT_ASSEMBLE, st);
     dispatch<LaunchAsm>(kind, kind == FLG_BRINKMANLET && alpha_im != 0.0, asm_grid(M, N), 128, st, a);
+    FLG_LAUNCH_CHECK();
+    prof_end(FLG_SLOT_ASSEMBLE, st);
+    return FLG_OK;
+}
+
+extern "C" int flg_assemble_bucket(int kind, double alpha_re, double alpha_im, const double *points, const double *eps,
+                                   const int64_t *n_real, int64_t n_cap, double mu_re, void *out, int out_type,
+                                   int64_t ld, void *stream) {
+    AsmArgs a{};
+    FLG_TRY(prepare(kind, alpha_re, alpha_im, mu_re, 0.0, out_type, a));
+    FLG_REQUIRE(!(kind == FLG_BRINKMANLET && alpha_im != 0.0), "bucket assembly is real only");
+    FLG_REQUIRE(out_type == FLG_F64 || out_type == FLG_F32, "bucket assembly writes FLG_F64 or FLG_F32");
+    FLG_REQUIRE(n_cap >= 0 && ld >= 3 * n_cap, "bad bucket shape");
+    if (n_cap == 0) return FLG_OK;
+    FLG_REQUIRE(points && eps && n_real && out, "null pointer");
+    a.tg = points;
+    a.M = n_cap;
+    a.src = points;
+    a.eps = eps;
+    a.N = n_cap;
+    a.out = out;
+    a.ld = ld;
+    cudaStream_t st = as_stream(stream);
+    const dim3 grid = asm_grid(n_cap, n_cap);
+    prof_begin(FLG_SLOT_ASSEMBLE, st);
+    if (kind == FLG_STOKESLET) assemble_bucket_kernel<FLG_STOKESLET><<<grid, 128, 0, st>>>(a, n_real);
+    else if (kind == FLG_WALL) assemble_bucket_kernel<FLG_WALL><<<grid, 128, 0, st>>>(a, n_real);
+    else assemble_bucket_kernel<FLG_BRINKMANLET><<<grid, 128, 0, st>>>(a, n_real);
     FLG_LAUNCH_CHECK();
     prof_end(FLG_SLOT_ASSEMBLE, st);
     return FLG_OK;

@@ -957,30 +957,31 @@ extern "C" size_t flg_lu_factor_lowp_workspace(int64_t n, int mode) {
     char *w;
     size_t t;
     lowp_carve(c, n, mode, &a, &b, &d, &w, &t);
-    c.take<int>(2);
-    return c.bytes();
+    return c.bytes() + 256;  // + the flags of flg_lu_factor_lowp, at the end
 }
 
-extern "C" int flg_lu_factor_lowp(int64_t n, float *A, int64_t ld, int mode, float *dinv, int *info, void *work,
-                                  size_t work_bytes, void *stream) {
-    FLG_REQUIRE(n >= 0 && ld >= n && info, "bad LU arguments");
+extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mode, float *dinv, int *flags, void *work,
+                                        size_t work_bytes, void *stream) {
+    FLG_REQUIRE(n >= 0 && ld >= n && flags, "bad LU arguments");
     FLG_REQUIRE(mode == FLG_LU_TF32 || mode == FLG_LU_BF16 || mode == FLG_LU_FP32, "unknown LU mode %d", mode);
     FLG_REQUIRE(ld % 4 == 0, "ld must be a multiple of 4 (16-byte rows)");
-    *info = 0;
+    cudaStream_t st = as_stream(stream);
+    FLG_CUDA(cudaMemsetAsync(flags, 0, 2 * sizeof(int), st));
     if (n == 0) return FLG_OK;
     FLG_REQUIRE(A && dinv, "null pointer");
-    cudaStream_t st = as_stream(stream);
     Arena ar(work, work_bytes);
     float *U12, *L21, *U12T;
     char *tcw;
     size_t tcb;
     lowp_carve(ar, n, mode, &U12, &L21, &U12T, &tcw, &tcb);
-    int *dinfo = ar.take<int>(2);  // [0] first bad pivot, [1] tensor-core wait timed out
-    FLG_REQUIRE(U12 && L21 && U12T && dinfo && (tcb == 0 || tcw), "workspace too small for LU (%zu bytes)",
-                work_bytes);
-    FLG_CUDA(cudaMemsetAsync(dinfo, 0, 2 * sizeof(int), st));
+    FLG_REQUIRE(U12 && L21 && U12T && (tcb == 0 || tcw), "workspace too small for LU (%zu bytes)", work_bytes);
+    int *dinfo = flags;  // [0] first bad pivot, [1] tensor-core wait timed out
     const size_t dsmem = kDiagSmem;
-    FLG_CUDA(cudaFuncSetAttribute(diag_lowp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem));
+    static bool attr_set = false;  // set once, so a later call can be captured in a graph
+    if (!attr_set) {
+        FLG_CUDA(cudaFuncSetAttribute(diag_lowp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem));
+        attr_set = true;
+    }
     const int64_t nblk = ceil_div(n, kNB);
     float *Linv = dinv, *Uinv = dinv + nblk * kNB * kNB;
     for (int64_t k = 0; k < nblk; k++) {
@@ -1016,17 +1017,31 @@ extern "C" int flg_lu_factor_lowp(int64_t n, float *A, int64_t ld, int mode, flo
             prof_end(FLG_SLOT_LU_PANEL, st);
         }
     }
+    return FLG_OK;
+}
+
+extern "C" int flg_lu_factor_lowp(int64_t n, float *A, int64_t ld, int mode, float *dinv, int *info, void *work,
+                                  size_t work_bytes, void *stream) {
+    FLG_REQUIRE(info, "null info");
+    *info = 0;
+    FLG_REQUIRE(n >= 0 && ld >= n, "bad LU arguments");
+    if (n == 0) return FLG_OK;
+    // the two device flags live at the end of the workspace
+    const size_t need = flg_lu_factor_lowp_workspace(n, mode);
+    FLG_REQUIRE(work && work_bytes >= need, "workspace too small for LU (%zu bytes, %zu needed)", work_bytes, need);
+    int *flags = (int *)((char *)work + ((need - 64) & ~size_t(15)));
+    cudaStream_t st = as_stream(stream);
+    FLG_TRY(flg_lu_factor_lowp_async(n, A, ld, mode, dinv, flags, work, need - 128, stream));
     int hflags[2] = {0, 0};
-    FLG_CUDA(cudaMemcpyAsync(hflags, dinfo, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
+    FLG_CUDA(cudaMemcpyAsync(hflags, flags, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
     FLG_CUDA(cudaStreamSynchronize(st));
     if (hflags[1]) {
         set_error("tensor-core update: an mbarrier wait timed out");
         return FLG_ERR_CUDA;
     }
-    const int hinfo = hflags[0];
-    *info = hinfo;
-    if (hinfo) {
-        set_error("zero or non-finite pivot at row %d in the low-precision LU", hinfo - 1);
+    *info = hflags[0];
+    if (hflags[0]) {
+        set_error("zero or non-finite pivot at row %d in the low-precision LU", hflags[0] - 1);
         return FLG_ERR_SINGULAR;
     }
     return FLG_OK;

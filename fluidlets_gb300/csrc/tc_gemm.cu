@@ -299,13 +299,17 @@ int tc_update(float *C, int64_t ldc, const float *Lp, int64_t ldl, const float *
     const size_t smem = tc_smem_bytes();
     dim3 grid((unsigned)ceil_div(nc, TC_BN), (unsigned)ceil_div(m, TC_BM));
     FLG_REQUIRE(grid.y <= 65535, "too many row tiles");
-    if (mode == FLG_LU_TF32) {
+    static bool attr_set = false;  // set once, so a later call can be captured in a graph
+    if (!attr_set) {
         FLG_CUDA(cudaFuncSetAttribute(tc_update_kernel<FLG_LU_TF32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
-        tc_update_kernel<FLG_LU_TF32><<<grid, TC_THREADS, smem, st>>>(ma, mb, C, ldc, (int)m, (int)nc, err);
-    } else {
         FLG_CUDA(cudaFuncSetAttribute(tc_update_kernel<FLG_LU_BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
+        attr_set = true;
+    }
+    if (mode == FLG_LU_TF32) {
+        tc_update_kernel<FLG_LU_TF32><<<grid, TC_THREADS, smem, st>>>(ma, mb, C, ldc, (int)m, (int)nc, err);
+    } else {
         tc_update_kernel<FLG_LU_BF16><<<grid, TC_THREADS, smem, st>>>(ma, mb, C, ldc, (int)m, (int)nc, err);
     }
     FLG_LAUNCH_CHECK();

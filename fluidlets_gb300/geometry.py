@@ -62,3 +62,46 @@ def wall_sum_workload(n_src: int = 262144, n_tgt: int = 262144, n_wall: int = 16
     wall = np.c_[rng.uniform(-1, 1, (n_wall, 2)), np.zeros(n_wall)]
     f = rng.normal(size=(n_src, 3))
     return np.r_[tgt, wall], src, f, eps
+
+
+def ellipsoid_points(n: int, axes=(0.6, 0.4, 0.4)) -> np.ndarray:
+    """n points on an ellipsoid surface (a stretched Fibonacci lattice)."""
+    return fibonacci_sphere(n) * np.asarray(axes, float)
+
+
+def biflagellate_shape(t: float, n_body: int = 96, fine: int = 4, segments: int = 64, amplitude: float = 0.2,
+                       wavelength: float = 1.0, length: float = 1.0, frequency: float = 1.0):
+    """A model biflagellate swimmer in its body frame at time t.
+
+    Body: ellipsoid with semi-axes 0.6 : 0.4 : 0.4 (3:2:2), n_body force points and fine * n_body
+    quadrature points, at rest in the body frame.  Two planar flagella of `segments` segments
+    attached at the front (x = 0.6, z = +-0.1), pointing along +x and beating in the x-z plane as
+    travelling sine waves z = +-(0.1 + A sin(k s - w t) s/L) of amplitude A = 0.2 and wavelength 1;
+    force points at the segment ends, `fine` quadrature points per segment.  Returns a SwimmerShape.
+    """
+    from .swimming import SwimmerShape
+
+    k = 2 * np.pi / wavelength
+    w = 2 * np.pi * frequency
+
+    def flagellum(sign, s):
+        env = s / length
+        x = 0.6 + s
+        z = sign * (0.1 + amplitude * env * np.sin(k * s - w * t))
+        vz = sign * (-amplitude * env * w * np.cos(k * s - w * t))
+        pos = np.c_[x, np.zeros_like(s), z]
+        vel = np.c_[np.zeros_like(s), np.zeros_like(s), vz]
+        return pos, vel
+
+    s_c = np.linspace(0, length, segments + 1)[1:]
+    s_f = np.linspace(0, length, fine * segments + 1)[1:]
+    body_c = ellipsoid_points(n_body)
+    body_f = ellipsoid_points(fine * n_body)
+    xs, vs, Xs = [body_c], [np.zeros_like(body_c)], [body_f]
+    for sign in (1.0, -1.0):
+        p, v = flagellum(sign, s_c)
+        pf, _ = flagellum(sign, s_f)
+        xs.append(p)
+        vs.append(v)
+        Xs.append(pf)
+    return SwimmerShape(x=np.vstack(xs), v=np.vstack(vs), X=np.vstack(Xs))

@@ -1,0 +1,487 @@
+"""Continuous-batching solve server on one GPU.
+
+Requests -- rigid-body resistance solves and free-swimmer instants of uneven
+size -- are submitted as they arrive and served by `slots` workers, each a host
+thread with its own CUDA stream, so the work of concurrent requests overlaps
+on the device.  Scheduling is continuous: whenever a slot finishes, it admits
+the next pending request (preferring one of the bucket it already has a plan
+for) provided the HBM budget allows; nothing waits for a batch to fill.
+
+Resistance requests are padded to a size bucket (N rounded up on a ~19 %
+geometric grid of multiples of 128 points).  Each slot keeps one *bucket plan*:
+fixed device buffers and a CUDA graph capturing, for that bucket size,
+``flg_assemble_bucket`` (real block + identity padding) -> FP32 copy ->
+``flg_lu_factor_lowp_async`` (tensor-core LU, no host sync).  A request copies
+its points into the plan's buffers, replays the graph and runs FP64 GMRES-IR
+on the padded system; padded rows are identity and padded right-hand sides
+zero, so the solution is exactly that of the unpadded system (the forces
+agree with a solve of the request alone to rounding).  The per-bucket choice
+of tensor-core precision (TF32 or BF16) is made by a small autotuner that
+times both on the first request of the bucket and keeps the faster one that
+converges.  Swimmer requests run the mixed-precision swimmer solve on the
+slot's stream without a graph.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import queue
+import threading
+import time
+from concurrent.futures import Future
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _device as dv
+from ._lib import F64, LU_MODE, check, load
+from .kernels import Stokeslet3D, kernel_params
+
+BUCKET_BASE = 128
+
+
+def bucket_of(n_points: int) -> int:
+    """Smallest bucket >= n_points: multiples of 128 on a 2^(1/4) geometric grid."""
+    b = BUCKET_BASE
+    while b < n_points:
+        b = int(math.ceil(b * 2 ** 0.25 / BUCKET_BASE)) * BUCKET_BASE
+    return b
+
+
+@dataclass
+class ResistanceRequest:
+    kernel: object
+    points: np.ndarray
+    velocities: np.ndarray
+    eps: float
+    mu: float = 1.0
+
+
+@dataclass
+class SwimmerRequest:
+    shape: object
+    x0: np.ndarray
+    B: np.ndarray
+    eps: float
+    mu: float = 1.0
+    kernel: object = None
+
+
+@dataclass
+class Result:
+    value: object               # forces (N, 3) or a SwimState
+    residual: float
+    t_arrival: float
+    t_start: float
+    t_done: float
+    slot: int
+    bucket: int = 0
+    lu: str = ""
+    ir_steps: int = 0
+
+    @property
+    def latency(self) -> float:
+        return self.t_done - self.t_arrival
+
+
+def plan_bytes(nb_points: int) -> int:
+    n = 3 * nb_points
+    ld32 = (n + 31) // 32 * 32
+    return 8 * n * n + 4 * n * ld32 + 64 * n * 128 + 128 * n * 8 + (64 << 20)
+
+
+class BucketPlan:
+    """Device buffers and the captured assemble + factor graph of one bucket size."""
+
+    def __init__(self, kernel, nb_points: int, mu: float, lu: str, stream: torch.cuda.Stream):
+        L = load()
+        self.kernel, self.mu, self.lu, self.nbp = kernel, mu, lu, nb_points
+        self.kind, self.are, self.aim = kernel_params(kernel)
+        dev = torch.device("cuda", torch.cuda.current_device())
+        n = 3 * nb_points
+        self.n = n
+        self.ld32 = (n + 31) // 32 * 32
+        self.pts = torch.zeros((nb_points, 3), dtype=torch.float64, device=dev)
+        self.eps = torch.ones(nb_points, dtype=torch.float64, device=dev)
+        self.n_real = torch.zeros(1, dtype=torch.int64, device=dev)
+        self.K = torch.empty((n, n), dtype=torch.float64, device=dev)
+        self.K32 = torch.empty((n, self.ld32), dtype=torch.float32, device=dev)
+        self.dinv = torch.empty(L.flg_lu_lowp_dinv_elems(n), dtype=torch.float32, device=dev)
+        self.flags = torch.zeros(2, dtype=torch.int32, device=dev)
+        mode = LU_MODE[lu]
+        self.lu_bytes = L.flg_lu_factor_lowp_workspace(n, mode)
+        self.lu_ws = dv.workspace(self.lu_bytes)
+        self.b = torch.zeros(n, dtype=torch.float64, device=dev)
+        self.x = torch.zeros(n, dtype=torch.float64, device=dev)
+        self.graph = None
+        self.stream = stream
+        self.mode = mode
+
+    def _run(self):
+        L = load()
+        st = ctypes.c_void_p(self.stream.cuda_stream)
+        check(L.flg_assemble_bucket(self.kind, self.are, self.aim, dv.ptr(self.pts), dv.ptr(self.eps),
+                                    dv.ptr(self.n_real), self.nbp, float(self.mu), dv.ptr(self.K), F64, self.n, st),
+              "bucket assembly")
+        check(L.flg_convert_f64_f32(self.n, self.n, dv.ptr(self.K), self.n, dv.ptr(self.K32), self.ld32, st), "convert")
+        check(L.flg_lu_factor_lowp_async(self.n, dv.ptr(self.K32), self.ld32, self.mode, dv.ptr(self.dinv),
+                                         dv.ptr(self.flags), dv.ptr(self.lu_ws), self.lu_bytes, st), "LU")
+
+    def capture(self):
+        """Capture assembly -> FP32 copy -> tensor-core LU as a CUDA graph (in the library,
+        thread-local capture mode); on failure the plan stays eager."""
+        L = load()
+        h = ctypes.c_void_p(0)
+        st = L.flg_bucket_graph_create(self.kind, self.are, self.aim, dv.ptr(self.pts), dv.ptr(self.eps),
+                                       dv.ptr(self.n_real), self.nbp, float(self.mu), dv.ptr(self.K), dv.ptr(self.K32),
+                                       self.ld32, self.mode, dv.ptr(self.dinv), dv.ptr(self.flags), dv.ptr(self.lu_ws),
+                                       self.lu_bytes, ctypes.c_void_p(self.stream.cuda_stream), ctypes.byref(h))
+        if st == 0 and h.value:
+            self.graph = h.value
+        else:
+            self.graph = None
+            self.capture_error = L.flg_last_error().decode(errors="replace")
+
+    def __del__(self):
+        if getattr(self, "graph", None):
+            try:
+                load().flg_graph_destroy(ctypes.c_void_p(self.graph))
+            except Exception:  # noqa: BLE001 - interpreter shutdown
+                pass
+
+    def factor(self, X: torch.Tensor, eps: torch.Tensor):
+        N = X.shape[0]
+        self.pts[:N].copy_(X)
+        self.eps[:N].copy_(eps)
+        self.n_real.fill_(N)
+        if self.graph is not None:
+            check(load().flg_graph_launch(ctypes.c_void_p(self.graph), ctypes.c_void_p(self.stream.cuda_stream)),
+                  "graph launch")
+        else:
+            self._run()
+
+    def solve(self, U: torch.Tensor, rtol: float, restart: int = 60, maxiter: int = 200):
+        L = load()
+        N = U.shape[0]
+        self.b.zero_()
+        self.b[:3 * N].copy_(U.reshape(-1))
+        self.x.zero_()
+        flags = self.flags.cpu()
+        if int(flags[1]):
+            raise RuntimeError("tensor-core update: an mbarrier wait timed out")
+        if int(flags[0]):
+            raise np.linalg.LinAlgError(f"zero pivot at row {int(flags[0]) - 1} in the low-precision LU")
+        nbytes = L.flg_gmres_ir_dense_workspace(self.n, restart)
+        ws = dv.workspace(nbytes)
+        iters, outer, resid = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_double(0.0)
+        from .core import _accept
+
+        st = L.flg_gmres_ir_dense(self.n, dv.ptr(self.K), self.n, dv.ptr(self.K32), self.ld32, dv.ptr(self.dinv),
+                                  dv.ptr(self.b), dv.ptr(self.x), rtol * 1e-2, restart, maxiter, ctypes.byref(iters),
+                                  ctypes.byref(outer), ctypes.byref(resid), dv.ptr(ws), nbytes,
+                                  ctypes.c_void_p(self.stream.cuda_stream))
+        _accept(st, resid.value, rtol, "GMRES-IR")
+        return self.x[:3 * N].reshape(N, 3).clone(), iters.value, outer.value, resid.value
+
+
+class SolveServer:
+    """Continuous-batching server: submit() returns a Future of a Result."""
+
+    def __init__(self, slots: int = 6, hbm_budget_gb: float = 150.0, rtol: float = 1e-10, graphs: bool = True,
+                 lu: str = "auto", lookahead: int = 8):
+        self.slots = slots
+        self.budget = int(hbm_budget_gb * 2**30)
+        self.rtol = rtol
+        self.graphs = graphs
+        self.lu = lu
+        self.lookahead = lookahead
+        self._pending = []            # [(request, future, t_arrival, bucket)]
+        self._cv = threading.Condition()
+        self._used = 0                # bytes held by slot plans and in-flight swimmer solves
+        self._held = [0] * slots      # plan bytes held per slot
+        self._busy = [False] * slots  # slot is running a request
+        self._plans = [None] * slots  # current BucketPlan per slot
+        self._tuned = {}              # (kernel kind, bucket) -> "tf32" | "bf16"
+        self.stats = {"graph_replays": 0, "eager_factors": 0, "captures": 0, "capture_errors": []}
+        self._closed = False
+        self._dev = self._device()
+        self._threads = [threading.Thread(target=self._worker, args=(s,), daemon=True) for s in range(slots)]
+        for t in self._threads:
+            t.start()
+
+    # ---- public -----------------------------------------------------------------
+    def submit(self, req, t_arrival: float | None = None) -> Future:
+        fut = Future()
+        t = time.perf_counter() if t_arrival is None else t_arrival
+        b = bucket_of(len(req.points)) if isinstance(req, ResistanceRequest) else 0
+        with self._cv:
+            self._pending.append((req, fut, t, b))
+            self._cv.notify_all()
+        return fut
+
+    def close(self):
+        with self._cv:
+            self._closed = True
+            self._cv.notify_all()
+        for t in self._threads:
+            t.join()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---- scheduling -----------------------------------------------------------------
+    def _evict_idle(self, keep_slot=None):
+        """Drop the bucket plans of idle slots (their device memory returns to the pool)."""
+        for s in range(self.slots):
+            if not self._busy[s] and self._held[s] > 0 and s != keep_slot:
+                self._plans[s] = None
+                self._used -= self._held[s]
+                self._held[s] = 0
+
+    def _pick(self, slot):
+        """Oldest admissible request, preferring the slot's current bucket within the lookahead window.
+        Called with the lock held; returns None when the HBM budget does not allow it yet."""
+        plan = self._plans[slot]
+        cand = None
+        for k, (req, fut, t, b) in enumerate(self._pending[: self.lookahead]):
+            if plan is not None and isinstance(req, ResistanceRequest) and b == plan.nbp and \
+                    kernel_params(req.kernel)[0] == plan.kind:
+                cand = k
+                break
+        if cand is None:
+            cand = 0
+        req, fut, t, b = self._pending[cand]
+        same = isinstance(req, ResistanceRequest) and plan is not None and plan.nbp == b and \
+            kernel_params(req.kernel)[0] == plan.kind
+
+        def cost():
+            if isinstance(req, ResistanceRequest):
+                return 0 if same else plan_bytes(b) - self._held[slot]
+            n = 3 * len(req.shape.x) + 6
+            return 16 * n * n + (64 << 20)
+
+        delta = cost()
+        if self._used + delta > self.budget:
+            self._evict_idle(keep_slot=slot if same else None)
+            delta = cost()
+            if self._used + delta > self.budget and any(self._busy):
+                return None  # wait until running requests release memory
+        self._pending.pop(cand)
+        self._used += delta
+        self._busy[slot] = True
+        if isinstance(req, ResistanceRequest) and not same:
+            self._held[slot] = plan_bytes(b)
+        return req, fut, t, b, (delta if isinstance(req, SwimmerRequest) else 0)
+
+    # ---- device hooks (overridden by the scheduler's CPU test) ---------------------------
+    def _device(self):
+        return torch.cuda.current_device()
+
+    def _make_stream(self):
+        torch.cuda.set_device(self._dev)
+        return torch.cuda.Stream()
+
+    def _run_request(self, slot, stream, req, b):
+        with torch.cuda.stream(stream):
+            if isinstance(req, ResistanceRequest):
+                res = self._resistance(slot, stream, req, b)
+            else:
+                res = self._swimmer(stream, req)
+            stream.synchronize()
+        return res
+
+    def _worker(self, slot):
+        stream = self._make_stream()
+        while True:
+            with self._cv:
+                while True:
+                    if self._pending:
+                        item = self._pick(slot)
+                        if item is not None:
+                            break
+                    elif self._closed:
+                        return
+                    self._cv.wait(timeout=0.05)
+            req, fut, t_arr, b, reserved = item
+            t0 = time.perf_counter()
+            try:
+                res = self._run_request(slot, stream, req, b)
+                res.t_arrival, res.t_start, res.t_done, res.slot = t_arr, t0, time.perf_counter(), slot
+                fut.set_result(res)
+            except Exception as e:  # noqa: BLE001 - delivered to the caller
+                if isinstance(req, ResistanceRequest):  # drop the slot's plan and its reservation
+                    with self._cv:
+                        self._plans[slot] = None
+                        self._used -= self._held[slot]
+                        self._held[slot] = 0
+                fut.set_exception(e)
+            finally:
+                with self._cv:
+                    self._used -= reserved  # swimmer systems are transient
+                    self._busy[slot] = False
+                    self._cv.notify_all()
+
+    # ---- request pipelines ------------------------------------------------------------
+    def _lu_for(self, req, b):
+        if self.lu != "auto":
+            return self.lu
+        key = (kernel_params(req.kernel)[0], b)
+        return self._tuned.get(key)
+
+    def _resistance(self, slot, stream, req, b):
+        from .core import _evaluate_dev
+
+        dev = torch.device("cuda", self._dev)
+        X = torch.as_tensor(np.ascontiguousarray(req.points, dtype=np.float64)).to(dev, non_blocking=True)
+        U = torch.as_tensor(np.ascontiguousarray(req.velocities, dtype=np.float64)).to(dev, non_blocking=True)
+        N = X.shape[0]
+        e = torch.full((N,), float(req.eps), dtype=torch.float64, device=dev) if np.ndim(req.eps) == 0 else \
+            torch.as_tensor(np.asarray(req.eps, dtype=np.float64)).to(dev)
+        lu = self._lu_for(req, b)
+        plan = self._plans[slot]
+        if lu is None:  # autotune this bucket: time TF32 and BF16, keep the faster that converges
+            best = None
+            for mode in ("tf32", "bf16"):
+                p = BucketPlan(req.kernel, b, req.mu, mode, stream)
+                stream.synchronize()  # only this slot's stream: another slot may be capturing a graph
+                t0 = time.perf_counter()
+                p.factor(X, e)
+                x, it, outer, resid = p.solve(U, self.rtol)
+                stream.synchronize()
+                dt = time.perf_counter() - t0
+                if resid <= self.rtol and (best is None or dt < best[0]):
+                    best = (dt, mode)
+                del p
+            lu = best[1] if best else "tf32"
+            self._tuned[(kernel_params(req.kernel)[0], b)] = lu
+            plan = None
+        if plan is None or plan.nbp != b or plan.kind != kernel_params(req.kernel)[0] or plan.lu != lu \
+                or plan.mu != req.mu:
+            self._plans[slot] = None
+            del plan
+            plan = BucketPlan(req.kernel, b, req.mu, lu, stream)
+            if self.graphs:
+                plan.capture()
+                with self._cv:
+                    self.stats["captures"] += 1
+                    if plan.graph is None:
+                        self.stats["capture_errors"].append(getattr(plan, "capture_error", "?"))
+            with self._cv:
+                self._plans[slot] = plan  # its bytes were reserved in _pick (self._held[slot])
+        plan.factor(X, e)
+        with self._cv:
+            self.stats["graph_replays" if plan.graph is not None else "eager_factors"] += 1
+        F, it, outer, resid = plan.solve(U, self.rtol)
+        Kf = _evaluate_dev(req.kernel, X, X, F, e, req.mu, "fp64").reshape(-1)
+        r = float(torch.linalg.vector_norm(Kf - U.reshape(-1)) / torch.linalg.vector_norm(U))
+        return Result(F.cpu().numpy(), r, 0, 0, 0, slot, b, lu, outer)
+
+    def _swimmer(self, stream, req):
+        from .swimming import swimming_problem
+
+        st = swimming_problem(req.shape, req.x0, req.B, req.eps, req.mu, req.kernel, precision="mixed", rtol=self.rtol)
+        return Result(st, float("nan"), 0, 0, 0, 0, 0, "tf32", 0)
+
+
+# ---- the served mixed workload ------------------------------------------------------
+def make_requests(n_requests=4096, seed=0):
+    """Synthetic mixed workload: 75 % rigid bodies (sphere, or prolate spheroid with aspect ratio
+    U[1, 5] and random orientation; N log-uniform in [256, 6144]; free space or a wall at gap
+    U[0.05, 2]; eps / spacing U[0.15, 0.4]; translation or rotation), 25 % biflagellate swimmers."""
+    from .geometry import biflagellate_shape, fibonacci_sphere, mean_nn_spacing
+
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for _ in range(n_requests):
+        if rng.random() < 0.25:
+            t = rng.uniform(0, 1)
+            shape = biflagellate_shape(t)
+            B = np.linalg.qr(rng.normal(size=(3, 3)))[0]
+            B *= np.sign(np.linalg.det(B))
+            reqs.append(SwimmerRequest(shape, np.zeros(3), B, 0.02))
+            continue
+        N = int(round(math.exp(rng.uniform(math.log(256), math.log(6144)))))
+        unit = fibonacci_sphere(N)
+        if rng.random() < 0.5:
+            a = rng.uniform(1, 5)
+            R = np.linalg.qr(rng.normal(size=(3, 3)))[0]
+            pts = (unit * np.array([a, 1.0, 1.0])) @ R.T
+        else:
+            pts = unit
+        wall = rng.random() < 0.5
+        if wall:
+            pts = pts + np.array([0, 0, -pts[:, 2].min() + rng.uniform(0.05, 2.0)])
+        sp = mean_nn_spacing(pts)
+        eps = rng.uniform(0.15, 0.4) * sp
+        if rng.random() < 0.5:
+            U = np.tile(rng.normal(size=3), (N, 1))
+        else:
+            w = rng.normal(size=3)
+            U = np.cross(w, pts - pts.mean(0))
+        from .kernels import WallStokeslet3D
+
+        reqs.append(ResistanceRequest(WallStokeslet3D() if wall else Stokeslet3D(), pts, U, eps))
+    return reqs
+
+
+def bench_serving(args):
+    """Poisson arrivals at rates {50, 200, 800}/s over the mixed workload, served with continuous
+    batching; p50 / p99 latency and solves/s, and the one-solve-at-a-time FP64 GPU service time on a
+    sample of the same requests."""
+    import json
+
+    import fluidlets_gb300 as fl
+
+    n_req = getattr(args, "n_points", None) or 4096
+    reqs = make_requests(n_req)
+    out = {"workload": f"served mixed workload: {n_req} requests (75% rigid bodies N log-uniform [256, 6144], "
+                       "25% biflagellate swimmers), Poisson arrivals, HBM budget 150 GB", "rates": []}
+    with SolveServer(slots=6) as srv:
+        # warm-up and autotuning of the buckets in use, outside the timed runs
+        warm = {}
+        for r in reqs:
+            key = (type(r).__name__, bucket_of(len(r.points)) if isinstance(r, ResistanceRequest) else 0,
+                   type(getattr(r, "kernel", None)).__name__)
+            warm.setdefault(key, r)
+        for f in [srv.submit(r) for r in warm.values()]:
+            f.result()
+        for rate in (50.0, 200.0, 800.0):
+            rng = np.random.default_rng(int(rate))
+            gaps = rng.exponential(1.0 / rate, size=len(reqs))
+            t0 = time.perf_counter()
+            arrivals = t0 + np.cumsum(gaps)
+            futs = []
+            for r, ta in zip(reqs, arrivals):
+                now = time.perf_counter()
+                if ta > now:
+                    time.sleep(ta - now)
+                futs.append(srv.submit(r, t_arrival=ta))
+            res = [f.result() for f in futs]
+            t_end = max(x.t_done for x in res)
+            lat = np.array([x.latency for x in res]) * 1e3
+            resid = np.array([x.residual for x in res if np.isfinite(x.residual)])
+            line = {"rate_per_s": rate, "requests": len(res), "solves_per_s": len(res) / (t_end - t0),
+                    "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                    "max_residual": float(resid.max()) if len(resid) else None}
+            out["rates"].append(line)
+            print(json.dumps(line), flush=True)
+    # one-solve-at-a-time FP64 GPU service times on a stratified sample
+    sample = reqs[:: max(1, len(reqs) // 48)]
+    times = []
+    for r in sample:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        if isinstance(r, ResistanceRequest):
+            fl.resistance(r.kernel, r.points, r.velocities, r.eps, method="lu")
+        else:
+            fl.swimming_problem(r.shape, r.x0, r.B, r.eps)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    mean_fp64 = float(np.mean(times))
+    out["fp64_one_at_a_time"] = {"sample_requests": len(sample), "mean_service_ms": 1e3 * mean_fp64,
+                                 "max_solves_per_s": 1.0 / mean_fp64}
+    print(json.dumps(out), flush=True)

@@ -64,7 +64,7 @@ def _system_dev(kernel, x, X, nearest, x0, eps, mu):
 
 
 def swimming_problem(shape: SwimmerShape, x0, B, eps, mu=1.0, kernel=None, nearest=None, *, precision="fp64",
-                     lu="tf32", rtol=1e-12) -> SwimState:
+                     lu="tf32", rtol=1e-10) -> SwimState:
     """Solve the instantaneous free-swimming problem (``swimming.py:66-102``)."""
     kernel = Stokeslet3D() if kernel is None else kernel
     if complex(mu).imag != 0.0:
@@ -83,7 +83,7 @@ def swimming_problem(shape: SwimmerShape, x0, B, eps, mu=1.0, kernel=None, neare
     rhs[:3 * N] = torch.from_numpy(v.ravel()).to(A.device)
     if _prec(precision) == 1:
         K32, ld32, dinv = _lowp_factor_dev(A, lu)
-        sol, *_ = _gmres_ir_dense_dev(A, K32, ld32, dinv, rhs, rtol, 60, 200)
+        sol, *_ = _gmres_ir_dense_dev(A, K32, ld32, dinv, rhs, rtol * 1e-2, 60, 200, required=rtol)
     else:
         sol = _lu_solve_dev(A, rhs)
     sol = dv.to_host(sol)

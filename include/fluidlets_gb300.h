@@ -126,6 +126,16 @@ int flg_assemble(int kind, double alpha_re, double alpha_im,
                  double mu_re, double mu_im,
                  void *out, int out_type, int64_t ld, void *stream);
 
+/* Assembly into a fixed-size bucket (used by the solve server's captured CUDA
+ * graphs): points/eps hold n_cap entries of which the first *n_real (a DEVICE
+ * int64) are real; the matrix (3 n_cap x 3 n_cap, ld) gets the kernel block
+ * for real pairs and the identity for padded rows/columns, so the padded
+ * system has exactly the real solution followed by zeros.  Real kernels and
+ * real mu; out_type FLG_F64 or FLG_F32.  No counterpart in the reference. */
+int flg_assemble_bucket(int kind, double alpha_re, double alpha_im, const double *points, const double *eps,
+                        const int64_t *n_real, int64_t n_cap, double mu_re, void *out, int out_type,
+                        int64_t ld, void *stream);
+
 /* Replaces fluidlets.assemble_nearest (core/assemble.py:68-101) and
  * _fill_nearest (49-58): K[:, group j] = sum_{k: nearest[k] = j} G(x_i, X_k)/mu.
  * nearest (Q,) int64 in [0, n_force).  The grouping is a deterministic
@@ -182,6 +192,12 @@ int64_t flg_lu_lowp_dinv_elems(int64_t n);
 size_t flg_lu_factor_lowp_workspace(int64_t n, int mode);
 int flg_lu_factor_lowp(int64_t n, float *A, int64_t ld, int mode, float *dinv, int *info,
                        void *work, size_t work_bytes, void *stream);
+/* The same factorization without any host synchronization (so it can be
+ * captured in a CUDA graph): the pivot / timeout flags are written to the
+ * device array flags[2] (flags[0] = 1 + first bad pivot row, flags[1] = 1 if
+ * a tensor-core wait timed out) for the caller to check after the stream. */
+int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mode, float *dinv, int *flags,
+                             void *work, size_t work_bytes, void *stream);
 /* x = (L U)^{-1} b in FP32 for one FP64 right-hand side (converted on the
  * fly), result written as FP64. */
 size_t flg_lu_solve_lowp_workspace(int64_t n);
@@ -232,6 +248,20 @@ int flg_gmres_ir_dense(int64_t n, const double *A, int64_t ld, const float *LU32
                        const float *dinv, const double *b, double *x, double rtol, int restart, int maxiter,
                        int *iters, int *outer, double *resid,
                        void *work, size_t work_bytes, void *stream);
+
+/* ---- captured graphs (solve server) ---------------------------------------
+ * Captures flg_assemble_bucket -> flg_convert_f64_f32 -> flg_lu_factor_lowp_async
+ * over fixed buffers (K: 3 n_cap x 3 n_cap FP64, K32 with ld32, dinv, flags[2],
+ * LU workspace) on `stream` (not the default stream) in thread-local capture
+ * mode, after one eager pass, and returns the instantiated graph.  Replay with
+ * flg_graph_launch; the real point count is read from *n_real at replay time.
+ * No counterpart in the reference. */
+int flg_bucket_graph_create(int kind, double alpha_re, double alpha_im, const double *points, const double *eps,
+                            const int64_t *n_real, int64_t n_cap, double mu_re, double *K, float *K32, int64_t ld32,
+                            int mode, float *dinv, int *flags, void *work, size_t work_bytes, void *stream,
+                            void **graph_exec);
+int flg_graph_launch(void *graph_exec, void *stream);
+int flg_graph_destroy(void *graph_exec);
 
 /* ---- dense helpers --------------------------------------------------------
  * y = A x (FP64, row-major n_rows x n_cols, ld); used for residuals. */

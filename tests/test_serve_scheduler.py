@@ -1,0 +1,94 @@
+"""Scheduling of the solve server, on the host only (device work replaced by fakes):
+admission by the HBM budget, eviction of idle plans, bucket affinity, no deadlock."""
+import threading
+import time
+
+import numpy as np
+import pytest
+
+import fluidlets_gb300 as fl
+from fluidlets_gb300.serve import ResistanceRequest, Result, SolveServer, SwimmerRequest, bucket_of, plan_bytes
+
+
+class _Plan:
+    def __init__(self, nbp, kind):
+        self.nbp, self.kind = nbp, kind
+
+
+class FakeServer(SolveServer):
+    def __init__(self, *a, **k):
+        self.peak = 0
+        self.switches = 0
+        self.concurrent = 0
+        self.max_concurrent = 0
+        self._lock2 = threading.Lock()
+        super().__init__(*a, **k)
+
+    def _device(self):
+        return 0
+
+    def _make_stream(self):
+        return None
+
+    def _run_request(self, slot, stream, req, b):
+        with self._lock2:
+            self.concurrent += 1
+            self.max_concurrent = max(self.max_concurrent, self.concurrent)
+        with self._cv:
+            self.peak = max(self.peak, self._used)
+            if isinstance(req, ResistanceRequest):
+                p = self._plans[slot]
+                if p is None or p.nbp != b:
+                    self._plans[slot] = _Plan(b, 0)
+                    self.switches += 1
+        time.sleep(0.001)
+        with self._lock2:
+            self.concurrent -= 1
+        return Result(None, 0.0, 0, 0, 0, slot, b)
+
+
+def mix(n, seed, sizes=(200, 700, 1500, 3000)):
+    rng = np.random.default_rng(seed)
+    out = []
+    shape = fl.SwimmerShape(np.zeros((50, 3)), np.zeros((50, 3)), np.zeros((200, 3)))
+    for _ in range(n):
+        if rng.random() < 0.25:
+            out.append(SwimmerRequest(shape, np.zeros(3), np.eye(3), 0.1))
+        else:
+            N = int(rng.choice(sizes))
+            out.append(ResistanceRequest(fl.Stokeslet3D(), np.zeros((N, 3)), np.zeros((N, 3)), 0.1))
+    return out
+
+
+@pytest.mark.parametrize("budget_gb", [0.05, 0.3, 1.0, 150.0])
+def test_everything_completes_within_the_budget(budget_gb):
+    reqs = mix(200, 1)
+    with FakeServer(slots=4, hbm_budget_gb=budget_gb) as srv:
+        futs = [srv.submit(r) for r in reqs]
+        res = [f.result(timeout=60) for f in futs]
+        peak, used = srv.peak, srv._used
+    assert len(res) == len(reqs)
+    largest = max(plan_bytes(bucket_of(len(r.points))) for r in reqs if isinstance(r, ResistanceRequest))
+    # over budget only while a single request larger than the budget runs alone
+    assert peak <= max(budget_gb * 2**30, largest + 16 * 156**2 + (64 << 20))
+    assert used >= 0
+
+
+def test_tight_budget_serializes_and_large_budget_overlaps():
+    reqs = mix(120, 2)
+    with FakeServer(slots=4, hbm_budget_gb=0.05) as srv:
+        [f.result(timeout=60) for f in [srv.submit(r) for r in reqs]]
+        tight = srv.max_concurrent
+    with FakeServer(slots=4, hbm_budget_gb=150.0) as srv:
+        [f.result(timeout=60) for f in [srv.submit(r) for r in reqs]]
+        wide = srv.max_concurrent
+    assert tight <= 2 and wide >= 3
+
+
+def test_bucket_affinity_limits_replanning():
+    reqs = mix(300, 3, sizes=(500, 2500))  # two buckets
+    with FakeServer(slots=4, hbm_budget_gb=150.0, lookahead=16) as srv:
+        [f.result(timeout=60) for f in [srv.submit(r) for r in reqs]]
+        switches = srv.switches
+    n_res = sum(isinstance(r, ResistanceRequest) for r in reqs)
+    assert switches < n_res / 4
