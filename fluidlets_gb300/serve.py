@@ -94,7 +94,7 @@ def plan_bytes(nb_points: int) -> int:
 class BucketPlan:
     """Device buffers and the captured assemble + factor graph of one bucket size."""
 
-    def __init__(self, kernel, nb_points: int, mu: float, lu: str, stream: torch.cuda.Stream):
+    def __init__(self, kernel, nb_points: int, mu: float, lu: str, stream):
         L = load()
         self.kernel, self.mu, self.lu, self.nbp = kernel, mu, lu, nb_points
         self.kind, self.are, self.aim = kernel_params(kernel)
@@ -186,10 +186,16 @@ class BucketPlan:
 
 
 class SolveServer:
-    """Continuous-batching server: submit() returns a Future of a Result."""
+    """Continuous-batching server: submit() returns a Future of a Result.
+
+    Bucket plans live in a shared pool, counted against the HBM budget: a
+    plan is checked out by one slot for one request and then returned; free
+    plans are evicted least-recently-used when a new plan or a swimmer system
+    needs the memory.  The scheduler takes the oldest request, preferring,
+    within a look-ahead window, one whose bucket has a free plan."""
 
     def __init__(self, slots: int = 6, hbm_budget_gb: float = 150.0, rtol: float = 1e-10, graphs: bool = True,
-                 lu: str = "auto", lookahead: int = 8):
+                 lu: str = "auto", lookahead: int = 16):
         self.slots = slots
         self.budget = int(hbm_budget_gb * 2**30)
         self.rtol = rtol
@@ -198,13 +204,14 @@ class SolveServer:
         self.lookahead = lookahead
         self._pending = []            # [(request, future, t_arrival, bucket)]
         self._cv = threading.Condition()
-        self._used = 0                # bytes held by slot plans and in-flight swimmer solves
-        self._held = [0] * slots      # plan bytes held per slot
-        self._busy = [False] * slots  # slot is running a request
-        self._plans = [None] * slots  # current BucketPlan per slot
+        self._used = 0                # bytes of pooled plans + in-flight swimmer systems
+        self._free = {}               # plan key -> [free BucketPlan], most recently used last
+        self._lru = []                # free plans, least recently used first
+        self._busy = [False] * slots
         self._tuned = {}              # (kernel kind, bucket) -> "tf32" | "bf16"
-        self.stats = {"graph_replays": 0, "eager_factors": 0, "captures": 0, "capture_errors": []}
         self._closed = False
+        self.stats = {"graph_replays": 0, "eager_factors": 0, "captures": 0, "capture_errors": [], "plans_built": 0,
+                      "plans_evicted": 0}
         self._dev = self._device()
         self._threads = [threading.Thread(target=self._worker, args=(s,), daemon=True) for s in range(slots)]
         for t in self._threads:
@@ -233,49 +240,50 @@ class SolveServer:
     def __exit__(self, *a):
         self.close()
 
-    # ---- scheduling -----------------------------------------------------------------
-    def _evict_idle(self, keep_slot=None):
-        """Drop the bucket plans of idle slots (their device memory returns to the pool)."""
-        for s in range(self.slots):
-            if not self._busy[s] and self._held[s] > 0 and s != keep_slot:
-                self._plans[s] = None
-                self._used -= self._held[s]
-                self._held[s] = 0
+    # ---- plan pool (lock held) ----------------------------------------------------------
+    def _key(self, req, b):
+        lu = self._lu_for(req, b) or "tune"
+        return (kernel_params(req.kernel)[0], b, float(req.mu), lu)
+
+    def _evict_free(self, need):
+        """Free least-recently-used idle plans until `need` more bytes fit the budget."""
+        while self._used + need > self.budget and self._lru:
+            plan = self._lru.pop(0)
+            self._free[plan.key].remove(plan)
+            self._used -= plan_bytes(plan.nbp)
+            self.stats["plans_evicted"] += 1
 
     def _pick(self, slot):
-        """Oldest admissible request, preferring the slot's current bucket within the lookahead window.
-        Called with the lock held; returns None when the HBM budget does not allow it yet."""
-        plan = self._plans[slot]
+        """Oldest admissible request, preferring one with a free plan within the look-ahead window.
+        Returns (request, future, t_arrival, bucket, plan or None, reserved bytes) or None."""
         cand = None
         for k, (req, fut, t, b) in enumerate(self._pending[: self.lookahead]):
-            if plan is not None and isinstance(req, ResistanceRequest) and b == plan.nbp and \
-                    kernel_params(req.kernel)[0] == plan.kind:
+            if isinstance(req, ResistanceRequest) and self._free.get(self._key(req, b)):
                 cand = k
                 break
         if cand is None:
             cand = 0
         req, fut, t, b = self._pending[cand]
-        same = isinstance(req, ResistanceRequest) and plan is not None and plan.nbp == b and \
-            kernel_params(req.kernel)[0] == plan.kind
-
-        def cost():
-            if isinstance(req, ResistanceRequest):
-                return 0 if same else plan_bytes(b) - self._held[slot]
+        if isinstance(req, ResistanceRequest):
+            key = self._key(req, b)
+            if self._free.get(key):
+                plan = self._free[key].pop()
+                self._lru.remove(plan)
+                self._pending.pop(cand)
+                self._busy[slot] = True
+                return req, fut, t, b, plan, 0
+            need = plan_bytes(b)
+        else:
             n = 3 * len(req.shape.x) + 6
-            return 16 * n * n + (64 << 20)
-
-        delta = cost()
-        if self._used + delta > self.budget:
-            self._evict_idle(keep_slot=slot if same else None)
-            delta = cost()
-            if self._used + delta > self.budget and any(self._busy):
+            need = 16 * n * n + (64 << 20)
+        if self._used + need > self.budget:
+            self._evict_free(need)
+            if self._used + need > self.budget and any(self._busy):
                 return None  # wait until running requests release memory
         self._pending.pop(cand)
-        self._used += delta
+        self._used += need
         self._busy[slot] = True
-        if isinstance(req, ResistanceRequest) and not same:
-            self._held[slot] = plan_bytes(b)
-        return req, fut, t, b, (delta if isinstance(req, SwimmerRequest) else 0)
+        return req, fut, t, b, None, need
 
     # ---- device hooks (overridden by the scheduler's CPU test) ---------------------------
     def _device(self):
@@ -285,14 +293,14 @@ class SolveServer:
         torch.cuda.set_device(self._dev)
         return torch.cuda.Stream()
 
-    def _run_request(self, slot, stream, req, b):
+    def _run_request(self, slot, stream, req, b, plan):
         with torch.cuda.stream(stream):
             if isinstance(req, ResistanceRequest):
-                res = self._resistance(slot, stream, req, b)
+                res, plan = self._resistance(slot, stream, req, b, plan)
             else:
                 res = self._swimmer(stream, req)
             stream.synchronize()
-        return res
+        return res, plan
 
     def _worker(self, slot):
         stream = self._make_stream()
@@ -306,22 +314,25 @@ class SolveServer:
                     elif self._closed:
                         return
                     self._cv.wait(timeout=0.05)
-            req, fut, t_arr, b, reserved = item
+            req, fut, t_arr, b, plan, reserved = item
             t0 = time.perf_counter()
             try:
-                res = self._run_request(slot, stream, req, b)
+                res, plan = self._run_request(slot, stream, req, b, plan)
                 res.t_arrival, res.t_start, res.t_done, res.slot = t_arr, t0, time.perf_counter(), slot
                 fut.set_result(res)
+                with self._cv:
+                    if isinstance(req, ResistanceRequest) and plan is not None:
+                        plan.key = self._key(req, b)
+                        self._free.setdefault(plan.key, []).append(plan)
+                        self._lru.append(plan)
+                    else:
+                        self._used -= reserved  # swimmer systems are transient
             except Exception as e:  # noqa: BLE001 - delivered to the caller
-                if isinstance(req, ResistanceRequest):  # drop the slot's plan and its reservation
-                    with self._cv:
-                        self._plans[slot] = None
-                        self._used -= self._held[slot]
-                        self._held[slot] = 0
+                with self._cv:
+                    self._used -= reserved if reserved else (plan_bytes(b) if plan is not None else 0)
                 fut.set_exception(e)
             finally:
                 with self._cv:
-                    self._used -= reserved  # swimmer systems are transient
                     self._busy[slot] = False
                     self._cv.notify_all()
 
@@ -329,10 +340,9 @@ class SolveServer:
     def _lu_for(self, req, b):
         if self.lu != "auto":
             return self.lu
-        key = (kernel_params(req.kernel)[0], b)
-        return self._tuned.get(key)
+        return self._tuned.get((kernel_params(req.kernel)[0], b))
 
-    def _resistance(self, slot, stream, req, b):
+    def _resistance(self, slot, stream, req, b, plan):
         from .core import _evaluate_dev
 
         dev = torch.device("cuda", self._dev)
@@ -341,44 +351,42 @@ class SolveServer:
         N = X.shape[0]
         e = torch.full((N,), float(req.eps), dtype=torch.float64, device=dev) if np.ndim(req.eps) == 0 else \
             torch.as_tensor(np.asarray(req.eps, dtype=np.float64)).to(dev)
-        lu = self._lu_for(req, b)
-        plan = self._plans[slot]
-        if lu is None:  # autotune this bucket: time TF32 and BF16, keep the faster that converges
-            best = None
-            for mode in ("tf32", "bf16"):
-                p = BucketPlan(req.kernel, b, req.mu, mode, stream)
-                stream.synchronize()  # only this slot's stream: another slot may be capturing a graph
-                t0 = time.perf_counter()
-                p.factor(X, e)
-                x, it, outer, resid = p.solve(U, self.rtol)
-                stream.synchronize()
-                dt = time.perf_counter() - t0
-                if resid <= self.rtol and (best is None or dt < best[0]):
-                    best = (dt, mode)
-                del p
-            lu = best[1] if best else "tf32"
-            self._tuned[(kernel_params(req.kernel)[0], b)] = lu
-            plan = None
-        if plan is None or plan.nbp != b or plan.kind != kernel_params(req.kernel)[0] or plan.lu != lu \
-                or plan.mu != req.mu:
-            self._plans[slot] = None
-            del plan
+        if plan is None:
+            lu = self._lu_for(req, b)
+            if lu is None:  # autotune this bucket: time TF32 and BF16, keep the faster that converges
+                best = None
+                for mode in ("tf32", "bf16"):
+                    p = BucketPlan(req.kernel, b, req.mu, mode, stream)
+                    stream.synchronize()  # only this slot's stream: another slot may be capturing a graph
+                    t0 = time.perf_counter()
+                    p.factor(X, e)
+                    x, it, outer, resid = p.solve(U, self.rtol)
+                    stream.synchronize()
+                    dt = time.perf_counter() - t0
+                    if resid <= self.rtol and (best is None or dt < best[0]):
+                        best = (dt, mode)
+                    del p
+                lu = best[1] if best else "tf32"
+                with self._cv:
+                    self._tuned[(kernel_params(req.kernel)[0], b)] = lu
             plan = BucketPlan(req.kernel, b, req.mu, lu, stream)
+            with self._cv:
+                self.stats["plans_built"] += 1
             if self.graphs:
+                plan.stream = stream
                 plan.capture()
                 with self._cv:
                     self.stats["captures"] += 1
                     if plan.graph is None:
                         self.stats["capture_errors"].append(getattr(plan, "capture_error", "?"))
-            with self._cv:
-                self._plans[slot] = plan  # its bytes were reserved in _pick (self._held[slot])
+        plan.stream = stream  # a pooled plan runs on the stream of the slot that checked it out
         plan.factor(X, e)
         with self._cv:
             self.stats["graph_replays" if plan.graph is not None else "eager_factors"] += 1
         F, it, outer, resid = plan.solve(U, self.rtol)
         Kf = _evaluate_dev(req.kernel, X, X, F, e, req.mu, "fp64").reshape(-1)
         r = float(torch.linalg.vector_norm(Kf - U.reshape(-1)) / torch.linalg.vector_norm(U))
-        return Result(F.cpu().numpy(), r, 0, 0, 0, slot, b, lu, outer)
+        return Result(F.cpu().numpy(), r, 0, 0, 0, slot, b, plan.lu, outer), plan
 
     def _swimmer(self, stream, req):
         from .swimming import swimming_problem
@@ -441,6 +449,7 @@ def bench_serving(args):
     out = {"workload": f"served mixed workload: {n_req} requests (75% rigid bodies N log-uniform [256, 6144], "
                        "25% biflagellate swimmers), Poisson arrivals, HBM budget 150 GB", "rates": []}
     with SolveServer(slots=6) as srv:
+        srv_stats = srv.stats
         # warm-up and autotuning of the buckets in use, outside the timed runs
         warm = {}
         for r in reqs:
@@ -469,6 +478,7 @@ def bench_serving(args):
                     "max_residual": float(resid.max()) if len(resid) else None}
             out["rates"].append(line)
             print(json.dumps(line), flush=True)
+    out["server_stats"] = {k: (v if not isinstance(v, list) else len(v)) for k, v in srv_stats.items()}
     # one-solve-at-a-time FP64 GPU service times on a stratified sample
     sample = reqs[:: max(1, len(reqs) // 48)]
     times = []
