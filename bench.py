@@ -52,6 +52,8 @@ def parse():
                    help="wall_sum (default, the headline) or one of the other benchmark configurations")
     p.add_argument("--n-points", type=int, default=None, help="override the point count of brinkman_gmres / wall_lu")
     p.add_argument("--fp64", action="store_true", help="also run the plain FP64 GPU solve (slow at full size)")
+    p.add_argument("--slots", type=int, default=6, help="solve-server slots (serve workload)")
+    p.add_argument("--rates", default="50,200,800", help="Poisson arrival rates (serve workload)")
     return p.parse_args()
 
 

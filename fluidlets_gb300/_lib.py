@@ -55,13 +55,14 @@ SIGNATURES = {
                           c_double, c_int, c_int, c_int, c_double, POINTER(c_int), POINTER(c_int),
                           POINTER(c_double), _P, c_size_t, _P]),
     "flg_gmres_ir_dense_workspace": (c_size_t, [c_int64, c_int]),
-    "flg_gmres_ir_dense": (c_int, [c_int64, _P, c_int64, _P, c_int64, _P, _P, _P, c_double, c_int, c_int,
+    "flg_gmres_ir_dense": (c_int, [c_int64, _P, c_int64, _P, c_int64, _P, c_int64, _P, _P, _P, c_double, c_int, c_int,
                                    POINTER(c_int), POINTER(c_int), POINTER(c_double), _P, c_size_t, _P]),
-    "flg_bucket_graph_create": (c_int, [c_int, c_double, c_double, _P, _P, _P, c_int64, c_double, _P, _P, c_int64,
+    "flg_bucket_graph_create": (c_int, [c_int, c_double, c_double, _P, _P, _P, c_int64, c_double, _P, _P, _P, c_int64,
                                         c_int, _P, _P, _P, c_size_t, _P, POINTER(c_void_p)]),
     "flg_graph_launch": (c_int, [_P, _P]),
     "flg_graph_destroy": (c_int, [_P]),
     "flg_gemv_f64": (c_int, [c_int64, c_int64, _P, c_int64, _P, _P, _P]),
+    "flg_gemv_f32": (c_int, [c_int64, c_int64, _P, c_int64, _P, _P, _P]),
     "flg_convert_f64_f32": (c_int, [c_int64, c_int64, _P, c_int64, _P, c_int64, _P]),
     "flg_measure_peaks": (c_int, [POINTER(c_double), POINTER(c_double), _P]),
     "flg_profile_enable": (c_int, [c_int]),

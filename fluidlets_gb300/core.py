@@ -234,12 +234,14 @@ def _lu_solve_dev(K: torch.Tensor, U: torch.Tensor) -> torch.Tensor:
 
 def _lowp_factor_dev(K: torch.Tensor, lu_mode: str):
     """FP32 copy of K (leading dimension padded to 32) factored without pivoting
-    on the tensor cores; returns (K32, ld32, dinv)."""
+    on the tensor cores; returns (K32, ld32, dinv, A32) with A32 an unfactored FP32
+    copy of K for the inner matvecs of GMRES-IR."""
     n = K.shape[0]
     L = load()
     ld32 = (n + 31) // 32 * 32
     K32 = torch.empty((n, ld32), dtype=torch.float32, device=K.device)
     check(L.flg_convert_f64_f32(n, n, dv.ptr(K), K.stride(0), dv.ptr(K32), ld32, dv.stream()), "convert")
+    A32 = K32.clone()
     dinv = torch.empty(L.flg_lu_lowp_dinv_elems(n), dtype=torch.float32, device=K.device)
     mode = LU_MODE[lu_mode]
     nbytes = L.flg_lu_factor_lowp_workspace(n, mode)
@@ -247,7 +249,7 @@ def _lowp_factor_dev(K: torch.Tensor, lu_mode: str):
     info = ctypes.c_int(0)
     check(L.flg_lu_factor_lowp(n, dv.ptr(K32), ld32, mode, dv.ptr(dinv), ctypes.byref(info), dv.ptr(ws), nbytes,
                                dv.stream()), "low-precision LU")
-    return K32, ld32, dinv
+    return K32, ld32, dinv, A32
 
 
 def _accept(status, resid, required, what):
@@ -258,15 +260,17 @@ def _accept(status, resid, required, what):
     check(status, what)
 
 
-def _gmres_ir_dense_dev(K, K32, ld32, dinv, b, rtol, restart, maxiter, required=None):
-    """FP64 GMRES-IR on the dense FP64 K, preconditioned by the low-precision factors."""
+def _gmres_ir_dense_dev(K, K32, ld32, dinv, b, rtol, restart, maxiter, required=None, A32=None):
+    """FP64 GMRES-IR on the dense FP64 K, preconditioned by the low-precision factors
+    (inner matvecs on the FP32 copy A32 when given)."""
     n = K.shape[0]
     L = load()
     x = torch.zeros_like(b)
     nbytes = L.flg_gmres_ir_dense_workspace(n, restart)
     ws = dv.workspace(nbytes)
     iters, outer, resid = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_double(0.0)
-    st = L.flg_gmres_ir_dense(n, dv.ptr(K), K.stride(0), dv.ptr(K32), ld32, dv.ptr(dinv), dv.ptr(b), dv.ptr(x), rtol,
+    st = L.flg_gmres_ir_dense(n, dv.ptr(K), K.stride(0), dv.ptr(A32), ld32, dv.ptr(K32), ld32, dv.ptr(dinv), dv.ptr(b),
+                              dv.ptr(x), rtol,
                               restart, maxiter, ctypes.byref(iters), ctypes.byref(outer), ctypes.byref(resid),
                               dv.ptr(ws), nbytes, dv.stream())
     _accept(st, resid.value, rtol if required is None else required, "GMRES-IR")
@@ -275,9 +279,9 @@ def _gmres_ir_dense_dev(K, K32, ld32, dinv, b, rtol, restart, maxiter, required=
 
 def _mixed_lu_solve_dev(K: torch.Tensor, U: torch.Tensor, rtol, restart, maxiter, lu_mode, required=None):
     """TF32/BF16 tensor-core LU of K (no pivoting) + FP64 GMRES iterative refinement."""
-    K32, ld32, dinv = _lowp_factor_dev(K, lu_mode)
+    K32, ld32, dinv, A32 = _lowp_factor_dev(K, lu_mode)
     b = U.reshape(-1).to(torch.float64).contiguous()
-    return _gmres_ir_dense_dev(K, K32, ld32, dinv, b, rtol, restart, maxiter, required)
+    return _gmres_ir_dense_dev(K, K32, ld32, dinv, b, rtol, restart, maxiter, required, A32=A32)
 
 
 def _gmres_dev(kernel, X, e, mu, b, rtol, restart, maxiter, precision, inner_rtol=1e-6, required=None):
@@ -336,7 +340,8 @@ def resistance(kernel, points, velocities, eps, mu=1.0, method="auto", rtol=1e-1
     if method == "lu":
         K = _assemble_dev(kernel, X, X, e, mu)
         if prec == PREC["mixed"] and not K.is_complex() and not Uc:
-            f, iterations, ir_steps, _ = _mixed_lu_solve_dev(K, U, rtol_ir, restart, maxiter, lu, required=rtol)
+            # the refinement's last residual is ||U - K f|| / ||U|| with the FP64 K: reported as is
+            f, iterations, ir_steps, resid = _mixed_lu_solve_dev(K, U, rtol_ir, restart, maxiter, lu, required=rtol)
         else:
             f = _lu_solve_dev(K, U.to(K.dtype) if K.is_complex() else U)
             iterations = 1

@@ -315,6 +315,34 @@ __global__ void __launch_bounds__(256) gemv_f64_kernel(int64_t nr, int64_t nc, c
     if (lane == 0) y[row] = acc;
 }
 
+// y (FP64) = A (FP32, row-major) x (FP64), FP64 accumulation; warp per row
+__global__ void __launch_bounds__(256) gemv_f32_kernel(int64_t nr, int64_t nc, const float *A, int64_t ld,
+                                                       const double *x, double *y) {
+    const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (row >= nr) return;
+    const float *a = A + row * ld;
+    double acc = 0.0;
+    if ((ld % 4 == 0) && (((uintptr_t)A & 15) == 0) && (((uintptr_t)x & 15) == 0)) {
+        const float4 *a4 = (const float4 *)a;
+        const double2 *x2 = (const double2 *)x;
+        const int64_t nc4 = nc / 4;
+        for (int64_t c = lane; c < nc4; c += 32) {
+            const float4 v = __ldcs(a4 + c);
+            const double2 x01 = x2[2 * c], x23 = x2[2 * c + 1];
+            acc = fma((double)v.x, x01.x, acc);
+            acc = fma((double)v.y, x01.y, acc);
+            acc = fma((double)v.z, x23.x, acc);
+            acc = fma((double)v.w, x23.y, acc);
+        }
+        for (int64_t c = 4 * nc4 + lane; c < nc; c += 32) acc = fma((double)a[c], x[c], acc);
+    } else {
+        for (int64_t c = lane; c < nc; c += 32) acc = fma((double)a[c], x[c], acc);
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) y[row] = acc;
+}
+
 __global__ void convert_f64_f32_kernel(int64_t nr, int64_t nc, const double *src, int64_t lds, float *dst,
                                        int64_t ldd) {
     const int64_t r = blockIdx.y;
@@ -502,6 +530,18 @@ extern "C" int flg_gemv_f64(int64_t n_rows, int64_t n_cols, const double *A, int
     cudaStream_t st = as_stream(stream);
     prof_begin(FLG_SLOT_GEMV, st);
     gemv_f64_kernel<<<(unsigned)ceil_div(n_rows * 32, 256), 256, 0, st>>>(n_rows, n_cols, A, ld, x, y);
+    FLG_LAUNCH_CHECK();
+    prof_end(FLG_SLOT_GEMV, st);
+    return FLG_OK;
+}
+
+extern "C" int flg_gemv_f32(int64_t n_rows, int64_t n_cols, const float *A, int64_t ld, const double *x, double *y,
+                            void *stream) {
+    FLG_REQUIRE(n_rows >= 0 && n_cols >= 0 && ld >= n_cols, "bad GEMV shape");
+    if (n_rows == 0) return FLG_OK;
+    cudaStream_t st = as_stream(stream);
+    prof_begin(FLG_SLOT_GEMV, st);
+    gemv_f32_kernel<<<(unsigned)ceil_div(n_rows * 32, 256), 256, 0, st>>>(n_rows, n_cols, A, ld, x, y);
     FLG_LAUNCH_CHECK();
     prof_end(FLG_SLOT_GEMV, st);
     return FLG_OK;

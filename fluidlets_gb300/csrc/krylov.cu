@@ -578,8 +578,8 @@ extern "C" size_t flg_gmres_ir_dense_workspace(int64_t n, int restart) {
     return c.bytes();
 }
 
-extern "C" int flg_gmres_ir_dense(int64_t n, const double *A, int64_t ld, const float *LU32, int64_t ld32,
-                                  const float *dinv, const double *b, double *x, double rtol, int restart, int maxiter, int *iters,
+extern "C" int flg_gmres_ir_dense(int64_t n, const double *A, int64_t ld, const float *A32, int64_t lda32,
+                                  const float *LU32, int64_t ld32, const float *dinv, const double *b, double *x, double rtol, int restart, int maxiter, int *iters,
                                   int *outer, double *resid, void *work, size_t work_bytes, void *stream) {
     FLG_REQUIRE(n >= 0 && ld >= n && ld32 >= n && restart >= 1 && maxiter >= 1, "bad GMRES-IR arguments");
     FLG_REQUIRE(iters && outer && resid, "null output pointer");
@@ -597,9 +597,13 @@ extern "C" int flg_gmres_ir_dense(int64_t n, const double *A, int64_t ld, const 
     const size_t lsb = lu_solve_lowp_bytes(n);
     char *lw = ar.take<char>(lsb);
     FLG_REQUIRE(d && lw, "workspace too small for GMRES-IR");
-    auto Aop = [&](const double *v, double *out) { return flg_gemv_f64(n, n, A, ld, v, out, st); };
-    g.A = Aop;
-    gi.A = Aop;
+    // outer residuals with the FP64 matrix; inner (preconditioned, tolerance 1e-4) matvecs
+    // with the FP32 copy when the caller provides one
+    g.A = [&](const double *v, double *out) { return flg_gemv_f64(n, n, A, ld, v, out, st); };
+    if (A32)
+        gi.A = [&](const double *v, double *out) { return flg_gemv_f32(n, n, A32, lda32, v, out, st); };
+    else
+        gi.A = g.A;
     gi.M = [&](const double *v, double *out) { return lu_solve_lowp_apply(n, LU32, ld32, dinv, v, out, lw, lsb, st); };
     double bn;
     FLG_TRY(g.norm(b, &bn));

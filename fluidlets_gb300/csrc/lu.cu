@@ -685,26 +685,15 @@ __device__ __forceinline__ void cp_async16(void *dst, const void *src) {
                  : "memory");
 }
 
-// stage one 128 x 128 block inverse into shared memory (asynchronous)
-__device__ __forceinline__ void stage_dinv(float *dst, const float *src) {
-    for (int e = threadIdx.x * 4; e < kNB * kNB; e += blockDim.x * 4) cp_async16(dst + e, src + e);
-    asm volatile("cp.async.commit_group;" ::: "memory");
-}
-
+// The kernel keeps its footprint small (1 KB of shared memory, 256 threads)
+// so that its cooperative launch can co-reside with other streams' kernels.
 __global__ void __launch_bounds__(256) lowp_apply_kernel(ApplyArgs a) {
-    extern __shared__ float4 dyn4[];
-    float *Dbuf = (float *)dyn4;  // 2 x 128 x 128
     __shared__ float yb[kNB], xb[kNB];
     const int nblk = (int)ceil_div(a.n, kNB);
     const int nwarp_tot = gridDim.x * (blockDim.x >> 5);
     const int gwarp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
     const int total = 2 * nblk;
-    // step t: forward block t (t < nblk), backward block 2 nblk - 1 - t
-    auto dinv_of = [&](int t) {
-        const int k = t < nblk ? t : 2 * nblk - 1 - t;
-        return (t < nblk ? a.Linv : a.Uinv) + (int64_t)k * kNB * kNB;
-    };
-    stage_dinv(Dbuf, dinv_of(0));
     for (int t = 0; t < total; t++) {
         const bool fwd = t < nblk;
         const int k = fwd ? t : 2 * nblk - 1 - t;
@@ -712,19 +701,26 @@ __global__ void __launch_bounds__(256) lowp_apply_kernel(ApplyArgs a) {
         const int bs = (int)min((int64_t)kNB, a.n - b0);
         const float *src = fwd ? a.y : a.z;  // backward pass reads the forward result
         for (int q = threadIdx.x; q < bs; q += blockDim.x) yb[q] = ((volatile float *)src)[b0 + q];
-        if (t + 1 < total) {
-            stage_dinv(Dbuf + ((t + 1) & 1) * kNB * kNB, dinv_of(t + 1));
-            asm volatile("cp.async.wait_group 1;" ::: "memory");
-        } else {
-            asm volatile("cp.async.wait_group 0;" ::: "memory");
-        }
         __syncthreads();
-        const float *Dk = Dbuf + (t & 1) * kNB * kNB;
-        for (int r = threadIdx.x >> 5; r < bs; r += blockDim.x >> 5) {  // warp per row
-            float acc = 0.0f;
-            for (int q = lane; q < bs; q += 32) acc = fmaf(Dk[r * kNB + q], yb[q], acc);
-            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (lane == 0) xb[r] = acc;
+        // x_b = Dinv_b y_b: each warp takes 16 rows, all row loads issued before the reductions
+        const float *Dk = (fwd ? a.Linv : a.Uinv) + (int64_t)k * kNB * kNB;
+        for (int rb = warp * 16; rb < bs; rb += nwarp * 16) {
+            float v[16][4];
+#pragma unroll
+            for (int i = 0; i < 16; i++)
+#pragma unroll
+                for (int c = 0; c < 4; c++) v[i][c] = Dk[(rb + i) * kNB + lane + 32 * c];
+#pragma unroll
+            for (int i = 0; i < 16; i++) {
+                float acc = 0.0f;
+#pragma unroll
+                for (int c = 0; c < 4; c++) {
+                    const int q = lane + 32 * c;
+                    acc = fmaf(v[i][c], q < bs ? yb[q] : 0.0f, acc);
+                }
+                for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+                if (lane == 0 && rb + i < bs) xb[rb + i] = acc;
+            }
         }
         __syncthreads();
         if (blockIdx.x == 0)
@@ -759,10 +755,7 @@ __global__ void __launch_bounds__(256) lowp_apply_kernel(ApplyArgs a) {
                 if (lane == 0 && rb + i < r1) atomicAdd((float *)&tgt[rb + i], -acc);
             }
         }
-        if (!grid_sync(a.bar, gridDim.x)) {
-            asm volatile("cp.async.wait_group 0;" ::: "memory");
-            return;
-        }
+        if (!grid_sync(a.bar, gridDim.x)) return;
     }
 }
 
@@ -795,15 +788,10 @@ int lu_solve_lowp_apply(int64_t n, const float *LU, int64_t ld, const float *din
     FLG_CUDA(cudaMemsetAsync(bar, 0, sizeof(GridBar), st));
     const int64_t nblk = ceil_div(n, kNB);
     ApplyArgs aa{LU, ld, n, dinv, dinv + nblk * kNB * kNB, y, z, bar};
-    const size_t smem = 2 * (size_t)kNB * kNB * sizeof(float);
-    FLG_CUDA(cudaFuncSetAttribute(lowp_apply_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int per_sm = 0;
-    FLG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lowp_apply_kernel, 256, smem));
-    FLG_REQUIRE(per_sm >= 1, "preconditioner kernel does not fit on an SM");
     const int grid = sm_count();
     void *args[] = {&aa};
     prof_begin(FLG_SLOT_LU_SOLVE, st);
-    FLG_CUDA(cudaLaunchCooperativeKernel((void *)lowp_apply_kernel, dim3(grid), dim3(256), args, smem, st));
+    FLG_CUDA(cudaLaunchCooperativeKernel((void *)lowp_apply_kernel, dim3(grid), dim3(256), args, 0, st));
     count_launch();
     prof_end(FLG_SLOT_LU_SOLVE, st);
     // after the backward pass the solution is in y

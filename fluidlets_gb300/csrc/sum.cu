@@ -612,7 +612,11 @@ static void split_plan(int64_t M, int64_t N, int targets_per_cta, int tile, int 
     S = ceil_div(N, split_len);
 }
 
-static inline int far_tpt(int kind, int nf, bool ck) { return (nf == 1 && !ck) ? 2 : 1; }
+// targets per thread of the FP32 far-field kernel for real strengths and kernels
+#ifndef FLG_FAR_TPT
+#define FLG_FAR_TPT 2
+#endif
+static inline int far_tpt(int kind, int nf, bool ck) { return (nf == 1 && !ck) ? FLG_FAR_TPT : 1; }
 
 void sum_layout(int kind, int64_t M, int64_t N, int nf, bool ck, int precision, SumLayout &L) {
     L.nf = nf;
@@ -723,7 +727,7 @@ static int launch_sum(const SumRun &r, const SumLayout &L, int precision, const 
     // mixed: strengths into the packed slots, FP32 far field, FP64 near field + combine
     pack_strengths_kernel<<<(unsigned)ceil_div(r.N, 256), 256, 0, st>>>(r.f, r.N, NF, p->packed);
     FLG_LAUNCH_CHECK();
-    constexpr int TPT = (NF == 1 && !CK) ? 2 : 1;
+    constexpr int TPT = (NF == 1 && !CK) ? FLG_FAR_TPT : 1;
     FarArgs fa{r.tg, r.M, p->packed, r.N, L.split_len, (float)r.alpha_re, (float)r.alpha_im, p->partial};
     dim3 grid((unsigned)ceil_div(r.M, kF32Threads * TPT), (unsigned)L.S);
     prof_begin(FLG_SLOT_FAR_F32, st);

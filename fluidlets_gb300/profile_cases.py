@@ -87,8 +87,9 @@ def breakdown(a, kern):
     for rep in range(a.reps):
         L.flg_profile_enable(1)
         K, t_asm = t(lambda: core._assemble_dev(kern, Xd, Xd, e, 1.0))
-        (K32, ld32, dinv), t_lu = t(lambda: core._lowp_factor_dev(K, a.lu))
-        (x, it, outer, res), t_ir = t(lambda: core._gmres_ir_dense_dev(K, K32, ld32, dinv, b, 1e-10, 60, 200))
+        (K32, ld32, dinv, A32), t_lu = t(lambda: core._lowp_factor_dev(K, a.lu))
+        (x, it, outer, res), t_ir = t(lambda: core._gmres_ir_dense_dev(K, K32, ld32, dinv, b, 1e-12, 60, 200,
+                                                                        required=1e-10, A32=A32))
         _, t_res = t(lambda: core._evaluate_dev(kern, Xd, Xd, x.reshape(-1, 3), e, 1.0, "fp64"))
         slots = {}
         for name, k in _lib.SLOT.items():

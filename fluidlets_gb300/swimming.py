@@ -82,8 +82,8 @@ def swimming_problem(shape: SwimmerShape, x0, B, eps, mu=1.0, kernel=None, neare
     rhs = torch.zeros(3 * N + 6, dtype=torch.float64, device=A.device)
     rhs[:3 * N] = torch.from_numpy(v.ravel()).to(A.device)
     if _prec(precision) == 1:
-        K32, ld32, dinv = _lowp_factor_dev(A, lu)
-        sol, *_ = _gmres_ir_dense_dev(A, K32, ld32, dinv, rhs, rtol * 1e-2, 60, 200, required=rtol)
+        K32, ld32, dinv, A32 = _lowp_factor_dev(A, lu)
+        sol, *_ = _gmres_ir_dense_dev(A, K32, ld32, dinv, rhs, rtol * 1e-2, 60, 200, required=rtol, A32=A32)
     else:
         sol = _lu_solve_dev(A, rhs)
     sol = dv.to_host(sol)

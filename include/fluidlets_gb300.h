@@ -239,33 +239,40 @@ int flg_gmres(int kind, double alpha_re, double alpha_im,
               int *iters, int *outer, double *resid,
               void *work, size_t work_bytes, void *stream);
 
-/* Dense GMRES-IR: solves A x = b (n x n FP64 row-major, ld) to rtol with an
- * FP64 residual and FP64 GEMV matvecs, preconditioned (left) by the
- * low-precision factors of flg_lu_factor_lowp (LU32, ld32, dinv).  Real only.
- * iters = total inner iterations, outer = refinement steps. Synchronizes. */
+/* Dense GMRES-IR: solves A x = b (n x n FP64 row-major, ld) to rtol with
+ * FP64 residuals b - A x (FP64 GEMV), correcting with inner GMRES (tolerance
+ * 1e-4) on the operator M^-1 A, M = the low-precision factors of
+ * flg_lu_factor_lowp (LU32, ld32, dinv).  The inner matvecs use A32 (an FP32
+ * copy of A, leading dimension lda32) when it is not NULL, else A.  Real
+ * only.  iters = total inner iterations, outer = refinement steps, resid =
+ * final ||b - A x|| / ||b|| with the FP64 A.  Synchronizes. */
 size_t flg_gmres_ir_dense_workspace(int64_t n, int restart);
-int flg_gmres_ir_dense(int64_t n, const double *A, int64_t ld, const float *LU32, int64_t ld32,
-                       const float *dinv, const double *b, double *x, double rtol, int restart, int maxiter,
-                       int *iters, int *outer, double *resid,
+int flg_gmres_ir_dense(int64_t n, const double *A, int64_t ld, const float *A32, int64_t lda32,
+                       const float *LU32, int64_t ld32, const float *dinv, const double *b, double *x,
+                       double rtol, int restart, int maxiter, int *iters, int *outer, double *resid,
                        void *work, size_t work_bytes, void *stream);
 
 /* ---- captured graphs (solve server) ---------------------------------------
  * Captures flg_assemble_bucket -> flg_convert_f64_f32 -> flg_lu_factor_lowp_async
- * over fixed buffers (K: 3 n_cap x 3 n_cap FP64, K32 with ld32, dinv, flags[2],
+ * over fixed buffers (K: 3 n_cap x 3 n_cap FP64; A32 (optional) and K32, FP32 copies
+ * with ld32, the second factored in place; dinv, flags[2],
  * LU workspace) on `stream` (not the default stream) in thread-local capture
  * mode, after one eager pass, and returns the instantiated graph.  Replay with
  * flg_graph_launch; the real point count is read from *n_real at replay time.
  * No counterpart in the reference. */
 int flg_bucket_graph_create(int kind, double alpha_re, double alpha_im, const double *points, const double *eps,
-                            const int64_t *n_real, int64_t n_cap, double mu_re, double *K, float *K32, int64_t ld32,
-                            int mode, float *dinv, int *flags, void *work, size_t work_bytes, void *stream,
-                            void **graph_exec);
+                            const int64_t *n_real, int64_t n_cap, double mu_re, double *K, float *A32, float *K32,
+                            int64_t ld32, int mode, float *dinv, int *flags, void *work, size_t work_bytes,
+                            void *stream, void **graph_exec);
 int flg_graph_launch(void *graph_exec, void *stream);
 int flg_graph_destroy(void *graph_exec);
 
 /* ---- dense helpers --------------------------------------------------------
  * y = A x (FP64, row-major n_rows x n_cols, ld); used for residuals. */
 int flg_gemv_f64(int64_t n_rows, int64_t n_cols, const double *A, int64_t ld, const double *x, double *y,
+                 void *stream);
+/* y (FP64) = A (FP32, row-major n_rows x n_cols, ld) x (FP64), FP64 accumulation. */
+int flg_gemv_f32(int64_t n_rows, int64_t n_cols, const float *A, int64_t ld, const double *x, double *y,
                  void *stream);
 /* dst (FP32, ldd) = (float) src (FP64, lds), n_rows x n_cols */
 int flg_convert_f64_f32(int64_t n_rows, int64_t n_cols, const double *src, int64_t lds, float *dst, int64_t ldd,

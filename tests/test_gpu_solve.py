@@ -153,7 +153,8 @@ def test_lowp_lu_factors(mode, n):
     rng = np.random.default_rng(n)
     A = rng.normal(size=(n, n)) / np.sqrt(n) + 4.0 * np.eye(n)  # no pivoting needed
     K = torch.tensor(A, device="cuda")
-    K32, ld32, dinv = _lowp_factor_dev(K, mode)
+    K32, ld32, dinv, A32 = _lowp_factor_dev(K, mode)
+    assert torch.equal(A32[:, :n], K.float())  # unfactored copy for the inner matvecs
     LU = K32[:, :n].double().cpu().numpy()
     Lm = np.tril(LU, -1) + np.eye(n)
     Um = np.triu(LU)
@@ -161,6 +162,27 @@ def test_lowp_lu_factors(mode, n):
     tol = {"fp32": 1e-6, "tf32": 2e-3, "bf16": 2e-2}[mode]
     assert err < tol, err
     del X
+
+
+@pytest.mark.parametrize("rows,cols", [(1, 1), (5, 3), (97, 250), (1536, 1536), (3000, 4099)])
+def test_gemv_f64_and_f32(rows, cols):
+    L = _lib.load()
+    rng = np.random.default_rng(rows + cols)
+    A = rng.normal(size=(rows, cols))
+    x = rng.normal(size=cols)
+    ld = (cols + 31) // 32 * 32
+    Ad = torch.zeros((rows, ld), dtype=torch.float64, device="cuda")
+    Ad[:, :cols] = torch.tensor(A)
+    A32 = Ad.float()
+    xd = torch.tensor(x, device="cuda")
+    y = torch.empty(rows, dtype=torch.float64, device="cuda")
+    _lib.check(L.flg_gemv_f64(rows, cols, dv.ptr(Ad), ld, dv.ptr(xd), dv.ptr(y), dv.stream()))
+    ref = A @ x
+    scale = np.abs(A) @ np.abs(x)
+    assert np.all(np.abs(y.cpu().numpy() - ref) <= 1e-13 * scale + 1e-300)
+    _lib.check(L.flg_gemv_f32(rows, cols, dv.ptr(A32), ld, dv.ptr(xd), dv.ptr(y), dv.stream()))
+    ref32 = A32[:, :cols].double().cpu().numpy() @ x  # FP32 matrix entries, FP64 products and sums
+    assert np.all(np.abs(y.cpu().numpy() - ref32) <= 1e-13 * scale + 1e-300)
 
 
 # ---- resistance ------------------------------------------------------------------------
