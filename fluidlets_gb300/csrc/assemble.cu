@@ -302,7 +302,16 @@ __global__ void __launch_bounds__(256) gemv_f64_kernel(int64_t nr, int64_t nc, c
         const double2 *a2 = (const double2 *)a;
         const double2 *x2 = (const double2 *)x;
         const int64_t nc2 = nc / 2;
-        for (int64_t c = lane; c < nc2; c += 32) {
+        int64_t c = lane;
+        // four independent 16-byte loads in flight per lane
+        for (; c + 96 < nc2; c += 128) {
+            double2 av[4], xv[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) av[u] = __ldcs(a2 + c + 32 * u), xv[u] = x2[c + 32 * u];
+#pragma unroll
+            for (int u = 0; u < 4; u++) acc = fma(av[u].y, xv[u].y, fma(av[u].x, xv[u].x, acc));
+        }
+        for (; c < nc2; c += 32) {
             const double2 av = __ldcs(a2 + c), xv = x2[c];
             acc = fma(av.x, xv.x, acc);
             acc = fma(av.y, xv.y, acc);
@@ -327,7 +336,23 @@ __global__ void __launch_bounds__(256) gemv_f32_kernel(int64_t nr, int64_t nc, c
         const float4 *a4 = (const float4 *)a;
         const double2 *x2 = (const double2 *)x;
         const int64_t nc4 = nc / 4;
-        for (int64_t c = lane; c < nc4; c += 32) {
+        int64_t c = lane;
+        // four independent 16-byte loads of A in flight per lane
+        for (; c + 96 < nc4; c += 128) {
+            float4 v[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) v[u] = __ldcs(a4 + c + 32 * u);
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int64_t cc = c + 32 * u;
+                const double2 x01 = x2[2 * cc], x23 = x2[2 * cc + 1];
+                acc = fma((double)v[u].x, x01.x, acc);
+                acc = fma((double)v[u].y, x01.y, acc);
+                acc = fma((double)v[u].z, x23.x, acc);
+                acc = fma((double)v[u].w, x23.y, acc);
+            }
+        }
+        for (; c < nc4; c += 32) {
             const float4 v = __ldcs(a4 + c);
             const double2 x01 = x2[2 * c], x23 = x2[2 * c + 1];
             acc = fma((double)v.x, x01.x, acc);

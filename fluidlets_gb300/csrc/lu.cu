@@ -332,197 +332,210 @@ __global__ void trsv_update_kernel(const double *LU, int64_t ld, double *B, int6
 }
 
 // ---- low precision (FP32) no-pivot LU ----------------------------------------------
-// One CTA factors the nb x nb diagonal block (nb <= 128, padded with the
-// identity to 128) in shared memory, blocked in 32 x 32 sub-blocks:
-//   per sub-block step s: warp 0 factors D[s][s]; warps solve the panels
-//   U[s][t] = L[s][s]^-1 D[s][t] and L[t][s] = D[t][s] U[s][s]^-1; all threads
-//   update the trailing sub-blocks.
-// Then the inverses of L (unit lower) and U (upper) by block recursion:
-//   diagonal 32 x 32 inverses by single warps, off-diagonal blocks level by
-//   level:  Linv[t][s] = -Linv[t][t] sum_{q=s}^{t-1} L[t][q] Linv[q][s],
-//           Uinv[s][t] = -Uinv[s][s] sum_{q=s+1}^{t} U[s][q] Uinv[q][t].
-// L, U go back to A; Linv, Uinv (full 128 x 128) to dinv.
+// One CTA (16 warps) factors the nb x nb diagonal block (nb <= 128, padded with
+// the identity to 128) in shared memory, in 32 x 32 sub-blocks, and builds the
+// inverses of its L and U factors alongside (they precondition the panels and
+// the solves).  With X = inv(L) and Y = inv(U) started at the identity, step s:
+//   warp 0:  D[s][s] = L_ss U_ss in registers (lane = row, pivot row by
+//            shuffles); the same eliminations applied to the identity give
+//            inv(L_ss) -> X[s][s] (Gauss-Jordan), and a backward sweep gives
+//            inv(U_ss) -> Y[s][s];
+//   stage 1: U panel D[s][t] = X[s][s] D[s][t], L panel D[t][s] = D[t][s] Y[s][s]
+//            (t > s); X[s][q] = X[s][s] X[s][q], Y[q][s] = Y[q][s] Y[s][s] (q < s);
+//   stage 2: D[t][u] -= D[t][s] D[s][u] (t, u > s);
+//            X[t][q] -= D[t][s] X[s][q] (t > s, q <= s);
+//            Y[q][u] -= Y[q][s] D[s][u] (q <= s, u > s).
+// (X <- inv(L_s) X and Y <- Y inv(U_s) for the block-column / block-row factors
+// L = L_0 L_1 L_2 L_3, U = U_3 U_2 U_1 U_0.)  Every stage-1/2 product is a
+// 32 x 32 x 32 block product split into two warp tasks (16-row or 16-column
+// halves, 4 x 4 outputs per lane, float4 operand loads); the row stride kLD
+// keeps rows 16-byte aligned and the loads free of bank conflicts.
 constexpr int kSB = 32;          // sub-block
 constexpr int kNS = kNB / kSB;   // sub-blocks per side (4)
-constexpr int kPD = kNB + 1;     // padded shared-memory row stride
-constexpr size_t kDiagSmem = (3 * (size_t)kNB * kPD + 2 * (kNS - 1) * kSB * kSB) * sizeof(float);
+constexpr int kLD = kNB + 4;     // shared-memory row stride (floats)
+constexpr size_t kDiagSmem = 3 * (size_t)kNB * kLD * sizeof(float);
+
+__device__ __forceinline__ float *sblk(float *M, int i, int j) { return M + i * kSB * kLD + j * kSB; }
+
+// One warp: C (=|-=) A B over k = 32, C of (128 / CG) rows x (4 CG) columns, 4 x 4
+// per lane.  C may alias A when CG = 8 (row halves read only their own rows of A)
+// or B when CG = 4 (column halves read only their own columns of B): all operands
+// are read before the first store.
+template <int CG, bool SUB>
+__device__ __forceinline__ void warp_mm(const float *A, const float *B, float *C, int lane) {
+    const int r0 = (lane / CG) * 4, c0 = (lane % CG) * 4;
+    float acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        if (SUB) {
+            const float4 v = *reinterpret_cast<const float4 *>(C + (r0 + i) * kLD + c0);
+            acc[i][0] = v.x, acc[i][1] = v.y, acc[i][2] = v.z, acc[i][3] = v.w;
+        } else {
+#pragma unroll
+            for (int j = 0; j < 4; j++) acc[i][j] = 0.0f;
+        }
+    }
+#pragma unroll 2
+    for (int k = 0; k < kSB; k += 4) {
+        float a[4][4], b[4][4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const float4 v = *reinterpret_cast<const float4 *>(A + (r0 + i) * kLD + k);
+            a[i][0] = SUB ? -v.x : v.x, a[i][1] = SUB ? -v.y : v.y, a[i][2] = SUB ? -v.z : v.z,
+            a[i][3] = SUB ? -v.w : v.w;
+            const float4 w = *reinterpret_cast<const float4 *>(B + (k + i) * kLD + c0);
+            b[i][0] = w.x, b[i][1] = w.y, b[i][2] = w.z, b[i][3] = w.w;
+        }
+#pragma unroll
+        for (int kk = 0; kk < 4; kk++)
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int j = 0; j < 4; j++) acc[i][j] = fmaf(a[i][kk], b[kk][j], acc[i][j]);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+        *reinterpret_cast<float4 *>(C + (r0 + i) * kLD + c0) = make_float4(acc[i][0], acc[i][1], acc[i][2], acc[i][3]);
+    __syncwarp();
+}
+
+// One warp factors the 32 x 32 block P in place without pivoting and writes
+// inv(L) to Xb, inv(U) to Yb (lane = row).  A zero or non-finite pivot of a real
+// (not padding) row records its 1-based global index in *info.
+__device__ __forceinline__ void warp_lu32(float *P, float *Xb, float *Yb, int lane, int row0, int nb, int64_t k0,
+                                          int *info) {
+    constexpr unsigned kAll = 0xffffffffu;
+    float d[kSB], x[kSB];
+#pragma unroll
+    for (int c = 0; c < kSB; c += 4) {
+        const float4 v = *reinterpret_cast<const float4 *>(P + lane * kLD + c);
+        d[c] = v.x, d[c + 1] = v.y, d[c + 2] = v.z, d[c + 3] = v.w;
+    }
+#pragma unroll
+    for (int c = 0; c < kSB; c++) x[c] = (c == lane) ? 1.0f : 0.0f;
+#pragma unroll
+    for (int j = 0; j < kSB; j++) {
+        const float piv = __shfl_sync(kAll, d[j], j);
+        const bool ok = piv != 0.0f && isfinite(piv);
+        if (!ok && lane == 0 && row0 + j < nb) atomicCAS(info, 0, (int)(k0 + row0 + j + 1));
+        const float rp = ok ? 1.0f / piv : 0.0f;
+        const bool below = lane > j;
+        const float l = d[j] * rp;
+#pragma unroll
+        for (int c = 0; c < kSB; c++) {
+            if (c == j) continue;
+            // pivot row j: U part right of the diagonal, inv(L) part left of it
+            const float v = __shfl_sync(kAll, c > j ? d[c] : x[c], j);
+            if (below) {
+                if (c > j) d[c] = fmaf(-l, v, d[c]);
+                else x[c] = fmaf(-l, v, x[c]);
+            }
+        }
+        if (below) {
+            x[j] -= l;
+            d[j] = l;
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < kSB; c += 4) {
+        *reinterpret_cast<float4 *>(P + lane * kLD + c) = make_float4(d[c], d[c + 1], d[c + 2], d[c + 3]);
+        *reinterpret_cast<float4 *>(Xb + lane * kLD + c) = make_float4(x[c], x[c + 1], x[c + 2], x[c + 3]);
+    }
+    // inv(U): backward Gauss-Jordan on [U | I]; row j is scaled by 1/U[j][j], then
+    // rows above subtract U[i][j] times it (column j of U above the diagonal is
+    // untouched by the later pivots, so d[j] still holds U[i][j]).
+    float y[kSB];
+#pragma unroll
+    for (int c = 0; c < kSB; c++) y[c] = (c == lane) ? 1.0f : 0.0f;
+#pragma unroll
+    for (int j = kSB - 1; j >= 0; j--) {
+        const float piv = __shfl_sync(kAll, d[j], j);
+        const float rp = (piv != 0.0f && isfinite(piv)) ? 1.0f / piv : 0.0f;
+        const float u = d[j];
+#pragma unroll
+        for (int c = j; c < kSB; c++) {
+            const float v = __shfl_sync(kAll, y[c], j) * rp;
+            if (lane == j) y[c] = v;
+            else if (lane < j) y[c] = fmaf(-u, v, y[c]);
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < kSB; c += 4)
+        *reinterpret_cast<float4 *>(Yb + lane * kLD + c) = make_float4(y[c], y[c + 1], y[c + 2], y[c + 3]);
+}
 
 __global__ void __launch_bounds__(512) diag_lowp_kernel(float *A, int64_t ld, int64_t k0, int nb, float *Linv,
                                                         float *Uinv, int *info) {
-    extern __shared__ float sm[];
-    float *D = sm, *Li = sm + kNB * kPD, *Ui = sm + 2 * kNB * kPD, *T = sm + 3 * kNB * kPD;
+    extern __shared__ __align__(16) float sm[];
+    float *D = sm, *X = sm + kNB * kLD, *Y = sm + 2 * kNB * kLD;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, nthr = blockDim.x, nwarp = nthr >> 5;
     for (int e = tid; e < kNB * kNB; e += nthr) {
         const int r = e / kNB, c = e - r * kNB;
-        D[r * kPD + c] = (r < nb && c < nb) ? A[(k0 + r) * ld + k0 + c] : (r == c ? 1.0f : 0.0f);
-        Li[r * kPD + c] = 0.0f;
-        Ui[r * kPD + c] = 0.0f;
+        D[r * kLD + c] = (r < nb && c < nb) ? A[(k0 + r) * ld + k0 + c] : (r == c ? 1.0f : 0.0f);
+        X[r * kLD + c] = 0.0f;
+        Y[r * kLD + c] = 0.0f;
     }
     __syncthreads();
-    // ---- phase A: right-looking LU without pivoting over the whole block.
-    // Thread t owns two 4 x 4 tiles in registers: tile rows/cols (tr, tc) with
-    // tc = t % 32 and tr = t / 32 and t / 32 + 16.  Step j: the owners of
-    // column j form the multipliers (pivot row j published in shared memory by
-    // the previous step) and publish them; every thread updates its tiles; the
-    // owners of row j + 1 publish it.  Two barriers per column.
-    {
-        __shared__ float rowj[2][kNB], colj[kNB];
-        float a[2][4][4];
-        const int tc = tid & 31;
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-            const int tr = (tid >> 5) + 16 * h;
-#pragma unroll
-            for (int i = 0; i < 4; i++)
-#pragma unroll
-                for (int c = 0; c < 4; c++) a[h][i][c] = D[(4 * tr + i) * kPD + 4 * tc + c];
-        }
-        if (tid < kNB) rowj[0][tid] = D[tid];  // row 0
+    for (int s = 0; s < kNS; s++) {
+        const int m = kNS - 1 - s;  // sub-blocks after s
+        if (warp == 0) warp_lu32(sblk(D, s, s), sblk(X, s, s), sblk(Y, s, s), lane, s * kSB, nb, k0, info);
         __syncthreads();
-        for (int j = 0; j < kNB; j++) {
-            const float *rj = rowj[j & 1];
-            const float piv = rj[j];
-            const bool ok = piv != 0.0f && isfinite(piv);
-            if (!ok && tid == 0 && j < nb) atomicCAS(info, 0, (int)(k0 + j + 1));
-            const float rp = ok ? 1.0f / piv : 0.0f;
-            // owners of column j: multipliers for rows below j
-            if (tc == (j >> 2)) {
-                const int cc = j & 3;
-#pragma unroll
-                for (int h = 0; h < 2; h++) {
-                    const int tr = (tid >> 5) + 16 * h;
-#pragma unroll
-                    for (int i = 0; i < 4; i++) {
-                        const int r = 4 * tr + i;
-                        float v = cc == 0 ? a[h][i][0] : cc == 1 ? a[h][i][1] : cc == 2 ? a[h][i][2] : a[h][i][3];
-                        if (r > j) {
-                            v *= rp;
-                            if (cc == 0) a[h][i][0] = v;
-                            else if (cc == 1) a[h][i][1] = v;
-                            else if (cc == 2) a[h][i][2] = v;
-                            else a[h][i][3] = v;
-                        }
-                        colj[r] = (r > j) ? v : 0.0f;
-                    }
-                }
-            }
-            __syncthreads();
-            // rank-1 update of the trailing part: a[r][c] -= l_r u_c for r > j, c > j
-            float u[4];
-#pragma unroll
-            for (int c = 0; c < 4; c++) u[c] = (4 * tc + c > j) ? rj[4 * tc + c] : 0.0f;
-#pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const int tr = (tid >> 5) + 16 * h;
-                if (4 * tr + 3 <= j) continue;
-#pragma unroll
-                for (int i = 0; i < 4; i++) {
-                    const float l = colj[4 * tr + i];
-#pragma unroll
-                    for (int c = 0; c < 4; c++) a[h][i][c] = fmaf(-l, u[c], a[h][i][c]);
-                }
-            }
-            // publish row j + 1 (final after this update) into the other buffer
-            if (j + 1 < kNB) {
-                const int r = j + 1, tr_need = r >> 2, i = r & 3;
-#pragma unroll
-                for (int h = 0; h < 2; h++) {
-                    if ((tid >> 5) + 16 * h == tr_need) {
-#pragma unroll
-                        for (int c = 0; c < 4; c++) {
-                            const float v = i == 0 ? a[h][0][c] : i == 1 ? a[h][1][c] : i == 2 ? a[h][2][c] : a[h][3][c];
-                            rowj[(j + 1) & 1][4 * tc + c] = v;
-                        }
-                    }
-                }
-            }
-            __syncthreads();
-        }
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-            const int tr = (tid >> 5) + 16 * h;
-#pragma unroll
-            for (int i = 0; i < 4; i++)
-#pragma unroll
-                for (int c = 0; c < 4; c++) D[(4 * tr + i) * kPD + 4 * tc + c] = a[h][i][c];
-        }
-        __syncthreads();
-    }
-    // ---- phase B: inverses; diagonal sub-blocks first (warp per block, lane = column)
-    for (int task = warp; task < 2 * kNS; task += nwarp) {
-        const int o = (task % kNS) * kSB, c = lane;
-        if (task < kNS) {  // unit lower: X[i][c] = delta - sum_{c<=q<i} L[i][q] X[q][c]
-            for (int i = 0; i < kSB; i++) {
-                float v = (i == c) ? 1.0f : 0.0f;
-                if (i > c) {
-#pragma unroll 4
-                    for (int q = c; q < i; q++) v = fmaf(-D[(o + i) * kPD + o + q], Li[(o + q) * kPD + o + c], v);
-                }
-                Li[(o + i) * kPD + o + c] = (i < c) ? 0.0f : v;
-            }
-        } else {  // upper, bottom up
-            for (int ii = kSB - 1; ii >= 0; ii--) {
-                float v = 0.0f;
-                if (ii <= c) {
-                    v = (ii == c) ? 1.0f : 0.0f;
-#pragma unroll 4
-                    for (int q = ii + 1; q <= c; q++) v = fmaf(-D[(o + ii) * kPD + o + q], Ui[(o + q) * kPD + o + c], v);
-                    v = v / D[(o + ii) * kPD + o + ii];
-                }
-                Ui[(o + ii) * kPD + o + c] = v;
-            }
-        }
-    }
-    __syncthreads();
-    for (int d = 1; d < kNS; d++) {
-        const int npair = kNS - d;  // pairs (s, s + d), for Linv and for Uinv
-        // T = sum_q L[t][q] Linv[q][s]   |   T = sum_q U[s][q] Uinv[q][t]
-        for (int e = tid; e < 2 * npair * kSB * kSB; e += nthr) {
-            const int p = e / (kSB * kSB), i = (e / kSB) % kSB, j = e % kSB;
-            const bool lower = p < npair;
-            const int s = lower ? p : p - npair, t = s + d;
-            float acc = 0.0f;
-            if (lower) {
-                for (int q = s * kSB; q < t * kSB; q++) acc = fmaf(D[(t * kSB + i) * kPD + q], Li[q * kPD + s * kSB + j], acc);
+        // stage 1: 2m + 2s block products, two half tasks each
+        for (int t = warp; t < 2 * (2 * m + 2 * s); t += nwarp) {
+            const int b = t >> 1, h = (t & 1) * 16;
+            if (b < m) {  // U panel, C = B: column halves
+                float *C = sblk(D, s, s + 1 + b) + h;
+                warp_mm<4, false>(sblk(X, s, s), C, C, lane);
+            } else if (b < 2 * m) {  // L panel, C = A: row halves
+                float *C = sblk(D, s + 1 + (b - m), s) + h * kLD;
+                warp_mm<8, false>(C, sblk(Y, s, s), C, lane);
+            } else if (b < 2 * m + s) {
+                float *C = sblk(X, s, b - 2 * m) + h;
+                warp_mm<4, false>(sblk(X, s, s), C, C, lane);
             } else {
-                for (int q = (s + 1) * kSB; q < (t + 1) * kSB; q++)
-                    acc = fmaf(D[(s * kSB + i) * kPD + q], Ui[q * kPD + t * kSB + j], acc);
+                float *C = sblk(Y, b - 2 * m - s, s) + h * kLD;
+                warp_mm<8, false>(C, sblk(Y, s, s), C, lane);
             }
-            T[p * kSB * kSB + i * kSB + j] = acc;
         }
         __syncthreads();
-        // Linv[t][s] = -Linv[t][t] T   |   Uinv[s][t] = -Uinv[s][s] T
-        for (int e = tid; e < 2 * npair * kSB * kSB; e += nthr) {
-            const int p = e / (kSB * kSB), i = (e / kSB) % kSB, j = e % kSB;
-            const bool lower = p < npair;
-            const int s = lower ? p : p - npair, t = s + d;
-            float acc = 0.0f;
-            const float *Tp = T + p * kSB * kSB;
-            if (lower) {
-                for (int k = 0; k < kSB; k++) acc = fmaf(Li[(t * kSB + i) * kPD + t * kSB + k], Tp[k * kSB + j], acc);
-                Li[(t * kSB + i) * kPD + s * kSB + j] = -acc;
+        // stage 2: m^2 + 2 m (s + 1) block updates, row halves
+        const int nD = m * m, nX = m * (s + 1);
+        for (int t = warp; t < 2 * (nD + 2 * nX); t += nwarp) {
+            const int b = t >> 1, h = (t & 1) * 16;
+            if (b < nD) {
+                const int i = b / m, j = b - (b / m) * m;
+                warp_mm<8, true>(sblk(D, s + 1 + i, s) + h * kLD, sblk(D, s, s + 1 + j),
+                                 sblk(D, s + 1 + i, s + 1 + j) + h * kLD, lane);
+            } else if (b < nD + nX) {
+                const int i = (b - nD) / (s + 1), q = (b - nD) % (s + 1);
+                warp_mm<8, true>(sblk(D, s + 1 + i, s) + h * kLD, sblk(X, s, q), sblk(X, s + 1 + i, q) + h * kLD,
+                                 lane);
             } else {
-                for (int k = 0; k < kSB; k++) acc = fmaf(Ui[(s * kSB + i) * kPD + s * kSB + k], Tp[k * kSB + j], acc);
-                Ui[(s * kSB + i) * kPD + t * kSB + j] = -acc;
+                const int q = (b - nD - nX) / m, j = (b - nD - nX) % m;
+                warp_mm<8, true>(sblk(Y, q, s) + h * kLD, sblk(D, s, s + 1 + j), sblk(Y, q, s + 1 + j) + h * kLD,
+                                 lane);
             }
         }
         __syncthreads();
     }
     for (int e = tid; e < kNB * kNB; e += nthr) {
         const int r = e / kNB, c = e - r * kNB;
-        if (r < nb && c < nb) A[(k0 + r) * ld + k0 + c] = D[r * kPD + c];
-        Linv[r * kNB + c] = Li[r * kPD + c];
-        Uinv[r * kNB + c] = Ui[r * kPD + c];
+        if (r < nb && c < nb) A[(k0 + r) * ld + k0 + c] = D[r * kLD + c];
+        Linv[r * kNB + c] = X[r * kLD + c];
+        Uinv[r * kNB + c] = Y[r * kLD + c];
     }
 }
 
 // Panels of one LU step, in place, in one launch (CTA x < ntu: U tiles, else L tiles):
 //   U12[:, 32-col tile] = Linv (128 x 128) * A12[:, tile]  (all 128 rows per CTA; also
-//                         written transposed into Ut (nr x 128, K-major) for the tensor cores)
+//                         written transposed into Ut (nr rows of 128, row stride ldu, K-major)
+//                         for the tensor cores)
 //   L21[32-row tile, :] = A21[tile, :] * Uinv (128 x 128)  (all 128 columns per CTA)
 // Each CTA reads its whole input tile before writing it back, so in place is safe.
 __global__ void __launch_bounds__(256) lowp_panel_kernel(float *A, int64_t ld, int64_t k0, int64_t nr,
-                                                         const float *Linv, const float *Uinv, float *Ut, int ntu) {
+                                                         const float *Linv, const float *Uinv, float *Ut, int64_t ldu,
+                                                         int ntu) {
     __shared__ float tile[kNB][33];  // U: [row][col]; L: stored as [col][row]
     const int64_t c0 = k0 + kNB;
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
@@ -547,7 +560,7 @@ __global__ void __launch_bounds__(256) lowp_panel_kernel(float *A, int64_t ld, i
             for (int k = 0; k < 16; k++) {
                 const int r = w + 8 * k;
                 A[(k0 + r) * ld + c0 + j0 + lane] = acc[k];
-                Ut[(j0 + lane) * kNB + r] = acc[k];
+                Ut[(j0 + lane) * ldu + r] = acc[k];
             }
         }
     } else {
@@ -642,10 +655,10 @@ __global__ void transpose_f32_kernel(const float *src, int64_t lds, float *dst, 
     }
 }
 
-// tensor-core trailing update (tc_gemm.cu): C (m x nc, ldc) -= Lp (m x nb, ldl) * Ut^T (nc x nb)
-size_t tc_update_bytes(int64_t m, int64_t nc, int mode);
-int tc_update(float *C, int64_t ldc, const float *Lp, int64_t ldl, const float *Ut, int64_t m, int64_t nc, int mode,
-              void *work, size_t work_bytes, cudaStream_t st, int *err_dev);
+// tensor-core update (tc_gemm.cu): C (m x nc, ldc) -= Lp (m x K, ldl) * Ut^T (nc x K, ldu), K % 128 == 0
+size_t tc_update_bytes(int64_t m, int64_t nc, int64_t K, int mode);
+int tc_update(float *C, int64_t ldc, const float *Lp, int64_t ldl, const float *Ut, int64_t ldu, int64_t m,
+              int64_t nc, int64_t K, int mode, void *work, size_t work_bytes, cudaStream_t st, int *err_dev);
 
 static int sgemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, float alpha, const float *A, int64_t lda,
                  const float *B, int64_t ldb, float beta, float *C, int64_t ldc) {
@@ -929,13 +942,24 @@ extern "C" int flg_lu_solve_f64(int64_t n, int64_t nrhs, const double *LU, int64
 // ---- low-precision LU entry points ----------------------------------------------------
 extern "C" int64_t flg_lu_lowp_dinv_elems(int64_t n) { return 2 * ceil_div(std::max<int64_t>(n, 1), kNB) * kNB * kNB; }
 
+// Tensor-core modes defer most of the trailing update: blocks are grouped into
+// outer panels of kOuter x 128 columns [K0, E).  Inner step k0 (diagonal block,
+// panels) updates only the L-shaped part of the Schur complement that the next
+// inner steps read -- rows > k0 x columns (k0, E), and rows (k0, E) x columns
+// >= E -- with rank-128 updates; the rest, rows and columns >= E, receives one
+// rank-(E - K0) update per outer panel, which moves the trailing matrix through
+// HBM kOuter times less often.  The K-major copy of U (UtB: one row of
+// kOuter x 128 per column >= K0) feeds both.
+constexpr int kOuter = 4;
+constexpr int kOuterW = kOuter * kNB;
+
 template <class Ar>
-static void lowp_carve(Ar &ar, int64_t n, int mode, float **U12, float **L21, float **U12T, char **tcw,
+static void lowp_carve(Ar &ar, int64_t n, int mode, float **U12, float **L21, float **UtB, char **tcw,
                        size_t *tcb) {
     *U12 = ar.template take<float>((size_t)kNB * n);
     *L21 = ar.template take<float>((size_t)n * kNB);
-    *U12T = ar.template take<float>((size_t)n * kNB);
-    *tcb = (mode == FLG_LU_FP32) ? 0 : tc_update_bytes(n, n, mode);
+    *UtB = ar.template take<float>((size_t)n * kOuterW);
+    *tcb = (mode == FLG_LU_FP32) ? 0 : tc_update_bytes(n, n, kOuterW, mode);
     *tcw = ar.template take<char>(*tcb);
 }
 
@@ -958,11 +982,11 @@ extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mod
     if (n == 0) return FLG_OK;
     FLG_REQUIRE(A && dinv, "null pointer");
     Arena ar(work, work_bytes);
-    float *U12, *L21, *U12T;
+    float *U12, *L21, *UtB;
     char *tcw;
     size_t tcb;
-    lowp_carve(ar, n, mode, &U12, &L21, &U12T, &tcw, &tcb);
-    FLG_REQUIRE(U12 && L21 && U12T && (tcb == 0 || tcw), "workspace too small for LU (%zu bytes)", work_bytes);
+    lowp_carve(ar, n, mode, &U12, &L21, &UtB, &tcw, &tcb);
+    FLG_REQUIRE(U12 && L21 && UtB && (tcb == 0 || tcw), "workspace too small for LU (%zu bytes)", work_bytes);
     int *dinfo = flags;  // [0] first bad pivot, [1] tensor-core wait timed out
     const size_t dsmem = kDiagSmem;
     static bool attr_set = false;  // set once, so a later call can be captured in a graph
@@ -970,24 +994,32 @@ extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mod
         FLG_CUDA(cudaFuncSetAttribute(diag_lowp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem));
         attr_set = true;
     }
+    const bool tc = mode != FLG_LU_FP32;
     const int64_t nblk = ceil_div(n, kNB);
     float *Linv = dinv, *Uinv = dinv + nblk * kNB * kNB;
-    for (int64_t k = 0; k < nblk; k++) {
-        const int64_t k0 = k * kNB;
-        const int nb = (int)std::min<int64_t>(kNB, n - k0);
-        prof_begin(FLG_SLOT_LU_PANEL, st);
-        diag_lowp_kernel<<<1, 512, dsmem, st>>>(A, ld, k0, nb, Linv + k * kNB * kNB, Uinv + k * kNB * kNB, dinfo);
-        FLG_LAUNCH_CHECK();
-        const int64_t c0 = k0 + nb, nr = n - c0;
-        if (nr > 0) {
+    for (int64_t K0 = 0; K0 < n; K0 += kOuterW) {
+        const int64_t E = std::min<int64_t>(n, K0 + kOuterW);
+        for (int64_t k0 = K0; k0 < E; k0 += kNB) {
+            const int64_t k = k0 / kNB;
+            const int nb = (int)std::min<int64_t>(kNB, n - k0);
+            prof_begin(FLG_SLOT_LU_PANEL, st);
+            diag_lowp_kernel<<<1, 512, dsmem, st>>>(A, ld, k0, nb, Linv + k * kNB * kNB, Uinv + k * kNB * kNB, dinfo);
+            FLG_LAUNCH_CHECK();
+            const int64_t c0 = k0 + nb, nr = n - c0;
+            if (nr <= 0) {
+                prof_end(FLG_SLOT_LU_PANEL, st);
+                continue;
+            }
+            // (nb < kNB only for the last block, which has no trailing part)
             float *A12 = A + k0 * ld + c0, *A21 = A + c0 * ld + k0, *A22 = A + c0 * ld + c0;
+            float *Ut = UtB + (c0 - K0) * kOuterW + (k0 - K0);  // row: column - K0; K offset: k0 - K0
             if (nb == kNB) {
-                // U12 = Linv A12 (+ its K-major copy U12T), L21 = A21 Uinv: one launch, in place
+                // U12 = Linv A12 (+ its K-major copy), L21 = A21 Uinv: one launch, in place
                 const int ntu = (int)ceil_div(nr, 32), ntl = (int)ceil_div(nr, 32);
-                lowp_panel_kernel<<<ntu + ntl, 256, 0, st>>>(A, ld, k0, nr, Linv + k * kNB * kNB,
-                                                             Uinv + k * kNB * kNB, U12T, ntu);
+                lowp_panel_kernel<<<ntu + ntl, 256, 0, st>>>(A, ld, k0, nr, Linv + k * kNB * kNB, Uinv + k * kNB * kNB,
+                                                             Ut, kOuterW, ntu);
                 FLG_LAUNCH_CHECK();
-            } else {  // (only reachable for a partial last block, which has no trailing part)
+            } else {
                 FLG_TRY(sgemm(st, nb, nr, nb, 1.0f, Linv + k * kNB * kNB, kNB, A12, ld, 0.0f, U12, nr));
                 FLG_TRY(copy2d(st, U12, nr, A12, ld, nb, nr));
                 FLG_TRY(sgemm(st, nr, nb, nb, 1.0f, A21, ld, Uinv + k * kNB * kNB, kNB, 0.0f, L21, kNB));
@@ -995,14 +1027,23 @@ extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mod
             }
             prof_end(FLG_SLOT_LU_PANEL, st);
             prof_begin(FLG_SLOT_LU_UPDATE, st);
-            if (mode == FLG_LU_FP32 || nb < kNB) {
+            if (!tc || nb < kNB) {
                 FLG_TRY(sgemm(st, nr, nr, nb, -1.0f, A21, ld, A12, ld, 1.0f, A22, ld));
-            } else {
-                FLG_TRY(tc_update(A22, ld, A21, ld, U12T, nr, nr, mode, tcw, tcb, st, dinfo + 1));
+            } else if (E > c0) {
+                // rows > k0 x columns (k0, E)
+                FLG_TRY(tc_update(A22, ld, A21, ld, Ut, kOuterW, nr, E - c0, kNB, mode, tcw, tcb, st, dinfo + 1));
+                // rows (k0, E) x columns >= E
+                if (n > E)
+                    FLG_TRY(tc_update(A + c0 * ld + E, ld, A21, ld, Ut + (E - c0) * kOuterW, kOuterW, E - c0, n - E,
+                                      kNB, mode, tcw, tcb, st, dinfo + 1));
             }
             prof_end(FLG_SLOT_LU_UPDATE, st);
-        } else {
-            prof_end(FLG_SLOT_LU_PANEL, st);
+        }
+        if (tc && n > E) {  // the deferred rank-(E - K0) update of rows and columns >= E (E - K0 = kOuterW here)
+            prof_begin(FLG_SLOT_LU_UPDATE, st);
+            FLG_TRY(tc_update(A + E * ld + E, ld, A + E * ld + K0, ld, UtB + (E - K0) * kOuterW, kOuterW, n - E, n - E,
+                              E - K0, mode, tcw, tcb, st, dinfo + 1));
+            prof_end(FLG_SLOT_LU_UPDATE, st);
         }
     }
     return FLG_OK;

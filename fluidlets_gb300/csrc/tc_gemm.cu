@@ -1,33 +1,39 @@
-// tc_gemm.cu -- tcgen05 tensor-core rank-128 update for the low-precision LU.
+// tc_gemm.cu -- tcgen05 tensor-core rank-K update for the low-precision LU.
 //
-//   C (m x nc, FP32, row-major, ldc)  -=  A (m x 128) * B^T,  B given as Bt (nc x 128)
+//   C (m x nc, FP32, row-major, ldc)  -=  A (m x K) * B^T,  B given as Bt (nc x K)
 //
-// Both operands are K-major (K = 128 contiguous per row).  One CTA computes a
-// 128 x 128 tile of C:
-//   * thread 0 streams K-blocks of A and B (128 B = 32 TF32 or 64 BF16 per
-//     row) with TMA (cp.async.bulk.tensor, 128-byte swizzle) into a 2-stage
-//     shared-memory ring guarded by mbarriers;
-//   * thread 32 issues tcgen05.mma (cta_group::1, M = N = 128; kind::tf32, or
-//     kind::f16 with BF16 operands), accumulating in 128 TMEM columns, and
-//     releases each stage with tcgen05.commit;
-//   * all four warps read their 32 TMEM lanes (rows) with tcgen05.ld and
-//     update C in place.
+// Both operands are K-major (K contiguous per row, K a multiple of 128).  A
+// persistent kernel, one CTA per SM, walks the 128 x 128 tiles of C:
+//   * warp 0 (one lane) streams K-blocks of A and B (128 B = 32 TF32 or 64 BF16
+//     per row) with TMA (cp.async.bulk.tensor, 128-byte swizzle) into a
+//     4-stage shared-memory ring guarded by mbarriers;
+//   * warp 1 (one lane) issues tcgen05.mma (cta_group::1, M = N = 128;
+//     kind::tf32, or kind::f16 with BF16 operands) into one of two 128-column
+//     TMEM accumulators and releases each stage with tcgen05.commit;
+//   * warps 2-5 drain the other accumulator (tcgen05.ld, 32 TMEM lanes each),
+//     stage -acc in 32 x 32 swizzled boxes and add them to C with TMA
+//     reduce-add (cp.reduce.async.bulk.tensor): C is never read by the SM and
+//     the epilogue of one tile overlaps the MMAs of the next.
 // Every mbarrier wait is bounded; on a timeout the kernel raises an error
-// flag, skips the remaining work, frees its TMEM and returns.
+// flag, skips the remaining work, waits (bounded) for its own TMA loads and
+// MMAs, frees its TMEM and returns.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <mutex>
 
 #include "flg_common.cuh"
 
 namespace flg {
 
-constexpr int TC_BM = 128, TC_BN = 128, TC_K = 128, TC_STAGES = 2, TC_THREADS = 128;
+constexpr int TC_BM = 128, TC_BN = 128, TC_STAGES = 4, TC_THREADS = 192, TC_EPI_WARPS = 4;
 constexpr int TC_TILE_BYTES = 128 * 128;  // one operand tile of a K-block: 128 rows x 128 B
-constexpr uint32_t TC_TMEM_COLS = 128;
+constexpr int TC_STG_BYTES = 32 * 128;    // one 32 x 32 FP32 staging box
+constexpr uint32_t TC_TMEM_COLS = 256;    // two 128-column accumulators
 constexpr long long TC_WAIT_LIMIT = 2000000000LL;  // ~1 s of SM clock per wait
+constexpr size_t TC_SMEM = 1024 + 2 * TC_STAGES * TC_TILE_BYTES + TC_EPI_WARPS * 2 * TC_STG_BYTES;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -38,6 +44,9 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
                  : "memory");
 }
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
     uint32_t ok;
     asm volatile(
@@ -47,7 +56,7 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// bounded wait: false if the limit ran out (the error flag is raised)
+// bounded wait: false if the limit ran out (the error flag is raised) or another role raised it
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err) {
     const long long t0 = clock64();
     while (!mbar_try_wait(bar, parity)) {
@@ -59,6 +68,16 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *e
     }
     return true;
 }
+// bounded wait that ignores the error flag (draining own operations on the way out)
+__device__ __forceinline__ void mbar_drain(uint64_t *bar, uint32_t parity, int *err) {
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity)) {
+        if (clock64() - t0 > TC_WAIT_LIMIT) {
+            atomicExch(err, 1);
+            return;
+        }
+    }
+}
 
 __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar, int x, int y) {
     asm volatile(
@@ -66,6 +85,12 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, u
             smem_u32(dst)),
         "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(x), "r"(y)
         : "memory");
+}
+__device__ __forceinline__ void tma_reduce_add_2d(const CUtensorMap *map, const void *src, int x, int y) {
+    asm volatile("cp.reduce.async.bulk.tensor.2d.global.shared::cta.add.tile.bulk_group [%0, {%2, %3}], [%1];" ::"l"(
+                     (uint64_t)map),
+                 "r"(smem_u32(src)), "r"(x), "r"(y)
+                 : "memory");
 }
 
 // shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart
@@ -86,30 +111,34 @@ __host__ __device__ constexpr uint32_t tc_idesc(uint32_t fmt) {
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(TC_THREADS) tc_update_kernel(const __grid_constant__ CUtensorMap tmA,
-                                                               const __grid_constant__ CUtensorMap tmB, float *C,
-                                                               int64_t ldc, int m, int nc, int *err) {
+__global__ void __launch_bounds__(TC_THREADS, 1) tc_update_kernel(const __grid_constant__ CUtensorMap tmA,
+                                                                  const __grid_constant__ CUtensorMap tmB,
+                                                                  const __grid_constant__ CUtensorMap tmC, int m,
+                                                                  int nc, int nkb, int *err) {
     constexpr int KBLK = MODE == FLG_LU_TF32 ? 32 : 64;  // elements per 128-byte row
-    constexpr int NKB = TC_K / KBLK;                      // K-blocks
     constexpr int KSTEP_BYTES = 32;                       // one MMA consumes 32 bytes of each row
     constexpr uint32_t IDESC = tc_idesc(MODE == FLG_LU_TF32 ? 2u : 1u);
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint8_t *sA = smem, *sB = smem + TC_STAGES * TC_TILE_BYTES;
-    __shared__ __align__(8) uint64_t full[TC_STAGES], empty[TC_STAGES], done;
+    uint8_t *sA = smem, *sB = smem + TC_STAGES * TC_TILE_BYTES, *stg = smem + 2 * TC_STAGES * TC_TILE_BYTES;
+    __shared__ __align__(8) uint64_t full[TC_STAGES], empty[TC_STAGES], accf[2], acce[2], mma_done;
     __shared__ uint32_t tmem_base;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * TC_BN;
+    const int ntx = (nc + TC_BN - 1) / TC_BN, nty = (m + TC_BM - 1) / TC_BM, ntiles = ntx * nty;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < TC_STAGES; s++) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
-        mbar_init(&done, 1);
+        for (int b = 0; b < 2; b++) {
+            mbar_init(&accf[b], 1);
+            mbar_init(&acce[b], TC_EPI_WARPS);
+        }
+        mbar_init(&mma_done, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 0) {
+    if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
                      "r"(TC_TMEM_COLS)
                      : "memory");
@@ -120,106 +149,145 @@ __global__ void __launch_bounds__(TC_THREADS) tc_update_kernel(const __grid_cons
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_base;
 
-    if (threadIdx.x == 0) {
-        // producer: K-block kb goes to stage kb % 2
-        for (int kb = 0; kb < NKB; kb++) {
-            const int s = kb % TC_STAGES;
-            const uint32_t use = kb / TC_STAGES;
-            if (kb >= TC_STAGES && !mbar_wait(&empty[s], (use & 1) ^ 1, err)) break;
-            mbar_expect_tx(&full[s], 2 * TC_TILE_BYTES);
-            tma_load_2d(sA + s * TC_TILE_BYTES, &tmA, &full[s], kb * KBLK, m0);
-            tma_load_2d(sB + s * TC_TILE_BYTES, &tmB, &full[s], kb * KBLK, n0);
-        }
-    } else if (threadIdx.x == 32) {
-        // MMA issuer
-        bool ok = true;
-        for (int kb = 0; kb < NKB && ok; kb++) {
-            const int s = kb % TC_STAGES;
-            const uint32_t use = kb / TC_STAGES;
-            if (!mbar_wait(&full[s], use & 1, err)) {
-                ok = false;
-                break;
-            }
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-#pragma unroll
-            for (int kk = 0; kk < 128 / KSTEP_BYTES; kk++) {
-                const uint64_t ad = sw128_desc(sA + s * TC_TILE_BYTES + kk * KSTEP_BYTES);
-                const uint64_t bd = sw128_desc(sB + s * TC_TILE_BYTES + kk * KSTEP_BYTES);
-                const uint32_t acc = (kb | kk) ? 1u : 0u;
-                if constexpr (MODE == FLG_LU_TF32) {
-                    asm volatile(
-                        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-                        " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
-                        "l"(ad), "l"(bd), "r"(IDESC), "r"(acc)
-                        : "memory");
-                } else {
-                    asm volatile(
-                        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-                        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
-                        "l"(ad), "l"(bd), "r"(IDESC), "r"(acc)
-                        : "memory");
-                }
-            }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                             smem_u32(&empty[s]))
-                         : "memory");
-        }
-        if (ok)
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                             smem_u32(&done))
-                         : "memory");
-    }
-    __syncwarp();
-    // epilogue: every thread waits for the accumulator, then warp w owns rows m0 + 32 w + lane
-    // warp-uniform: tcgen05.ld.sync.aligned must be executed by the whole warp
-    const bool have = __all_sync(0xffffffffu, mbar_wait(&done, 0, err));
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (have) {
-        const int64_t row = (int64_t)m0 + warp * 32 + lane;
-#pragma unroll 1
-        for (int ch = 0; ch < TC_BN / 32; ch++) {
-            uint32_t v[32];
-            const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(ch * 32);
-            asm volatile(
-                "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
-                "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
-                  "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
-                  "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
-                  "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
-                : "r"(taddr));
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-            if (row < m) {
-                float *crow = C + row * ldc + n0 + ch * 32;
-                const int lim = nc - (n0 + ch * 32);
-                if (lim >= 32 && (((uintptr_t)crow & 15) == 0)) {
-#pragma unroll
-                    for (int j = 0; j < 32; j += 4) {
-                        float4 c4 = *(float4 *)(crow + j);
-                        c4.x -= __uint_as_float(v[j]);
-                        c4.y -= __uint_as_float(v[j + 1]);
-                        c4.z -= __uint_as_float(v[j + 2]);
-                        c4.w -= __uint_as_float(v[j + 3]);
-                        *(float4 *)(crow + j) = c4;
+    if (warp == 0) {
+        if (lane == 0) {  // TMA producer: global K-block counter g -> stage g % S, use g / S
+            uint32_t g = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+                const int m0 = (t / ntx) * TC_BM, n0 = (t % ntx) * TC_BN;
+                for (int kb = 0; kb < nkb; kb++, g++) {
+                    const int s = g % TC_STAGES;
+                    const uint32_t use = g / TC_STAGES;
+                    if (use > 0 && !mbar_wait(&empty[s], (use & 1) ^ 1, err)) {
+                        ok = false;
+                        break;
                     }
-                } else {
-                    for (int j = 0; j < 32 && j < lim; j++) crow[j] -= __uint_as_float(v[j]);
+                    mbar_expect_tx(&full[s], 2 * TC_TILE_BYTES);
+                    tma_load_2d(sA + s * TC_TILE_BYTES, &tmA, &full[s], kb * KBLK, m0);
+                    tma_load_2d(sB + s * TC_TILE_BYTES, &tmB, &full[s], kb * KBLK, n0);
                 }
             }
+            // the last (up to S) loads issued must have landed before the CTA exits
+            for (uint32_t q = (g > TC_STAGES ? g - TC_STAGES : 0); q < g; q++)
+                mbar_drain(&full[q % TC_STAGES], (q / TC_STAGES) & 1, err);
         }
+    } else if (warp == 1) {
+        if (lane == 0) {  // MMA issuer
+            uint32_t g = 0, i = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, i++) {
+                const uint32_t buf = i & 1, ause = i >> 1;
+                if (ause > 0 && !mbar_wait(&acce[buf], (ause & 1) ^ 1, err)) {
+                    ok = false;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t d = tmem + buf * TC_BN;
+                for (int kb = 0; kb < nkb; kb++, g++) {
+                    const int s = g % TC_STAGES;
+                    const uint32_t use = g / TC_STAGES;
+                    if (!mbar_wait(&full[s], use & 1, err)) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+                    for (int kk = 0; kk < 128 / KSTEP_BYTES; kk++) {
+                        const uint64_t ad = sw128_desc(sA + s * TC_TILE_BYTES + kk * KSTEP_BYTES);
+                        const uint64_t bd = sw128_desc(sB + s * TC_TILE_BYTES + kk * KSTEP_BYTES);
+                        const uint32_t acc = (kb | kk) ? 1u : 0u;
+                        if constexpr (MODE == FLG_LU_TF32) {
+                            asm volatile(
+                                "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                                " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(d),
+                                "l"(ad), "l"(bd), "r"(IDESC), "r"(acc)
+                                : "memory");
+                        } else {
+                            asm volatile(
+                                "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(d),
+                                "l"(ad), "l"(bd), "r"(IDESC), "r"(acc)
+                                : "memory");
+                        }
+                    }
+                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                     smem_u32(&empty[s]))
+                                 : "memory");
+                }
+                if (!ok) break;
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 smem_u32(&accf[buf]))
+                             : "memory");
+            }
+            // every MMA issued has completed before the TMEM is freed
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             smem_u32(&mma_done))
+                         : "memory");
+            mbar_drain(&mma_done, 0, err);
+        }
+    } else {
+        // epilogue: warp w reads TMEM lanes 32 (w % 4) .. +32, i.e. tile rows 32 (w % 4) + lane
+        const int q = warp & 3;
+        uint8_t *mystg = stg + (warp - 2) * 2 * TC_STG_BYTES;
+        uint32_t i = 0, nst = 0;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x, i++) {
+            const uint32_t buf = i & 1, ause = i >> 1;
+            // warp-uniform: tcgen05.ld.sync.aligned must be executed by the whole warp
+            if (!__all_sync(0xffffffffu, mbar_wait(&accf[buf], ause & 1, err))) break;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const int m0 = (t / ntx) * TC_BM, n0 = (t % ntx) * TC_BN;
+#pragma unroll 1
+            for (int ch = 0; ch < TC_BN / 32; ch++, nst++) {
+                uint32_t v[32];
+                const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + buf * TC_BN + (uint32_t)(ch * 32);
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
+                    "%13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, "
+                    "[%32];"
+                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                      "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+                      "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
+                      "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                    : "r"(taddr));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                // staging box nst % 2: the reduce that last read it (two boxes ago) must be done
+                uint8_t *box = mystg + (nst & 1) * TC_STG_BYTES;
+                if (nst >= 2 && lane == 0) asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+                __syncwarp();
+                // row `lane`, 16-byte chunk c at chunk position c ^ (row % 8) (128-byte swizzle)
+#pragma unroll
+                for (int c = 0; c < 8; c++) {
+                    const float4 w = make_float4(-__uint_as_float(v[4 * c]), -__uint_as_float(v[4 * c + 1]),
+                                                 -__uint_as_float(v[4 * c + 2]), -__uint_as_float(v[4 * c + 3]));
+                    *reinterpret_cast<float4 *>(box + lane * 128 + ((c ^ (lane & 7)) << 4)) = w;
+                }
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                __syncwarp();
+                if (lane == 0) {
+                    tma_reduce_add_2d(&tmC, box, n0 + ch * 32, m0 + q * 32);
+                    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+                }
+            }
+            // this accumulator's TMEM reads are complete: hand it back to the MMA issuer
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&acce[buf]);
+        }
+        if (lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+        __syncwarp();
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    if (warp == 0)
+    if (warp == 1)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS)
                      : "memory");
 }
 
-__global__ void f32_to_bf16_rows_kernel(const float *src, int64_t lds, __nv_bfloat16 *dst, int64_t rows) {
+__global__ void f32_to_bf16_rows_kernel(const float *src, int64_t lds, __nv_bfloat16 *dst, int64_t rows, int64_t K) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= rows * TC_K) return;
-    const int64_t r = i / TC_K, k = i % TC_K;
+    if (i >= rows * K) return;
+    const int64_t r = i / K, k = i % K;
     dst[i] = __float2bfloat16_rn(src[r * lds + k]);
 }
 
@@ -237,14 +305,14 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     return fn;
 }
 
-// 2D map over rows x 128 K-major elements, box 128 rows x 128 bytes, 128B swizzle
-static int make_map(CUtensorMap *map, const void *base, int64_t rows, int64_t ld_elems, int mode) {
+// operand map: rows x K K-major elements (row stride ld_elems), box 128 rows x 128 bytes, 128B swizzle
+static int make_operand_map(CUtensorMap *map, const void *base, int64_t rows, int64_t K, int64_t ld_elems, int mode) {
     auto fn = encode_fn();
     FLG_REQUIRE(fn != nullptr, "cuTensorMapEncodeTiled unavailable");
     const bool bf = mode == FLG_LU_BF16;
     const size_t esz = bf ? 2 : 4;
     FLG_REQUIRE(((uintptr_t)base & 15) == 0 && (ld_elems * esz) % 16 == 0, "TMA operand not 16-byte aligned");
-    cuuint64_t dims[2] = {(cuuint64_t)TC_K, (cuuint64_t)rows};
+    cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
     cuuint64_t strides[1] = {(cuuint64_t)(ld_elems * esz)};
     cuuint32_t box[2] = {(cuuint32_t)(128 / esz), (cuuint32_t)TC_BM};
     cuuint32_t estr[2] = {1, 1};
@@ -256,14 +324,42 @@ static int make_map(CUtensorMap *map, const void *base, int64_t rows, int64_t ld
     return FLG_OK;
 }
 
-static size_t tc_smem_bytes() { return 2 * TC_STAGES * TC_TILE_BYTES + 1024; }
+// C map: m x nc FP32 (row stride ldc), 32 x 32 boxes, 128B swizzle (the epilogue's staging layout)
+static int make_c_map(CUtensorMap *map, float *C, int64_t m, int64_t nc, int64_t ldc) {
+    auto fn = encode_fn();
+    FLG_REQUIRE(fn != nullptr, "cuTensorMapEncodeTiled unavailable");
+    FLG_REQUIRE(((uintptr_t)C & 15) == 0 && (ldc * 4) % 16 == 0, "C not 16-byte aligned");
+    cuuint64_t dims[2] = {(cuuint64_t)nc, (cuuint64_t)m};
+    cuuint64_t strides[1] = {(cuuint64_t)(ldc * 4)};
+    cuuint32_t box[2] = {32, 32};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, C, dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    FLG_REQUIRE(r == CUDA_SUCCESS, "cuTensorMapEncodeTiled failed for C (%d)", (int)r);
+    return FLG_OK;
+}
 
-size_t tc_update_bytes(int64_t m, int64_t nc, int mode) {
+static int sm_count_of_current_device() {
+    static std::mutex mu;
+    static int cached[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 148;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!cached[dev]) {
+        int n = 0;
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        cached[dev] = n > 0 ? n : 148;
+    }
+    return cached[dev];
+}
+
+size_t tc_update_bytes(int64_t m, int64_t nc, int64_t K, int mode) {
     CountingArena c;
     c.take<int>(1);
     if (mode == FLG_LU_BF16) {
-        c.take<__nv_bfloat16>((size_t)m * TC_K);
-        c.take<__nv_bfloat16>((size_t)nc * TC_K);
+        c.take<__nv_bfloat16>((size_t)m * K);
+        c.take<__nv_bfloat16>((size_t)nc * K);
     }
     return c.bytes();
 }
@@ -271,46 +367,49 @@ size_t tc_update_bytes(int64_t m, int64_t nc, int mode) {
 // err_dev: device flag raised on a timed-out wait.  When null, the flag lives in
 // the workspace and the call synchronizes to check it; the LU passes its own
 // flag and checks it once at the end of the factorization.
-int tc_update(float *C, int64_t ldc, const float *Lp, int64_t ldl, const float *Ut, int64_t m, int64_t nc, int mode,
-              void *work, size_t work_bytes, cudaStream_t st, int *err_dev) {
+int tc_update(float *C, int64_t ldc, const float *Lp, int64_t ldl, const float *Ut, int64_t ldu, int64_t m,
+              int64_t nc, int64_t K, int mode, void *work, size_t work_bytes, cudaStream_t st, int *err_dev) {
     FLG_REQUIRE(mode == FLG_LU_TF32 || mode == FLG_LU_BF16, "tensor-core mode must be TF32 or BF16");
     FLG_REQUIRE(m >= 0 && nc >= 0 && m < (1LL << 31) && nc < (1LL << 31), "bad tensor-core update shape");
+    FLG_REQUIRE(K > 0 && K % 128 == 0 && K <= (1 << 20), "tensor-core update depth must be a multiple of 128");
     if (m == 0 || nc == 0) return FLG_OK;
     Arena ar(work, work_bytes);
     int *own = ar.take<int>(1);
     int *err = err_dev ? err_dev : own;
     FLG_REQUIRE(err != nullptr && own != nullptr, "workspace too small for the tensor-core update");
-    CUtensorMap ma, mb;
+    CUtensorMap ma, mb, mc;
     if (mode == FLG_LU_TF32) {
-        FLG_TRY(make_map(&ma, Lp, m, ldl, mode));
-        FLG_TRY(make_map(&mb, Ut, nc, TC_K, mode));
+        FLG_TRY(make_operand_map(&ma, Lp, m, K, ldl, mode));
+        FLG_TRY(make_operand_map(&mb, Ut, nc, K, ldu, mode));
     } else {
-        __nv_bfloat16 *La = ar.take<__nv_bfloat16>((size_t)m * TC_K);
-        __nv_bfloat16 *Ub = ar.take<__nv_bfloat16>((size_t)nc * TC_K);
+        __nv_bfloat16 *La = ar.take<__nv_bfloat16>((size_t)m * K);
+        __nv_bfloat16 *Ub = ar.take<__nv_bfloat16>((size_t)nc * K);
         FLG_REQUIRE(La && Ub, "workspace too small for the BF16 operands");
-        f32_to_bf16_rows_kernel<<<(unsigned)ceil_div(m * TC_K, 256), 256, 0, st>>>(Lp, ldl, La, m);
+        f32_to_bf16_rows_kernel<<<(unsigned)ceil_div(m * K, 256), 256, 0, st>>>(Lp, ldl, La, m, K);
         FLG_LAUNCH_CHECK();
-        f32_to_bf16_rows_kernel<<<(unsigned)ceil_div(nc * TC_K, 256), 256, 0, st>>>(Ut, TC_K, Ub, nc);
+        f32_to_bf16_rows_kernel<<<(unsigned)ceil_div(nc * K, 256), 256, 0, st>>>(Ut, ldu, Ub, nc, K);
         FLG_LAUNCH_CHECK();
-        FLG_TRY(make_map(&ma, La, m, TC_K, mode));
-        FLG_TRY(make_map(&mb, Ub, nc, TC_K, mode));
+        FLG_TRY(make_operand_map(&ma, La, m, K, K, mode));
+        FLG_TRY(make_operand_map(&mb, Ub, nc, K, K, mode));
     }
+    FLG_TRY(make_c_map(&mc, C, m, nc, ldc));
     if (!err_dev) FLG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
-    const size_t smem = tc_smem_bytes();
-    dim3 grid((unsigned)ceil_div(nc, TC_BN), (unsigned)ceil_div(m, TC_BM));
-    FLG_REQUIRE(grid.y <= 65535, "too many row tiles");
+    const int64_t ntiles = ceil_div(m, TC_BM) * ceil_div(nc, TC_BN);
+    FLG_REQUIRE(ntiles < (1LL << 31), "too many tiles");
+    const unsigned grid = (unsigned)std::min<int64_t>(ntiles, sm_count_of_current_device());
     static bool attr_set = false;  // set once, so a later call can be captured in a graph
     if (!attr_set) {
         FLG_CUDA(cudaFuncSetAttribute(tc_update_kernel<FLG_LU_TF32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem));
+                                      (int)TC_SMEM));
         FLG_CUDA(cudaFuncSetAttribute(tc_update_kernel<FLG_LU_BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem));
+                                      (int)TC_SMEM));
         attr_set = true;
     }
+    const int nkb = (int)(K / (mode == FLG_LU_TF32 ? 32 : 64));
     if (mode == FLG_LU_TF32) {
-        tc_update_kernel<FLG_LU_TF32><<<grid, TC_THREADS, smem, st>>>(ma, mb, C, ldc, (int)m, (int)nc, err);
+        tc_update_kernel<FLG_LU_TF32><<<grid, TC_THREADS, TC_SMEM, st>>>(ma, mb, mc, (int)m, (int)nc, nkb, err);
     } else {
-        tc_update_kernel<FLG_LU_BF16><<<grid, TC_THREADS, smem, st>>>(ma, mb, C, ldc, (int)m, (int)nc, err);
+        tc_update_kernel<FLG_LU_BF16><<<grid, TC_THREADS, TC_SMEM, st>>>(ma, mb, mc, (int)m, (int)nc, nkb, err);
     }
     FLG_LAUNCH_CHECK();
     if (err_dev) return FLG_OK;
@@ -324,12 +423,12 @@ int tc_update(float *C, int64_t ldc, const float *Lp, int64_t ldl, const float *
 }  // namespace flg
 
 extern "C" size_t flg_tc_rank_update_workspace(int64_t m, int64_t nc, int mode) {
-    return flg::tc_update_bytes(m, nc, mode);
+    return flg::tc_update_bytes(m, nc, 128, mode);
 }
 
 extern "C" int flg_tc_rank_update(float *C, int64_t ldc, const float *A, int64_t lda, const float *Bt, int64_t ldb,
                                   int64_t m, int64_t nc, int mode, void *work, size_t work_bytes, void *stream) {
-    FLG_REQUIRE(ldb == flg::TC_K, "Bt must be compact (ldb == 128)");
-    FLG_REQUIRE(lda >= flg::TC_K && ldc >= nc, "bad leading dimensions");
-    return flg::tc_update(C, ldc, A, lda, Bt, m, nc, mode, work, work_bytes, flg::as_stream(stream), nullptr);
+    FLG_REQUIRE(ldb == 128, "Bt must be compact (ldb == 128)");
+    FLG_REQUIRE(lda >= 128 && ldc >= nc, "bad leading dimensions");
+    return flg::tc_update(C, ldc, A, lda, Bt, 128, m, nc, 128, mode, work, work_bytes, flg::as_stream(stream), nullptr);
 }

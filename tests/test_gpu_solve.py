@@ -162,6 +162,19 @@ def test_lowp_lu_factors(mode, n):
     tol = {"fp32": 1e-6, "tf32": 2e-3, "bf16": 2e-2}[mode]
     assert err < tol, err
     del X
+    # dinv: inverses of the unit-lower and upper factors of every 128 x 128 diagonal block
+    nblk = (n + 127) // 128
+    Dv = dinv.double().cpu().numpy().reshape(2, nblk, 128, 128)
+    for k in range(nblk):
+        r0, r1 = 128 * k, min(n, 128 * k + 128)
+        w = r1 - r0
+        Lk = np.eye(128)
+        Uk = np.eye(128)
+        Lk[:w, :w] = Lm[r0:r1, r0:r1]
+        Uk[:w, :w] = Um[r0:r1, r0:r1]
+        assert np.abs(Dv[0, k] @ Lk - np.eye(128)).max() < 1e-5, (k, "Linv")
+        assert np.abs(Dv[1, k] @ Uk - np.eye(128)).max() < 1e-5, (k, "Uinv")
+        assert np.abs(np.triu(Dv[0, k], 1)).max() == 0 and np.abs(np.tril(Dv[1, k], -1)).max() == 0
 
 
 @pytest.mark.parametrize("rows,cols", [(1, 1), (5, 3), (97, 250), (1536, 1536), (3000, 4099)])
