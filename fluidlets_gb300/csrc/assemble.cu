@@ -324,48 +324,93 @@ __global__ void __launch_bounds__(256) gemv_f64_kernel(int64_t nr, int64_t nc, c
     if (lane == 0) y[row] = acc;
 }
 
-// y (FP64) = A (FP32, row-major) x (FP64), FP64 accumulation; warp per row
-__global__ void __launch_bounds__(256) gemv_f32_kernel(int64_t nr, int64_t nc, const float *A, int64_t ld,
+// y (FP64) = A (FP32, row-major) x (FP64): the inner matvec of GMRES-IR.  The
+// product is formed to near-FP64 accuracy in FP32 arithmetic, so that GB300's
+// narrow FP64 pipe stays out of the loop: x = xh + xl (two FP32 parts), each
+// a xh exactly as p + pe (TwoProd by FMA), the running sum s by TwoSum with its
+// rounding errors, pe and a xl collected in a compensation c (Ogita, Rump and
+// Oishi, "Accurate sum and dot product", SIAM J. Sci. Comput. 26, 2005).  The
+// _rn intrinsics keep the compiler from contracting the error-free steps.  A
+// warp per two rows, 32 rows per block; x goes through shared memory in chunks.
+constexpr int kGvWarps = 16, kGvRpw = 2, kGvRows = kGvWarps * kGvRpw, kGvChunk = 2048;
+
+__device__ __forceinline__ void dot2_step(float &s, float &c, float a, float xh, float xl) {
+    const float p = __fmul_rn(a, xh);
+    const float pe = fmaf(a, xh, -p);
+    const float t = __fadd_rn(s, p);
+    const float z = __fsub_rn(t, s);
+    const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z));
+    s = t;
+    c = __fadd_rn(c, __fadd_rn(e, fmaf(a, xl, pe)));
+}
+
+__global__ void __launch_bounds__(512) gemv_f32_kernel(int64_t nr, int64_t nc, const float *A, int64_t ld,
                                                        const double *x, double *y) {
-    const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (row >= nr) return;
-    const float *a = A + row * ld;
-    double acc = 0.0;
-    if ((ld % 4 == 0) && (((uintptr_t)A & 15) == 0) && (((uintptr_t)x & 15) == 0)) {
-        const float4 *a4 = (const float4 *)a;
-        const double2 *x2 = (const double2 *)x;
-        const int64_t nc4 = nc / 4;
-        int64_t c = lane;
-        // four independent 16-byte loads of A in flight per lane
-        for (; c + 96 < nc4; c += 128) {
-            float4 v[4];
+    __shared__ __align__(16) float xh[kGvChunk], xl[kGvChunk];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t row0 = (int64_t)blockIdx.x * kGvRows + warp * kGvRpw;
+    const bool vec = (ld % 4 == 0) && (((uintptr_t)A & 15) == 0);
+    float s[kGvRpw][4], c[kGvRpw][4];
 #pragma unroll
-            for (int u = 0; u < 4; u++) v[u] = __ldcs(a4 + c + 32 * u);
+    for (int rr = 0; rr < kGvRpw; rr++)
 #pragma unroll
-            for (int u = 0; u < 4; u++) {
-                const int64_t cc = c + 32 * u;
-                const double2 x01 = x2[2 * cc], x23 = x2[2 * cc + 1];
-                acc = fma((double)v[u].x, x01.x, acc);
-                acc = fma((double)v[u].y, x01.y, acc);
-                acc = fma((double)v[u].z, x23.x, acc);
-                acc = fma((double)v[u].w, x23.y, acc);
+        for (int u = 0; u < 4; u++) s[rr][u] = 0.0f, c[rr][u] = 0.0f;
+    // rows past the end read row 0 (their sums are discarded)
+    const float *arow[kGvRpw];
+#pragma unroll
+    for (int rr = 0; rr < kGvRpw; rr++) arow[rr] = A + (row0 + rr < nr ? row0 + rr : 0) * ld;
+    for (int64_t c0 = 0; c0 < nc; c0 += kGvChunk) {
+        const int cw = (int)min((int64_t)kGvChunk, nc - c0);
+        __syncthreads();
+        for (int k = threadIdx.x; k < cw; k += blockDim.x) {
+            const double v = x[c0 + k];
+            const float h = __double2float_rn(v);
+            xh[k] = h;
+            xl[k] = __double2float_rn(v - (double)h);
+        }
+        __syncthreads();
+        if (row0 >= nr) continue;
+        if (vec && cw % 4 == 0) {
+            const float4 *h4 = reinterpret_cast<const float4 *>(xh);
+            const float4 *l4 = reinterpret_cast<const float4 *>(xl);
+            const int n4 = cw / 4;
+            for (int k = lane; k < n4; k += 64) {
+                const bool two = k + 32 < n4;
+                float4 v[kGvRpw][2];
+#pragma unroll
+                for (int rr = 0; rr < kGvRpw; rr++) {
+                    const float4 *a4 = reinterpret_cast<const float4 *>(arow[rr] + c0);
+                    v[rr][0] = __ldcs(a4 + k);
+                    v[rr][1] = two ? __ldcs(a4 + k + 32) : make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+#pragma unroll
+                for (int u = 0; u < 2; u++) {
+                    const int kk = two ? k + 32 * u : k;
+                    const float4 h = h4[kk], l = l4[kk];
+#pragma unroll
+                    for (int rr = 0; rr < kGvRpw; rr++) {
+                        dot2_step(s[rr][0], c[rr][0], v[rr][u].x, h.x, l.x);
+                        dot2_step(s[rr][1], c[rr][1], v[rr][u].y, h.y, l.y);
+                        dot2_step(s[rr][2], c[rr][2], v[rr][u].z, h.z, l.z);
+                        dot2_step(s[rr][3], c[rr][3], v[rr][u].w, h.w, l.w);
+                    }
+                }
+            }
+        } else {
+            for (int k = lane; k < cw; k += 32) {
+#pragma unroll
+                for (int rr = 0; rr < kGvRpw; rr++) dot2_step(s[rr][0], c[rr][0], arow[rr][c0 + k], xh[k], xl[k]);
             }
         }
-        for (; c < nc4; c += 32) {
-            const float4 v = __ldcs(a4 + c);
-            const double2 x01 = x2[2 * c], x23 = x2[2 * c + 1];
-            acc = fma((double)v.x, x01.x, acc);
-            acc = fma((double)v.y, x01.y, acc);
-            acc = fma((double)v.z, x23.x, acc);
-            acc = fma((double)v.w, x23.y, acc);
-        }
-        for (int64_t c = 4 * nc4 + lane; c < nc; c += 32) acc = fma((double)a[c], x[c], acc);
-    } else {
-        for (int64_t c = lane; c < nc; c += 32) acc = fma((double)a[c], x[c], acc);
     }
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0) y[row] = acc;
+#pragma unroll
+    for (int rr = 0; rr < kGvRpw; rr++) {
+        double acc = 0.0;
+#pragma unroll
+        for (int u = 0; u < 4; u++) acc += (double)s[rr][u] + (double)c[rr][u];
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0 && row0 + rr < nr) y[row0 + rr] = acc;
+    }
 }
 
 __global__ void convert_f64_f32_kernel(int64_t nr, int64_t nc, const double *src, int64_t lds, float *dst,
@@ -566,7 +611,7 @@ extern "C" int flg_gemv_f32(int64_t n_rows, int64_t n_cols, const float *A, int6
     if (n_rows == 0) return FLG_OK;
     cudaStream_t st = as_stream(stream);
     prof_begin(FLG_SLOT_GEMV, st);
-    gemv_f32_kernel<<<(unsigned)ceil_div(n_rows * 32, 256), 256, 0, st>>>(n_rows, n_cols, A, ld, x, y);
+    gemv_f32_kernel<<<(unsigned)ceil_div(n_rows, kGvRows), 32 * kGvWarps, 0, st>>>(n_rows, n_cols, A, ld, x, y);
     FLG_LAUNCH_CHECK();
     prof_end(FLG_SLOT_GEMV, st);
     return FLG_OK;

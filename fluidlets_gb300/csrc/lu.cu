@@ -678,97 +678,171 @@ static int copy2d(cudaStream_t st, const float *src, int64_t lds, float *dst, in
 }
 
 // ---- low precision triangular solve with the diagonal-block inverses ------------------
-// x = U^-1 L^-1 b for one right-hand side, FP32 factors, in ONE cooperative
-// launch: for each 128-row block b (forward, then backward) every CTA forms
-// x_b = Dinv_b y_b in shared memory (a 128 x 128 matvec, recomputed per CTA
-// instead of communicated), CTA 0 stores it, and the CTAs share out the rows
-// still to be updated, y[r] -= LU[r, block b] x_b (a warp per row); one bounded
-// grid barrier separates the blocks.
+// x = U^-1 L^-1 b for one right-hand side, FP32 factors, as a dataflow over the
+// 128-row blocks in ONE cooperative launch.  CTA c owns blocks c, c + G, ...
+// (G CTAs).  Forward: y_i = Linv_i (b_i - sum_{j<i} L_ij y_j); the owner of
+// block i consumes y_0, y_1, ... as their owners publish them (a release flag
+// per block, acquired with a bounded spin), accumulating L_ij y_j for all of
+// its blocks, and finalizes block i as soon as y_{i-1} has arrived.  The two
+// operands on that critical step -- L_{i,i-1} and Linv_i -- are prefetched
+// into registers before the wait.  Backward: the same in reverse with U and
+// Uinv on x_i = Uinv_i (y_i - sum_{j>i} U_ij x_j).  Every wait depends only
+// on blocks earlier in the order (forward by increasing, then backward by
+// decreasing index) and all CTAs are resident, so the order always advances.
+// 512 threads: thread t covers row t / 4 of a block, columns 32 (t % 4) + 0..31.
+constexpr int kApplyThreads = 512;
+constexpr int kApplyMaxOwn = 8;  // blocks per CTA
+
 struct ApplyArgs {
     const float *LU;
     int64_t ld, n;
     const float *Linv, *Uinv;
-    float *y;  // working right-hand side (n)
-    float *z;  // solution blocks (n)
-    GridBar *bar;
+    const float *b;  // right-hand side (FP32, n)
+    float *y, *x;    // forward / backward results (n)
+    int *fflag, *bflag;  // per-block ready flags (zeroed before the launch)
+    int *err;            // a wait ran out
 };
 
-__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
-                 : "memory");
+__device__ __forceinline__ int ld_acquire_i32(const int *p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_i32(int *p, int v) {
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// The kernel keeps its footprint small (1 KB of shared memory, 256 threads)
-// so that its cooperative launch can co-reside with other streams' kernels.
-__global__ void __launch_bounds__(256) lowp_apply_kernel(ApplyArgs a) {
-    __shared__ float yb[kNB], xb[kNB];
+// 32-wide slice of a row (`valid` leading entries exist; zeros for the rest)
+__device__ __forceinline__ void load_row32(float (&v)[32], const float *p, int valid) {
+    if (valid >= 32) {
+#pragma unroll
+        for (int c = 0; c < 32; c += 4) {
+            const float4 w = __ldg(reinterpret_cast<const float4 *>(p + c));
+            v[c] = w.x, v[c + 1] = w.y, v[c + 2] = w.z, v[c + 3] = w.w;
+        }
+    } else {
+#pragma unroll
+        for (int c = 0; c < 32; c++) v[c] = c < valid ? __ldg(p + c) : 0.0f;
+    }
+}
+__device__ __forceinline__ float dot32(const float (&v)[32], const float *s) {
+    float a0 = 0.f, a1 = 0.f;
+#pragma unroll
+    for (int c = 0; c < 32; c += 2) {
+        a0 = fmaf(v[c], s[c], a0);
+        a1 = fmaf(v[c + 1], s[c + 1], a1);
+    }
+    return a0 + a1;
+}
+// sum over the four threads of a row (consecutive lanes)
+__device__ __forceinline__ float row_sum4(float v) {
+    v += __shfl_xor_sync(0xffffffffu, v, 1);
+    v += __shfl_xor_sync(0xffffffffu, v, 2);
+    return v;
+}
+
+// thread 0 waits for *flag; false (for the whole CTA) if a wait ran out here or elsewhere
+__device__ bool wait_block(const int *flag, int *err, int *abort_s) {
+    if (threadIdx.x == 0) {
+        const long long t0 = clock64();
+        while (ld_acquire_i32(flag) == 0) {
+            if (*(volatile int *)err || clock64() - t0 > kSpinLimit) {
+                atomicExch(err, 1);
+                *abort_s = 1;
+                break;
+            }
+        }
+    }
+    __syncthreads();
+    return *(volatile int *)abort_s == 0;
+}
+
+__global__ void __launch_bounds__(kApplyThreads) lowp_apply_kernel(ApplyArgs a) {
+    __shared__ __align__(16) float vec[kNB];   // the block being consumed
+    __shared__ __align__(16) float tvec[kNB];  // t_i of the block being finalized
+    __shared__ float acc[kApplyMaxOwn][kApplyThreads];
+    __shared__ int abort_s;
+    const int t = threadIdx.x, r = t >> 2, q = t & 3;
+    const int G = gridDim.x, c = blockIdx.x;
     const int nblk = (int)ceil_div(a.n, kNB);
-    const int nwarp_tot = gridDim.x * (blockDim.x >> 5);
-    const int gwarp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-    const int warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-    const int total = 2 * nblk;
-    for (int t = 0; t < total; t++) {
-        const bool fwd = t < nblk;
-        const int k = fwd ? t : 2 * nblk - 1 - t;
-        const int64_t b0 = (int64_t)k * kNB;
-        const int bs = (int)min((int64_t)kNB, a.n - b0);
-        const float *src = fwd ? a.y : a.z;  // backward pass reads the forward result
-        for (int q = threadIdx.x; q < bs; q += blockDim.x) yb[q] = ((volatile float *)src)[b0 + q];
+    const int nown = c < nblk ? (nblk - 1 - c) / G + 1 : 0;
+    if (t == 0) abort_s = 0;
+    // the valid part of a 32-column slice starting at column col0
+    auto valid_cols = [&](int64_t col0) { return (int)max((int64_t)0, min((int64_t)32, a.n - col0)); };
+    for (int pass = 0; pass < 2 && nown > 0; pass++) {
+        const bool fwd = pass == 0;
+        const float *D = fwd ? a.Linv : a.Uinv;
+        const float *src = fwd ? a.y : a.x;  // the published blocks consumed by this pass
+        int *flag = fwd ? a.fflag : a.bflag;
+        for (int m = 0; m < nown; m++) acc[m][t] = 0.0f;
         __syncthreads();
-        // x_b = Dinv_b y_b: each warp takes 16 rows, all row loads issued before the reductions
-        const float *Dk = (fwd ? a.Linv : a.Uinv) + (int64_t)k * kNB * kNB;
-        for (int rb = warp * 16; rb < bs; rb += nwarp * 16) {
-            float v[16][4];
-#pragma unroll
-            for (int i = 0; i < 16; i++)
-#pragma unroll
-                for (int c = 0; c < 4; c++) v[i][c] = Dk[(rb + i) * kNB + lane + 32 * c];
-#pragma unroll
-            for (int i = 0; i < 16; i++) {
-                float acc = 0.0f;
-#pragma unroll
-                for (int c = 0; c < 4; c++) {
-                    const int q = lane + 32 * c;
-                    acc = fmaf(v[i][c], q < bs ? yb[q] : 0.0f, acc);
-                }
-                for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-                if (lane == 0 && rb + i < bs) xb[rb + i] = acc;
+        // processing position mi -> owned slot m (ascending blocks forward, descending backward)
+        auto slot = [&](int mi) { return fwd ? mi : nown - 1 - mi; };
+        int mi = 0, i = 0, jc = 0;
+        float P[32], Dr[32];
+        int64_t row = 0;
+        bool rok = false;
+        // make owned block (position mi) the target and prefetch its critical operands
+        auto target = [&]() {
+            i = c + slot(mi) * G;
+            jc = fwd ? i - 1 : i + 1;
+            row = (int64_t)i * kNB + r;
+            rok = row < a.n;
+            const bool has = fwd ? i > 0 : i < nblk - 1;
+            const int64_t col0 = (int64_t)jc * kNB + 32 * q;
+            if (has && rok) load_row32(P, a.LU + row * a.ld + col0, valid_cols(col0));
+            else load_row32(P, a.LU, 0);
+            load_row32(Dr, D + (int64_t)i * kNB * kNB + r * kNB + 32 * q, 32);
+        };
+        // block i: t_i = rhs_i - sum_j (...) , out_i = D_i t_i, then publish
+        auto finalize = [&]() {
+            const float tot = row_sum4(acc[slot(mi)][t]);
+            float rhs = 0.0f;
+            if (rok) rhs = fwd ? __ldg(a.b + row) : __ldcg(a.y + row);
+            if (q == 0) tvec[r] = rok ? rhs - tot : 0.0f;
+            __syncthreads();
+            const float out = row_sum4(dot32(Dr, tvec + 32 * q));
+            if (q == 0 && rok) (fwd ? a.y : a.x)[row] = out;
+            __threadfence();  // each writer orders its own store before the release below
+            __syncthreads();
+            if (t == 0) st_release_i32(flag + i, 1);
+        };
+        target();
+        if (fwd ? i == 0 : i == nblk - 1) {  // nothing to consume first
+            finalize();
+            if (++mi < nown) target();
+        }
+        for (int j = fwd ? 0 : nblk - 1; mi < nown; j += fwd ? 1 : -1) {
+            if (!wait_block(flag + j, a.err, &abort_s)) return;
+            if (t < kNB) {
+                const int64_t e = (int64_t)j * kNB + t;
+                vec[t] = e < a.n ? __ldcg(src + e) : 0.0f;
             }
+            __syncthreads();
+            const int64_t col0 = (int64_t)j * kNB + 32 * q;
+            const int vc = valid_cols(col0);
+            float v[32];
+            // the target's contribution first: on the critical path when j == jc
+            if (j == jc) {
+                acc[slot(mi)][t] += dot32(P, vec + 32 * q);
+            } else {
+                if (rok) load_row32(v, a.LU + row * a.ld + col0, vc);
+                else load_row32(v, a.LU, 0);
+                acc[slot(mi)][t] += dot32(v, vec + 32 * q);
+            }
+            const bool fin = j == jc;
+            if (fin) finalize();
+            // the owned blocks after the target consume block j as well
+            for (int mm = mi + 1; mm < nown; mm++) {
+                const int64_t row2 = (int64_t)(c + slot(mm) * G) * kNB + r;
+                if (row2 < a.n) load_row32(v, a.LU + row2 * a.ld + col0, vc);
+                else load_row32(v, a.LU, 0);
+                acc[slot(mm)][t] += dot32(v, vec + 32 * q);
+            }
+            __syncthreads();  // vec is rewritten by the next consumed block
+            if (fin && ++mi < nown) target();
         }
         __syncthreads();
-        if (blockIdx.x == 0)
-            for (int q = threadIdx.x; q < bs; q += blockDim.x) (fwd ? a.z : a.y)[b0 + q] = xb[q];
-        // rows still to update: below (forward) / above (backward); a row may be
-        // updated by different CTAs in different steps, so bypass L1
-        const int64_t r0 = fwd ? b0 + bs : 0, r1 = fwd ? a.n : b0;
-        volatile float *tgt = fwd ? a.y : a.z;
-        // four rows per warp at a time, all loads issued before the reductions
-        for (int64_t rb = r0 + 4 * (int64_t)gwarp; rb < r1; rb += 4 * (int64_t)nwarp_tot) {
-            float v[4][4];
-#pragma unroll
-            for (int i = 0; i < 4; i++) {
-                const int64_t r = rb + i;
-                const float *row = a.LU + (r < r1 ? r : rb) * a.ld + b0;
-#pragma unroll
-                for (int c = 0; c < 4; c++) {
-                    const int q = lane + 32 * c;
-                    v[i][c] = (q < bs) ? row[q] : 0.0f;
-                }
-            }
-#pragma unroll
-            for (int i = 0; i < 4; i++) {
-                float acc = 0.0f;
-#pragma unroll
-                for (int c = 0; c < 4; c++) {
-                    const int q = lane + 32 * c;
-                    acc = fmaf(v[i][c], q < bs ? xb[q] : 0.0f, acc);
-                }
-                for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-                // fire-and-forget reduction (RED): one update per row and step, steps ordered by the barrier
-                if (lane == 0 && rb + i < r1) atomicAdd((float *)&tgt[rb + i], -acc);
-            }
-        }
-        if (!grid_sync(a.bar, gridDim.x)) return;
     }
 }
 
@@ -776,39 +850,45 @@ __global__ void d2f_kernel(const double *a, float *b, int64_t n) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) b[i] = (float)a[i];
 }
-__global__ void f2d_kernel(const float *a, double *b, int64_t n) {
+// FP32 solution back to FP64; NaN everywhere if a wait of the apply ran out
+__global__ void f2d_kernel(const float *a, double *b, int64_t n, const int *err) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) b[i] = (double)a[i];
+    if (i < n) b[i] = *err ? __longlong_as_double(0x7ff8000000000000LL) : (double)a[i];
 }
 
 size_t lu_solve_lowp_bytes(int64_t n) {
     CountingArena c;
+    const int64_t nblk = ceil_div(std::max<int64_t>(n, 1), kNB);
     c.take<float>(n);
     c.take<float>(n);
-    c.take<GridBar>(1);
+    c.take<float>(n);
+    c.take<int>(2 * nblk + 1);
     return c.bytes();
 }
 
 int lu_solve_lowp_apply(int64_t n, const float *LU, int64_t ld, const float *dinv, const double *b, double *x,
                         void *work, size_t work_bytes, cudaStream_t st) {
+    FLG_REQUIRE(ld % 4 == 0 && ((uintptr_t)LU & 15) == 0, "LU rows must be 16-byte aligned (ld % 4 == 0)");
     Arena ar(work, work_bytes);
+    const int64_t nblk = ceil_div(n, kNB);
+    float *bf = ar.take<float>(n);
     float *y = ar.take<float>(n);
     float *z = ar.take<float>(n);
-    GridBar *bar = ar.take<GridBar>(1);
-    FLG_REQUIRE(y && z && bar, "workspace too small for the low-precision solve");
-    d2f_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(b, y, n);
+    int *flags = ar.take<int>(2 * nblk + 1);
+    FLG_REQUIRE(bf && y && z && flags, "workspace too small for the low-precision solve");
+    const int G = (int)std::min<int64_t>(nblk, sm_count());
+    FLG_REQUIRE(nblk <= (int64_t)kApplyMaxOwn * G, "system too large for the low-precision solve (%lld blocks)",
+                (long long)nblk);
+    d2f_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(b, bf, n);
     FLG_LAUNCH_CHECK();
-    FLG_CUDA(cudaMemsetAsync(bar, 0, sizeof(GridBar), st));
-    const int64_t nblk = ceil_div(n, kNB);
-    ApplyArgs aa{LU, ld, n, dinv, dinv + nblk * kNB * kNB, y, z, bar};
-    const int grid = sm_count();
+    FLG_CUDA(cudaMemsetAsync(flags, 0, sizeof(int) * (2 * nblk + 1), st));
+    ApplyArgs aa{LU, ld, n, dinv, dinv + nblk * kNB * kNB, bf, y, z, flags, flags + nblk, flags + 2 * nblk};
     void *args[] = {&aa};
     prof_begin(FLG_SLOT_LU_SOLVE, st);
-    FLG_CUDA(cudaLaunchCooperativeKernel((void *)lowp_apply_kernel, dim3(grid), dim3(256), args, 0, st));
+    FLG_CUDA(cudaLaunchCooperativeKernel((void *)lowp_apply_kernel, dim3(G), dim3(kApplyThreads), args, 0, st));
     count_launch();
     prof_end(FLG_SLOT_LU_SOLVE, st);
-    // after the backward pass the solution is in y
-    f2d_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(y, x, n);
+    f2d_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(z, x, n, flags + 2 * nblk);
     FLG_LAUNCH_CHECK();
     return FLG_OK;
 }

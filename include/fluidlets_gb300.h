@@ -271,7 +271,10 @@ int flg_graph_destroy(void *graph_exec);
  * y = A x (FP64, row-major n_rows x n_cols, ld); used for residuals. */
 int flg_gemv_f64(int64_t n_rows, int64_t n_cols, const double *A, int64_t ld, const double *x, double *y,
                  void *stream);
-/* y (FP64) = A (FP32, row-major n_rows x n_cols, ld) x (FP64), FP64 accumulation. */
+/* y (FP64) = A (FP32, row-major n_rows x n_cols, ld) x (FP64), computed with
+ * compensated FP32 arithmetic (x split into two FP32 parts, error-free products
+ * and sums) to about FP64 accuracy for the given FP32 entries: the inner matvec
+ * of GMRES-IR.  No counterpart in the reference. */
 int flg_gemv_f32(int64_t n_rows, int64_t n_cols, const float *A, int64_t ld, const double *x, double *y,
                  void *stream);
 /* dst (FP32, ldd) = (float) src (FP64, lds), n_rows x n_cols */

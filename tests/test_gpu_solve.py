@@ -177,6 +177,30 @@ def test_lowp_lu_factors(mode, n):
         assert np.abs(np.triu(Dv[0, k], 1)).max() == 0 and np.abs(np.tril(Dv[1, k], -1)).max() == 0
 
 
+@pytest.mark.parametrize("n", [100, 128, 300, 5000, 19500])
+def test_lowp_apply_matches_triangular_solves(n):
+    """flg_lu_solve_lowp: x = U^-1 L^-1 b with the FP32 factors; 19,500 unknowns give more
+    128-row blocks than SMs (one CTA owns two) and a partial last block."""
+    from fluidlets_gb300.core import _lowp_factor_dev
+    L = _lib.load()
+    g = torch.Generator(device="cuda").manual_seed(n)
+    K = torch.randn(n, n, device="cuda", dtype=torch.float64, generator=g) / n ** 0.5
+    K.diagonal().add_(4.0)
+    K32, ld32, dinv, A32 = _lowp_factor_dev(K, "fp32")
+    del A32, K
+    b = torch.randn(n, device="cuda", dtype=torch.float64, generator=g)
+    x = torch.empty_like(b)
+    nb = L.flg_lu_solve_lowp_workspace(n)
+    ws = dv.workspace(nb)
+    _lib.check(L.flg_lu_solve_lowp(n, dv.ptr(K32), ld32, dv.ptr(dinv), dv.ptr(b), dv.ptr(x), dv.ptr(ws), nb,
+                                   dv.stream()))
+    LU = K32[:, :n].double()
+    y = torch.linalg.solve_triangular(LU, b[:, None], upper=False, unitriangular=True)
+    ref = torch.linalg.solve_triangular(LU, y, upper=True)[:, 0]
+    err = float(torch.linalg.vector_norm(x - ref) / torch.linalg.vector_norm(ref))
+    assert err < 1e-5, err
+
+
 @pytest.mark.parametrize("rows,cols", [(1, 1), (5, 3), (97, 250), (1536, 1536), (3000, 4099)])
 def test_gemv_f64_and_f32(rows, cols):
     L = _lib.load()
@@ -194,8 +218,9 @@ def test_gemv_f64_and_f32(rows, cols):
     scale = np.abs(A) @ np.abs(x)
     assert np.all(np.abs(y.cpu().numpy() - ref) <= 1e-13 * scale + 1e-300)
     _lib.check(L.flg_gemv_f32(rows, cols, dv.ptr(A32), ld, dv.ptr(xd), dv.ptr(y), dv.stream()))
-    ref32 = A32[:, :cols].double().cpu().numpy() @ x  # FP32 matrix entries, FP64 products and sums
-    assert np.all(np.abs(y.cpu().numpy() - ref32) <= 1e-13 * scale + 1e-300)
+    # the FP32 entries times the FP64 x, to about FP64 accuracy (compensated FP32 arithmetic)
+    ref32 = A32[:, :cols].double().cpu().numpy() @ x
+    assert np.all(np.abs(y.cpu().numpy() - ref32) <= 1e-12 * scale + 1e-300)
 
 
 # ---- resistance ------------------------------------------------------------------------
