@@ -69,7 +69,7 @@ SIGNATURES = {
     "flg_profile_read": (c_int, [c_int, POINTER(c_double), POINTER(c_int64)]),
     "flg_launch_count": (c_int64, []),
 }
-SLOT = {"far_f32": 0, "near_f64": 1, "sum_f64": 2, "assemble": 3, "lu_update": 4, "lu_panel": 5, "gemv": 6, "lu_solve": 7}
+SLOT = {"far_f32": 0, "near_f64": 1, "sum_f64": 2, "assemble": 3, "lu_update": 4, "lu_panel": 5, "gemv": 6, "lu_solve": 7, "lu_diag": 8}
 
 _lib = None
 

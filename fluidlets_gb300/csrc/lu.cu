@@ -400,69 +400,70 @@ __device__ __forceinline__ void warp_mm(const float *A, const float *B, float *C
     __syncwarp();
 }
 
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 // One warp factors the 32 x 32 block P in place without pivoting and writes
-// inv(L) to Xb, inv(U) to Yb (lane = row).  A zero or non-finite pivot of a real
-// (not padding) row records its 1-based global index in *info.
+// inv(L) to Xb, inv(U) to Yb; lane = column, the column in registers.  Step j:
+// lane j forms the multipliers l_i = a_ij / a_jj (i > j) and broadcasts them;
+// columns c > j subtract l_i a_jc, and the same eliminations applied to the
+// identity build inv(L) (Gauss-Jordan).  inv(U) by column-oriented back
+// substitution, lane c solving U y = e_c.  A zero or non-finite pivot of a
+// real (not padding) row records its 1-based global index in *info.  The
+// reciprocal is the hardware approximation (1 ulp): this factorization only
+// preconditions FP64 iterative refinement.
 __device__ __forceinline__ void warp_lu32(float *P, float *Xb, float *Yb, int lane, int row0, int nb, int64_t k0,
                                           int *info) {
     constexpr unsigned kAll = 0xffffffffu;
-    float d[kSB], x[kSB];
+    float a[kSB], x[kSB];
 #pragma unroll
-    for (int c = 0; c < kSB; c += 4) {
-        const float4 v = *reinterpret_cast<const float4 *>(P + lane * kLD + c);
-        d[c] = v.x, d[c + 1] = v.y, d[c + 2] = v.z, d[c + 3] = v.w;
+    for (int i = 0; i < kSB; i++) {
+        a[i] = P[i * kLD + lane];
+        x[i] = (i == lane) ? 1.0f : 0.0f;
     }
-#pragma unroll
-    for (int c = 0; c < kSB; c++) x[c] = (c == lane) ? 1.0f : 0.0f;
 #pragma unroll
     for (int j = 0; j < kSB; j++) {
-        const float piv = __shfl_sync(kAll, d[j], j);
-        const bool ok = piv != 0.0f && isfinite(piv);
-        if (!ok && lane == 0 && row0 + j < nb) atomicCAS(info, 0, (int)(k0 + row0 + j + 1));
-        const float rp = ok ? 1.0f / piv : 0.0f;
-        const bool below = lane > j;
-        const float l = d[j] * rp;
-#pragma unroll
-        for (int c = 0; c < kSB; c++) {
-            if (c == j) continue;
-            // pivot row j: U part right of the diagonal, inv(L) part left of it
-            const float v = __shfl_sync(kAll, c > j ? d[c] : x[c], j);
-            if (below) {
-                if (c > j) d[c] = fmaf(-l, v, d[c]);
-                else x[c] = fmaf(-l, v, x[c]);
-            }
+        float rp = 0.0f;
+        if (lane == j) {
+            const float piv = a[j];
+            const bool ok = piv != 0.0f && isfinite(piv);
+            if (!ok && row0 + j < nb) atomicCAS(info, 0, (int)(k0 + row0 + j + 1));
+            rp = ok ? rcp_approx(piv) : 0.0f;
         }
-        if (below) {
-            x[j] -= l;
-            d[j] = l;
+        const float ujc = a[j];  // row j of U in column `lane` (for lane > j)
+        const float xjc = x[j];
+#pragma unroll
+        for (int i = 0; i < kSB; i++) {
+            if (i <= j) continue;
+            const float l = __shfl_sync(kAll, a[i] * rp, j);
+            if (lane == j) a[i] = l;
+            else if (lane > j) a[i] = fmaf(-l, ujc, a[i]);
+            x[i] = fmaf(-l, xjc, x[i]);
         }
     }
-#pragma unroll
-    for (int c = 0; c < kSB; c += 4) {
-        *reinterpret_cast<float4 *>(P + lane * kLD + c) = make_float4(d[c], d[c + 1], d[c + 2], d[c + 3]);
-        *reinterpret_cast<float4 *>(Xb + lane * kLD + c) = make_float4(x[c], x[c + 1], x[c + 2], x[c + 3]);
-    }
-    // inv(U): backward Gauss-Jordan on [U | I]; row j is scaled by 1/U[j][j], then
-    // rows above subtract U[i][j] times it (column j of U above the diagonal is
-    // untouched by the later pivots, so d[j] still holds U[i][j]).
     float y[kSB];
 #pragma unroll
-    for (int c = 0; c < kSB; c++) y[c] = (c == lane) ? 1.0f : 0.0f;
+    for (int i = 0; i < kSB; i++) {
+        P[i * kLD + lane] = a[i];
+        Xb[i * kLD + lane] = x[i];
+        y[i] = (i == lane) ? 1.0f : 0.0f;
+    }
 #pragma unroll
-    for (int j = kSB - 1; j >= 0; j--) {
-        const float piv = __shfl_sync(kAll, d[j], j);
-        const float rp = (piv != 0.0f && isfinite(piv)) ? 1.0f / piv : 0.0f;
-        const float u = d[j];
+    for (int i = kSB - 1; i >= 0; i--) {
+        const float piv = __shfl_sync(kAll, a[i], i);  // U[i][i]
+        const float rp = (piv != 0.0f && isfinite(piv)) ? rcp_approx(piv) : 0.0f;
+        y[i] *= rp;
 #pragma unroll
-        for (int c = j; c < kSB; c++) {
-            const float v = __shfl_sync(kAll, y[c], j) * rp;
-            if (lane == j) y[c] = v;
-            else if (lane < j) y[c] = fmaf(-u, v, y[c]);
+        for (int k = 0; k < kSB; k++) {
+            if (k >= i) continue;
+            y[k] = fmaf(-__shfl_sync(kAll, a[k], i), y[i], y[k]);  // U[k][i]
         }
     }
 #pragma unroll
-    for (int c = 0; c < kSB; c += 4)
-        *reinterpret_cast<float4 *>(Yb + lane * kLD + c) = make_float4(y[c], y[c + 1], y[c + 2], y[c + 3]);
+    for (int i = 0; i < kSB; i++) Yb[i * kLD + lane] = y[i];
 }
 
 __global__ void __launch_bounds__(512) diag_lowp_kernel(float *A, int64_t ld, int64_t k0, int nb, float *Linv,
@@ -470,11 +471,33 @@ __global__ void __launch_bounds__(512) diag_lowp_kernel(float *A, int64_t ld, in
     extern __shared__ __align__(16) float sm[];
     float *D = sm, *X = sm + kNB * kLD, *Y = sm + 2 * kNB * kLD;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, nthr = blockDim.x, nwarp = nthr >> 5;
-    for (int e = tid; e < kNB * kNB; e += nthr) {
-        const int r = e / kNB, c = e - r * kNB;
-        D[r * kLD + c] = (r < nb && c < nb) ? A[(k0 + r) * ld + k0 + c] : (r == c ? 1.0f : 0.0f);
-        X[r * kLD + c] = 0.0f;
-        Y[r * kLD + c] = 0.0f;
+    // 16-byte rows when the block is whole and aligned (ld % 4 == 0 is required by the caller)
+    const bool v4 = nb == kNB && (((uintptr_t)(A + k0 * ld + k0)) & 15) == 0;
+    {
+        const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        float4 buf[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) {  // 4096 float4 = 128 x 128, eight per thread
+            const int e = tid + u * 512, r = e >> 5, c4 = (e & 31) * 4;
+            if (v4) {
+                buf[u] = __ldg(reinterpret_cast<const float4 *>(A + (k0 + r) * ld + k0 + c4));
+            } else {
+                float w[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int c = c4 + q;
+                    w[q] = (r < nb && c < nb) ? A[(k0 + r) * ld + k0 + c] : (r == c ? 1.0f : 0.0f);
+                }
+                buf[u] = make_float4(w[0], w[1], w[2], w[3]);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            const int e = tid + u * 512, r = e >> 5, c4 = (e & 31) * 4;
+            *reinterpret_cast<float4 *>(D + r * kLD + c4) = buf[u];
+            *reinterpret_cast<float4 *>(X + r * kLD + c4) = z4;
+            *reinterpret_cast<float4 *>(Y + r * kLD + c4) = z4;
+        }
     }
     __syncthreads();
     for (int s = 0; s < kNS; s++) {
@@ -519,11 +542,20 @@ __global__ void __launch_bounds__(512) diag_lowp_kernel(float *A, int64_t ld, in
         }
         __syncthreads();
     }
-    for (int e = tid; e < kNB * kNB; e += nthr) {
-        const int r = e / kNB, c = e - r * kNB;
-        if (r < nb && c < nb) A[(k0 + r) * ld + k0 + c] = D[r * kLD + c];
-        Linv[r * kNB + c] = X[r * kLD + c];
-        Uinv[r * kNB + c] = Y[r * kLD + c];
+#pragma unroll 2
+    for (int u = 0; u < 8; u++) {
+        const int e = tid + u * 512, r = e >> 5, c4 = (e & 31) * 4;
+        const float4 d = *reinterpret_cast<const float4 *>(D + r * kLD + c4);
+        if (v4) {
+            *reinterpret_cast<float4 *>(A + (k0 + r) * ld + k0 + c4) = d;
+        } else if (r < nb) {
+            const float w[4] = {d.x, d.y, d.z, d.w};
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                if (c4 + q < nb) A[(k0 + r) * ld + k0 + c4 + q] = w[q];
+        }
+        *reinterpret_cast<float4 *>(Linv + r * kNB + c4) = *reinterpret_cast<const float4 *>(X + r * kLD + c4);
+        *reinterpret_cast<float4 *>(Uinv + r * kNB + c4) = *reinterpret_cast<const float4 *>(Y + r * kLD + c4);
     }
 }
 
@@ -1082,14 +1114,13 @@ extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mod
         for (int64_t k0 = K0; k0 < E; k0 += kNB) {
             const int64_t k = k0 / kNB;
             const int nb = (int)std::min<int64_t>(kNB, n - k0);
-            prof_begin(FLG_SLOT_LU_PANEL, st);
+            prof_begin(FLG_SLOT_LU_DIAG, st);
             diag_lowp_kernel<<<1, 512, dsmem, st>>>(A, ld, k0, nb, Linv + k * kNB * kNB, Uinv + k * kNB * kNB, dinfo);
             FLG_LAUNCH_CHECK();
+            prof_end(FLG_SLOT_LU_DIAG, st);
             const int64_t c0 = k0 + nb, nr = n - c0;
-            if (nr <= 0) {
-                prof_end(FLG_SLOT_LU_PANEL, st);
-                continue;
-            }
+            if (nr <= 0) continue;
+            prof_begin(FLG_SLOT_LU_PANEL, st);
             // (nb < kNB only for the last block, which has no trailing part)
             float *A12 = A + k0 * ld + c0, *A21 = A + c0 * ld + k0, *A22 = A + c0 * ld + c0;
             float *Ut = UtB + (c0 - K0) * kOuterW + (k0 - K0);  // row: column - K0; K offset: k0 - K0

@@ -298,10 +298,11 @@ int flg_measure_peaks(double *fp32_tflops, double *fp64_tflops, void *stream);
 #define FLG_SLOT_SUM_F64 2      /* sum_f64_kernel (plain FP64 sum)              */
 #define FLG_SLOT_ASSEMBLE 3     /* dense assembly kernels                       */
 #define FLG_SLOT_LU_UPDATE 4    /* LU trailing updates (tensor-core GEMM)       */
-#define FLG_SLOT_LU_PANEL 5     /* LU panel / diagonal-block kernels            */
+#define FLG_SLOT_LU_PANEL 5     /* LU panel kernels (FP64 panel; low-precision L21 / U12) */
 #define FLG_SLOT_GEMV 6         /* FP64 GEMV (residuals)                        */
 #define FLG_SLOT_LU_SOLVE 7     /* low-precision triangular solves (preconditioner) */
-#define FLG_NUM_SLOTS 8
+#define FLG_SLOT_LU_DIAG 8      /* low-precision LU diagonal-block factor + inverses */
+#define FLG_NUM_SLOTS 9
 int flg_profile_enable(int enable);
 int flg_profile_read(int slot, double *total_ms, int64_t *launches);
 int64_t flg_launch_count(void);
