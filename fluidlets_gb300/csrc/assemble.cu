@@ -344,8 +344,13 @@ __device__ __forceinline__ void dot2_step(float &s, float &c, float a, float xh,
     c = __fadd_rn(c, __fadd_rn(e, fmaf(a, xl, pe)));
 }
 
+// SPLIT: x arrives already split into FP32 parts xh_g, xl_g (global); otherwise each
+// block splits its chunk of the FP64 x.  The loads of the next iteration are issued
+// before the Dot2 chains of the current one.
+template <bool SPLIT>
 __global__ void __launch_bounds__(512) gemv_f32_kernel(int64_t nr, int64_t nc, const float *A, int64_t ld,
-                                                       const double *x, double *y) {
+                                                       const double *x, const float *xh_g, const float *xl_g,
+                                                       double *y) {
     __shared__ __align__(16) float xh[kGvChunk], xl[kGvChunk];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t row0 = (int64_t)blockIdx.x * kGvRows + warp * kGvRpw;
@@ -362,11 +367,18 @@ __global__ void __launch_bounds__(512) gemv_f32_kernel(int64_t nr, int64_t nc, c
     for (int64_t c0 = 0; c0 < nc; c0 += kGvChunk) {
         const int cw = (int)min((int64_t)kGvChunk, nc - c0);
         __syncthreads();
-        for (int k = threadIdx.x; k < cw; k += blockDim.x) {
-            const double v = x[c0 + k];
-            const float h = __double2float_rn(v);
-            xh[k] = h;
-            xl[k] = __double2float_rn(v - (double)h);
+        if (SPLIT) {
+            for (int k = threadIdx.x; k < cw; k += blockDim.x) {
+                xh[k] = xh_g[c0 + k];
+                xl[k] = xl_g[c0 + k];
+            }
+        } else {
+            for (int k = threadIdx.x; k < cw; k += blockDim.x) {
+                const double v = x[c0 + k];
+                const float h = __double2float_rn(v);
+                xh[k] = h;
+                xl[k] = __double2float_rn(v - (double)h);
+            }
         }
         __syncthreads();
         if (row0 >= nr) continue;
@@ -374,26 +386,25 @@ __global__ void __launch_bounds__(512) gemv_f32_kernel(int64_t nr, int64_t nc, c
             const float4 *h4 = reinterpret_cast<const float4 *>(xh);
             const float4 *l4 = reinterpret_cast<const float4 *>(xl);
             const int n4 = cw / 4;
-            for (int k = lane; k < n4; k += 64) {
-                const bool two = k + 32 < n4;
-                float4 v[kGvRpw][2];
+            const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+            float4 v[kGvRpw], nv[kGvRpw];
+            int k = lane;
+#pragma unroll
+            for (int rr = 0; rr < kGvRpw; rr++)
+                v[rr] = k < n4 ? __ldcs(reinterpret_cast<const float4 *>(arow[rr] + c0) + k) : z4;
+            for (; k < n4; k += 32) {
+                const int kn = k + 32;
+#pragma unroll
+                for (int rr = 0; rr < kGvRpw; rr++)
+                    nv[rr] = kn < n4 ? __ldcs(reinterpret_cast<const float4 *>(arow[rr] + c0) + kn) : z4;
+                const float4 h = h4[k], l = l4[k];
 #pragma unroll
                 for (int rr = 0; rr < kGvRpw; rr++) {
-                    const float4 *a4 = reinterpret_cast<const float4 *>(arow[rr] + c0);
-                    v[rr][0] = __ldcs(a4 + k);
-                    v[rr][1] = two ? __ldcs(a4 + k + 32) : make_float4(0.f, 0.f, 0.f, 0.f);
-                }
-#pragma unroll
-                for (int u = 0; u < 2; u++) {
-                    const int kk = two ? k + 32 * u : k;
-                    const float4 h = h4[kk], l = l4[kk];
-#pragma unroll
-                    for (int rr = 0; rr < kGvRpw; rr++) {
-                        dot2_step(s[rr][0], c[rr][0], v[rr][u].x, h.x, l.x);
-                        dot2_step(s[rr][1], c[rr][1], v[rr][u].y, h.y, l.y);
-                        dot2_step(s[rr][2], c[rr][2], v[rr][u].z, h.z, l.z);
-                        dot2_step(s[rr][3], c[rr][3], v[rr][u].w, h.w, l.w);
-                    }
+                    dot2_step(s[rr][0], c[rr][0], v[rr].x, h.x, l.x);
+                    dot2_step(s[rr][1], c[rr][1], v[rr].y, h.y, l.y);
+                    dot2_step(s[rr][2], c[rr][2], v[rr].z, h.z, l.z);
+                    dot2_step(s[rr][3], c[rr][3], v[rr].w, h.w, l.w);
+                    v[rr] = nv[rr];
                 }
             }
         } else {
@@ -411,6 +422,16 @@ __global__ void __launch_bounds__(512) gemv_f32_kernel(int64_t nr, int64_t nc, c
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
         if (lane == 0 && row0 + rr < nr) y[row0 + rr] = acc;
     }
+}
+
+// x (FP64) -> xh + xl (FP32 parts, exactly xh + xl = x up to 2^-48 relative)
+__global__ void split_f64_kernel(const double *x, float *xh, float *xl, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double v = x[i];
+    const float h = __double2float_rn(v);
+    xh[i] = h;
+    xl[i] = __double2float_rn(v - (double)h);
 }
 
 __global__ void convert_f64_f32_kernel(int64_t nr, int64_t nc, const double *src, int64_t lds, float *dst,
@@ -611,11 +632,32 @@ extern "C" int flg_gemv_f32(int64_t n_rows, int64_t n_cols, const float *A, int6
     if (n_rows == 0) return FLG_OK;
     cudaStream_t st = as_stream(stream);
     prof_begin(FLG_SLOT_GEMV, st);
-    gemv_f32_kernel<<<(unsigned)ceil_div(n_rows, kGvRows), 32 * kGvWarps, 0, st>>>(n_rows, n_cols, A, ld, x, y);
+    gemv_f32_kernel<false><<<(unsigned)ceil_div(n_rows, kGvRows), 32 * kGvWarps, 0, st>>>(n_rows, n_cols, A, ld, x,
+                                                                                         nullptr, nullptr, y);
     FLG_LAUNCH_CHECK();
     prof_end(FLG_SLOT_GEMV, st);
     return FLG_OK;
 }
+
+namespace flg {
+// the same product with x split once into xsplit[0, n_cols) (high parts) and
+// xsplit[n_cols, 2 n_cols) (low parts), a caller workspace (GMRES-IR)
+int gemv_f32_presplit(int64_t n_rows, int64_t n_cols, const float *A, int64_t ld, const double *x, float *xsplit,
+                      double *y, cudaStream_t st) {
+    FLG_REQUIRE(n_rows >= 0 && n_cols >= 0 && ld >= n_cols, "bad GEMV shape");
+    if (n_rows == 0) return FLG_OK;
+    if (n_cols > 0) {
+        split_f64_kernel<<<(unsigned)ceil_div(n_cols, 256), 256, 0, st>>>(x, xsplit, xsplit + n_cols, n_cols);
+        FLG_LAUNCH_CHECK();
+    }
+    prof_begin(FLG_SLOT_GEMV, st);
+    gemv_f32_kernel<true><<<(unsigned)ceil_div(n_rows, kGvRows), 32 * kGvWarps, 0, st>>>(
+        n_rows, n_cols, A, ld, nullptr, xsplit, xsplit + n_cols, y);
+    FLG_LAUNCH_CHECK();
+    prof_end(FLG_SLOT_GEMV, st);
+    return FLG_OK;
+}
+}  // namespace flg
 
 extern "C" int flg_convert_f64_f32(int64_t n_rows, int64_t n_cols, const double *src, int64_t lds, float *dst,
                                    int64_t ldd, void *stream) {

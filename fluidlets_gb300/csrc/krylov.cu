@@ -527,6 +527,8 @@ static int gmres_run(int kind, double are, double aim, const double *X, const do
 }
 
 // ---- dense GMRES-IR (flg_gmres_ir_dense) -------------------------------------------
+int gemv_f32_presplit(int64_t n_rows, int64_t n_cols, const float *A, int64_t ld, const double *x, float *xsplit,
+                      double *y, cudaStream_t st);
 int lu_solve_lowp_apply(int64_t n, const float *LU, int64_t ld, const float *dinv, const double *b, double *x,
                         void *work, size_t work_bytes, cudaStream_t st);
 size_t lu_solve_lowp_bytes(int64_t n);
@@ -575,6 +577,7 @@ extern "C" size_t flg_gmres_ir_dense_workspace(int64_t n, int restart) {
     Gmres<double>::carve_sizes(n, restart, c);  // inner preconditioned solve
     c.take<double>(n);                          // correction
     c.take<char>(lu_solve_lowp_bytes(n));
+    c.take<float>(2 * n);                       // x split into FP32 parts for the inner matvec
     return c.bytes();
 }
 
@@ -596,12 +599,13 @@ extern "C" int flg_gmres_ir_dense(int64_t n, const double *A, int64_t ld, const 
     double *d = ar.take<double>(n);
     const size_t lsb = lu_solve_lowp_bytes(n);
     char *lw = ar.take<char>(lsb);
-    FLG_REQUIRE(d && lw, "workspace too small for GMRES-IR");
+    float *xs = ar.take<float>(2 * n);
+    FLG_REQUIRE(d && lw && xs, "workspace too small for GMRES-IR");
     // outer residuals with the FP64 matrix; inner (preconditioned, tolerance 1e-4) matvecs
     // with the FP32 copy when the caller provides one
     g.A = [&](const double *v, double *out) { return flg_gemv_f64(n, n, A, ld, v, out, st); };
     if (A32)
-        gi.A = [&](const double *v, double *out) { return flg_gemv_f32(n, n, A32, lda32, v, out, st); };
+        gi.A = [&](const double *v, double *out) { return gemv_f32_presplit(n, n, A32, lda32, v, xs, out, st); };
     else
         gi.A = g.A;
     gi.M = [&](const double *v, double *out) { return lu_solve_lowp_apply(n, LU32, ld32, dinv, v, out, lw, lsb, st); };

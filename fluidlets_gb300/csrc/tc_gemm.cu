@@ -3,13 +3,14 @@
 //   C (m x nc, FP32, row-major, ldc)  -=  A (m x K) * B^T,  B given as Bt (nc x K)
 //
 // Both operands are K-major (K contiguous per row, K a multiple of 128).  A
-// persistent kernel, one CTA per SM, walks the 128 x 128 tiles of C:
+// persistent kernel, one CTA per SM, walks the 128 x 256 tiles of C:
 //   * warp 0 (one lane) streams K-blocks of A and B (128 B = 32 TF32 or 64 BF16
 //     per row) with TMA (cp.async.bulk.tensor, 128-byte swizzle) into a
 //     4-stage shared-memory ring guarded by mbarriers;
-//   * warp 1 (one lane) issues tcgen05.mma (cta_group::1, M = N = 128;
-//     kind::tf32, or kind::f16 with BF16 operands) into one of two 128-column
-//     TMEM accumulators and releases each stage with tcgen05.commit;
+//   * warp 1 (one lane) issues tcgen05.mma (cta_group::1, M = 128, N = 256;
+//     kind::tf32, or kind::f16 with BF16 operands) into one of two 256-column
+//     TMEM accumulators (all 512 columns) and releases each stage with
+//     tcgen05.commit;
 //   * warps 2-5 drain the other accumulator (tcgen05.ld, 32 TMEM lanes each),
 //     stage -acc in 32 x 32 swizzled boxes and add them to C with TMA
 //     reduce-add (cp.reduce.async.bulk.tensor): C is never read by the SM and
@@ -28,12 +29,14 @@
 
 namespace flg {
 
-constexpr int TC_BM = 128, TC_BN = 128, TC_STAGES = 4, TC_THREADS = 192, TC_EPI_WARPS = 4;
-constexpr int TC_TILE_BYTES = 128 * 128;  // one operand tile of a K-block: 128 rows x 128 B
+constexpr int TC_BM = 128, TC_BN = 256, TC_STAGES = 4, TC_THREADS = 192, TC_EPI_WARPS = 4;
+constexpr int TC_A_BYTES = TC_BM * 128;   // A tile of a K-block: 128 rows x 128 B
+constexpr int TC_B_BYTES = TC_BN * 128;   // B tile of a K-block: 256 rows x 128 B
 constexpr int TC_STG_BYTES = 32 * 128;    // one 32 x 32 FP32 staging box
-constexpr uint32_t TC_TMEM_COLS = 256;    // two 128-column accumulators
+constexpr uint32_t TC_TMEM_COLS = 2 * TC_BN;  // two 256-column accumulators: all of TMEM
 constexpr long long TC_WAIT_LIMIT = 2000000000LL;  // ~1 s of SM clock per wait
-constexpr size_t TC_SMEM = 1024 + 2 * TC_STAGES * TC_TILE_BYTES + TC_EPI_WARPS * 2 * TC_STG_BYTES;
+constexpr size_t TC_SMEM = 1024 + TC_STAGES * (TC_A_BYTES + TC_B_BYTES) + TC_EPI_WARPS * 2 * TC_STG_BYTES;
+static_assert(TC_SMEM <= 232448 - 256, "shared memory per CTA");
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -105,7 +108,7 @@ __device__ __forceinline__ uint64_t sw128_desc(const void *p) {
     return d;
 }
 
-// instruction descriptor: D = F32, A/B format (TF32 = 2, BF16 = 1), K-major A and B, M = N = 128
+// instruction descriptor: D = F32, A/B format (TF32 = 2, BF16 = 1), K-major A and B, M = 128, N = 256
 __host__ __device__ constexpr uint32_t tc_idesc(uint32_t fmt) {
     return (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(TC_BN >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
 }
@@ -120,7 +123,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_update_kernel(const __grid_c
     constexpr uint32_t IDESC = tc_idesc(MODE == FLG_LU_TF32 ? 2u : 1u);
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint8_t *sA = smem, *sB = smem + TC_STAGES * TC_TILE_BYTES, *stg = smem + 2 * TC_STAGES * TC_TILE_BYTES;
+    uint8_t *sA = smem, *sB = smem + TC_STAGES * TC_A_BYTES, *stg = sB + TC_STAGES * TC_B_BYTES;
     __shared__ __align__(8) uint64_t full[TC_STAGES], empty[TC_STAGES], accf[2], acce[2], mma_done;
     __shared__ uint32_t tmem_base;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -162,9 +165,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_update_kernel(const __grid_c
                         ok = false;
                         break;
                     }
-                    mbar_expect_tx(&full[s], 2 * TC_TILE_BYTES);
-                    tma_load_2d(sA + s * TC_TILE_BYTES, &tmA, &full[s], kb * KBLK, m0);
-                    tma_load_2d(sB + s * TC_TILE_BYTES, &tmB, &full[s], kb * KBLK, n0);
+                    mbar_expect_tx(&full[s], TC_A_BYTES + TC_B_BYTES);
+                    tma_load_2d(sA + s * TC_A_BYTES, &tmA, &full[s], kb * KBLK, m0);
+                    tma_load_2d(sB + s * TC_B_BYTES, &tmB, &full[s], kb * KBLK, n0);
                 }
             }
             // the last (up to S) loads issued must have landed before the CTA exits
@@ -193,8 +196,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_update_kernel(const __grid_c
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
                     for (int kk = 0; kk < 128 / KSTEP_BYTES; kk++) {
-                        const uint64_t ad = sw128_desc(sA + s * TC_TILE_BYTES + kk * KSTEP_BYTES);
-                        const uint64_t bd = sw128_desc(sB + s * TC_TILE_BYTES + kk * KSTEP_BYTES);
+                        const uint64_t ad = sw128_desc(sA + s * TC_A_BYTES + kk * KSTEP_BYTES);
+                        const uint64_t bd = sw128_desc(sB + s * TC_B_BYTES + kk * KSTEP_BYTES);
                         const uint32_t acc = (kb | kk) ? 1u : 0u;
                         if constexpr (MODE == FLG_LU_TF32) {
                             asm volatile(
@@ -305,8 +308,9 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     return fn;
 }
 
-// operand map: rows x K K-major elements (row stride ld_elems), box 128 rows x 128 bytes, 128B swizzle
-static int make_operand_map(CUtensorMap *map, const void *base, int64_t rows, int64_t K, int64_t ld_elems, int mode) {
+// operand map: rows x K K-major elements (row stride ld_elems), box box_rows x 128 bytes, 128B swizzle
+static int make_operand_map(CUtensorMap *map, const void *base, int64_t rows, int64_t K, int64_t ld_elems, int mode,
+                            int box_rows) {
     auto fn = encode_fn();
     FLG_REQUIRE(fn != nullptr, "cuTensorMapEncodeTiled unavailable");
     const bool bf = mode == FLG_LU_BF16;
@@ -314,7 +318,7 @@ static int make_operand_map(CUtensorMap *map, const void *base, int64_t rows, in
     FLG_REQUIRE(((uintptr_t)base & 15) == 0 && (ld_elems * esz) % 16 == 0, "TMA operand not 16-byte aligned");
     cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
     cuuint64_t strides[1] = {(cuuint64_t)(ld_elems * esz)};
-    cuuint32_t box[2] = {(cuuint32_t)(128 / esz), (cuuint32_t)TC_BM};
+    cuuint32_t box[2] = {(cuuint32_t)(128 / esz), (cuuint32_t)box_rows};
     cuuint32_t estr[2] = {1, 1};
     CUresult r = fn(map, bf ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
                     const_cast<void *>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -379,8 +383,8 @@ int tc_update(float *C, int64_t ldc, const float *Lp, int64_t ldl, const float *
     FLG_REQUIRE(err != nullptr && own != nullptr, "workspace too small for the tensor-core update");
     CUtensorMap ma, mb, mc;
     if (mode == FLG_LU_TF32) {
-        FLG_TRY(make_operand_map(&ma, Lp, m, K, ldl, mode));
-        FLG_TRY(make_operand_map(&mb, Ut, nc, K, ldu, mode));
+        FLG_TRY(make_operand_map(&ma, Lp, m, K, ldl, mode, TC_BM));
+        FLG_TRY(make_operand_map(&mb, Ut, nc, K, ldu, mode, TC_BN));
     } else {
         __nv_bfloat16 *La = ar.take<__nv_bfloat16>((size_t)m * K);
         __nv_bfloat16 *Ub = ar.take<__nv_bfloat16>((size_t)nc * K);
@@ -389,8 +393,8 @@ int tc_update(float *C, int64_t ldc, const float *Lp, int64_t ldl, const float *
         FLG_LAUNCH_CHECK();
         f32_to_bf16_rows_kernel<<<(unsigned)ceil_div(nc * K, 256), 256, 0, st>>>(Ut, ldu, Ub, nc, K);
         FLG_LAUNCH_CHECK();
-        FLG_TRY(make_operand_map(&ma, La, m, K, K, mode));
-        FLG_TRY(make_operand_map(&mb, Ub, nc, K, K, mode));
+        FLG_TRY(make_operand_map(&ma, La, m, K, K, mode, TC_BM));
+        FLG_TRY(make_operand_map(&mb, Ub, nc, K, K, mode, TC_BN));
     }
     FLG_TRY(make_c_map(&mc, C, m, nc, ldc));
     if (!err_dev) FLG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
