@@ -713,35 +713,48 @@ static int copy2d(cudaStream_t st, const float *src, int64_t lds, float *dst, in
 // x = U^-1 L^-1 b for one right-hand side, FP32 factors, as a dataflow over the
 // 128-row blocks in ONE cooperative launch.  CTA c owns blocks c, c + G, ...
 // (G CTAs).  Forward: y_i = Linv_i (b_i - sum_{j<i} L_ij y_j); the owner of
-// block i consumes y_0, y_1, ... as their owners publish them (a release flag
-// per block, acquired with a bounded spin), accumulating L_ij y_j for all of
-// its blocks, and finalizes block i as soon as y_{i-1} has arrived.  The two
-// operands on that critical step -- L_{i,i-1} and Linv_i -- are prefetched
-// into registers before the wait.  Backward: the same in reverse with U and
-// Uinv on x_i = Uinv_i (y_i - sum_{j>i} U_ij x_j).  Every wait depends only
-// on blocks earlier in the order (forward by increasing, then backward by
-// decreasing index) and all CTAs are resident, so the order always advances.
-// 512 threads: thread t covers row t / 4 of a block, columns 32 (t % 4) + 0..31.
+// block i consumes y_0, y_1, ... as their owners publish them, accumulating
+// L_ij y_j for all of its blocks, and finalizes block i as soon as y_{i-1} has
+// arrived.  The two operands on that critical step -- L_{i,i-1} and Linv_i --
+// are prefetched into registers before the wait.  Backward: the same in
+// reverse with U and Uinv on x_i = Uinv_i (y_i - sum_{j>i} U_ij x_j).
+// Publication is the data itself: y and x start filled with an all-ones bit
+// pattern (a NaN that FP32 arithmetic never produces; results are stored
+// canonicalized), values are stored with st.relaxed.gpu and consumers poll
+// their element with ld.relaxed.gpu (bounded) -- no flag, no fence.  Every
+// wait is on a block earlier in the global order (forward by increasing, then
+// backward by decreasing index) and all CTAs are resident, so the order always
+// advances.  512 threads: thread t covers row t / 4 of a block, columns
+// 32 (t % 4) + 0..31.
 constexpr int kApplyThreads = 512;
-constexpr int kApplyMaxOwn = 8;  // blocks per CTA
+constexpr unsigned kUnset = 0xffffffffu;
+
+// A 128-entry vector in shared memory is stored as four 32-float quarters kQP
+// floats apart: the four quarters that the threads of a warp read at once then
+// sit in different banks (with a plain 32-float stride, all four hit the same
+// bank, a 4-way conflict on every load).
+constexpr int kQP = 36;
+__device__ __forceinline__ int qpos(int e) { return (e >> 5) * kQP + (e & 31); }
+
 
 struct ApplyArgs {
     const float *LU;
     int64_t ld, n;
     const float *Linv, *Uinv;
     const float *b;  // right-hand side (FP32, n)
-    float *y, *x;    // forward / backward results (n)
-    int *fflag, *bflag;  // per-block ready flags (zeroed before the launch)
-    int *err;            // a wait ran out
+    float *y, *x;    // forward / backward results (n), preset to kUnset
+    int *err;        // a wait ran out
 };
 
-__device__ __forceinline__ int ld_acquire_i32(const int *p) {
-    int v;
-    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+__device__ __forceinline__ unsigned ld_relaxed_u32(const float *p) {
+    unsigned v;
+    asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
-__device__ __forceinline__ void st_release_i32(int *p, int v) {
-    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+__device__ __forceinline__ void st_relaxed_f32(float *p, float v) {
+    unsigned u = __float_as_uint(v);
+    if (u == kUnset) u = 0x7fffffffu;  // keep the sentinel unique
+    asm volatile("st.relaxed.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(u) : "memory");
 }
 
 // 32-wide slice of a row (`valid` leading entries exist; zeros for the rest)
@@ -757,15 +770,6 @@ __device__ __forceinline__ void load_row32(float (&v)[32], const float *p, int v
         for (int c = 0; c < 32; c++) v[c] = c < valid ? __ldg(p + c) : 0.0f;
     }
 }
-__device__ __forceinline__ float dot32(const float (&v)[32], const float *s) {
-    float a0 = 0.f, a1 = 0.f;
-#pragma unroll
-    for (int c = 0; c < 32; c += 2) {
-        a0 = fmaf(v[c], s[c], a0);
-        a1 = fmaf(v[c + 1], s[c + 1], a1);
-    }
-    return a0 + a1;
-}
 // sum over the four threads of a row (consecutive lanes)
 __device__ __forceinline__ float row_sum4(float v) {
     v += __shfl_xor_sync(0xffffffffu, v, 1);
@@ -773,108 +777,166 @@ __device__ __forceinline__ float row_sum4(float v) {
     return v;
 }
 
-// thread 0 waits for *flag; false (for the whole CTA) if a wait ran out here or elsewhere
-__device__ bool wait_block(const int *flag, int *err, int *abort_s) {
-    if (threadIdx.x == 0) {
-        const long long t0 = clock64();
-        while (ld_acquire_i32(flag) == 0) {
-            if (*(volatile int *)err || clock64() - t0 > kSpinLimit) {
-                atomicExch(err, 1);
-                *abort_s = 1;
-                break;
+// vec = block j of src, each of the first 128 threads waiting (bounded) for its
+// element to be published (`first` is an earlier probe of that element);
+// false (for the whole CTA) if a wait ran out here or elsewhere
+__device__ bool fetch_block(float *vec, const float *src, int64_t j, int64_t n, unsigned first, int *err,
+                            int *abort_s) {
+    const int t = threadIdx.x;
+    if (t < kNB) {
+        const int64_t e = j * kNB + t;
+        float v = 0.0f;
+        if (e < n) {
+            unsigned u = first;
+            if (u == kUnset) {
+                const long long t0 = clock64();
+                while ((u = ld_relaxed_u32(src + e)) == kUnset) {
+                    if (*(volatile int *)err || clock64() - t0 > kSpinLimit) {
+                        atomicExch(err, 1);
+                        *abort_s = 1;
+                        break;
+                    }
+                }
             }
+            v = __uint_as_float(u);
         }
+        vec[qpos(t)] = v;
     }
     __syncthreads();
     return *(volatile int *)abort_s == 0;
 }
 
+// Per-thread prefetch ring: thread t's 32-float slice of each consumed block goes
+// to shared memory by cp.async (kRing blocks in flight, 64 KB each per CTA);
+// 16-byte chunk c of thread t sits at chunk position c ^ (t % 8), so the
+// LDS.128 reads of a warp are free of bank conflicts.
+constexpr int kRing = 3;
+constexpr size_t kApplySmem = (size_t)kRing * kApplyThreads * 32 * sizeof(float);
+
+__device__ __forceinline__ void ring_issue(float *slot, const float *src, int valid_floats) {
+    const int t = threadIdx.x;
+    float *dst = slot + t * 32;
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+        const int bytes = max(0, min(16, (valid_floats - 4 * c) * 4));
+        const float *g = bytes > 0 ? src + 4 * c : src;  // a valid address even when nothing is read
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(
+                         (unsigned)__cvta_generic_to_shared(dst + 4 * (c ^ (t & 7)))),
+                     "l"(g), "r"(bytes)
+                     : "memory");
+    }
+}
+// dot of a 32-float slice with quarter v (kQP layout), float4 reads
+__device__ __forceinline__ float dot32q(const float (&w)[32], const float *v) {
+    float a0 = 0.f, a1 = 0.f;
+#pragma unroll
+    for (int c = 0; c < 32; c += 4) {
+        const float4 x = *reinterpret_cast<const float4 *>(v + c);
+        a0 = fmaf(w[c], x.x, a0);
+        a1 = fmaf(w[c + 1], x.y, a1);
+        a0 = fmaf(w[c + 2], x.z, a0);
+        a1 = fmaf(w[c + 3], x.w, a1);
+    }
+    return a0 + a1;
+}
+__device__ __forceinline__ float ring_dot(const float *slot, const float *v) {
+    const int t = threadIdx.x;
+    const float *src = slot + t * 32;
+    float a0 = 0.f, a1 = 0.f;
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+        const float4 w = *reinterpret_cast<const float4 *>(src + 4 * (c ^ (t & 7)));
+        const float4 x = *reinterpret_cast<const float4 *>(v + 4 * c);
+        a0 = fmaf(w.x, x.x, a0);
+        a1 = fmaf(w.y, x.y, a1);
+        a0 = fmaf(w.z, x.z, a0);
+        a1 = fmaf(w.w, x.w, a1);
+    }
+    return a0 + a1;
+}
+
+// loads that stay where they are written (volatile asm is not moved past the other
+// volatile asm of the loop), so operands needed after a wait are fetched before it
+__device__ __forceinline__ void load_row32_early(float (&v)[32], const float *p) {
+#pragma unroll
+    for (int c = 0; c < 32; c += 4)
+        asm volatile("ld.global.nc.v4.f32 {%0, %1, %2, %3}, [%4];"
+                     : "=f"(v[c]), "=f"(v[c + 1]), "=f"(v[c + 2]), "=f"(v[c + 3])
+                     : "l"(p + c));
+}
+__device__ __forceinline__ float load_f32_early(const float *p) {
+    float v;
+    asm volatile("ld.global.nc.f32 %0, [%1];" : "=f"(v) : "l"(p));
+    return v;
+}
+
 __global__ void __launch_bounds__(kApplyThreads) lowp_apply_kernel(ApplyArgs a) {
-    __shared__ __align__(16) float vec[kNB];   // the block being consumed
-    __shared__ __align__(16) float tvec[kNB];  // t_i of the block being finalized
-    __shared__ float acc[kApplyMaxOwn][kApplyThreads];
+    extern __shared__ __align__(16) float ring[];  // [kRing][kApplyThreads * 32]
+    __shared__ __align__(16) float vec[4 * kQP];    // the block being consumed (kQP layout)
+    __shared__ __align__(16) float tvec[4 * kQP];   // t_i of the block being finalized (kQP layout)
     __shared__ int abort_s;
     const int t = threadIdx.x, r = t >> 2, q = t & 3;
     const int G = gridDim.x, c = blockIdx.x;
     const int nblk = (int)ceil_div(a.n, kNB);
     const int nown = c < nblk ? (nblk - 1 - c) / G + 1 : 0;
     if (t == 0) abort_s = 0;
-    // the valid part of a 32-column slice starting at column col0
-    auto valid_cols = [&](int64_t col0) { return (int)max((int64_t)0, min((int64_t)32, a.n - col0)); };
+    __syncthreads();
     for (int pass = 0; pass < 2 && nown > 0; pass++) {
         const bool fwd = pass == 0;
+        const int dir = fwd ? 1 : -1;
         const float *D = fwd ? a.Linv : a.Uinv;
-        const float *src = fwd ? a.y : a.x;  // the published blocks consumed by this pass
-        int *flag = fwd ? a.fflag : a.bflag;
-        for (int m = 0; m < nown; m++) acc[m][t] = 0.0f;
-        __syncthreads();
-        // processing position mi -> owned slot m (ascending blocks forward, descending backward)
-        auto slot = [&](int mi) { return fwd ? mi : nown - 1 - mi; };
-        int mi = 0, i = 0, jc = 0;
-        float P[32], Dr[32];
-        int64_t row = 0;
-        bool rok = false;
-        // make owned block (position mi) the target and prefetch its critical operands
-        auto target = [&]() {
-            i = c + slot(mi) * G;
-            jc = fwd ? i - 1 : i + 1;
-            row = (int64_t)i * kNB + r;
-            rok = row < a.n;
-            const bool has = fwd ? i > 0 : i < nblk - 1;
-            const int64_t col0 = (int64_t)jc * kNB + 32 * q;
-            if (has && rok) load_row32(P, a.LU + row * a.ld + col0, valid_cols(col0));
-            else load_row32(P, a.LU, 0);
-            load_row32(Dr, D + (int64_t)i * kNB * kNB + r * kNB + 32 * q, 32);
-        };
-        // block i: t_i = rhs_i - sum_j (...) , out_i = D_i t_i, then publish
-        auto finalize = [&]() {
-            const float tot = row_sum4(acc[slot(mi)][t]);
+        float *out_v = fwd ? a.y : a.x;  // this pass publishes into out_v and consumes from it
+        // owned blocks in order: ascending forward, descending backward
+        for (int mi = 0; mi < nown; mi++) {
+            const int i = c + (fwd ? mi : nown - 1 - mi) * G;
+            const int64_t row = (int64_t)i * kNB + r;
+            const bool rok = row < a.n;
+            float Dr[32];
+            load_row32_early(Dr, D + (int64_t)i * kNB * kNB + r * kNB + 32 * q);
             float rhs = 0.0f;
-            if (rok) rhs = fwd ? __ldg(a.b + row) : __ldcg(a.y + row);
-            if (q == 0) tvec[r] = rok ? rhs - tot : 0.0f;
+            if (rok) rhs = fwd ? load_f32_early(a.b + row) : __uint_as_float(ld_relaxed_u32(a.y + row));
+            // consume blocks jfirst, jfirst + dir, ..., i - dir (nc of them), kRing slices ahead
+            const int jfirst = fwd ? 0 : nblk - 1;
+            const int nc = fwd ? i : nblk - 1 - i;
+            auto issue = [&](int k) {
+                const int j = jfirst + dir * k;
+                const int64_t col0 = (int64_t)j * kNB + 32 * q;
+                const int valid = rok ? (int)max((int64_t)0, min((int64_t)32, a.n - col0)) : 0;
+                ring_issue(ring + (k % kRing) * (kApplyThreads * 32), rok ? a.LU + row * a.ld + col0 : a.LU, valid);
+                asm volatile("cp.async.commit_group;" ::: "memory");
+            };
+            auto probe = [&](int k) {
+                const int64_t e = (int64_t)(jfirst + dir * k) * kNB + t;
+                return (t < kNB && e < a.n) ? ld_relaxed_u32(out_v + e) : 0u;
+            };
+            float acc = 0.0f;
+            int issued = 0;
+            for (; issued < min(kRing, nc); issued++) issue(issued);
+            unsigned pc = nc > 0 ? probe(0) : 0u;
+            for (int k = 0; k < nc; k++) {
+                // slice k has landed once at most (issued - k - 1) newer groups are pending
+                const int pend = issued - k - 1;
+                if (pend >= 2) asm volatile("cp.async.wait_group 2;" ::: "memory");
+                else if (pend == 1) asm volatile("cp.async.wait_group 1;" ::: "memory");
+                else asm volatile("cp.async.wait_group 0;" ::: "memory");
+                const unsigned pn = k + 1 < nc ? probe(k + 1) : 0u;
+                if (!fetch_block(vec, out_v, jfirst + dir * k, a.n, pc, a.err, &abort_s)) {
+                    asm volatile("cp.async.wait_all;" ::: "memory");
+                    return;
+                }
+                acc += ring_dot(ring + (k % kRing) * (kApplyThreads * 32), vec + q * kQP);
+                __syncthreads();  // vec is rewritten next
+                if (issued < nc) issue(issued++);  // reuses slot k % kRing, just read by this thread
+                pc = pn;
+            }
+            // finalize block i: t_i = rhs_i - sum, out_i = D_i t_i, published element by element
+            const float tot = row_sum4(acc);
+            if (q == 0) tvec[qpos(r)] = rok ? rhs - tot : 0.0f;
             __syncthreads();
-            const float out = row_sum4(dot32(Dr, tvec + 32 * q));
-            if (q == 0 && rok) (fwd ? a.y : a.x)[row] = out;
-            __threadfence();  // each writer orders its own store before the release below
-            __syncthreads();
-            if (t == 0) st_release_i32(flag + i, 1);
-        };
-        target();
-        if (fwd ? i == 0 : i == nblk - 1) {  // nothing to consume first
-            finalize();
-            if (++mi < nown) target();
+            const float out = row_sum4(dot32q(Dr, tvec + q * kQP));
+            if (q == 0 && rok) st_relaxed_f32(out_v + row, out);
+            __syncthreads();  // tvec is rewritten by the next block
         }
-        for (int j = fwd ? 0 : nblk - 1; mi < nown; j += fwd ? 1 : -1) {
-            if (!wait_block(flag + j, a.err, &abort_s)) return;
-            if (t < kNB) {
-                const int64_t e = (int64_t)j * kNB + t;
-                vec[t] = e < a.n ? __ldcg(src + e) : 0.0f;
-            }
-            __syncthreads();
-            const int64_t col0 = (int64_t)j * kNB + 32 * q;
-            const int vc = valid_cols(col0);
-            float v[32];
-            // the target's contribution first: on the critical path when j == jc
-            if (j == jc) {
-                acc[slot(mi)][t] += dot32(P, vec + 32 * q);
-            } else {
-                if (rok) load_row32(v, a.LU + row * a.ld + col0, vc);
-                else load_row32(v, a.LU, 0);
-                acc[slot(mi)][t] += dot32(v, vec + 32 * q);
-            }
-            const bool fin = j == jc;
-            if (fin) finalize();
-            // the owned blocks after the target consume block j as well
-            for (int mm = mi + 1; mm < nown; mm++) {
-                const int64_t row2 = (int64_t)(c + slot(mm) * G) * kNB + r;
-                if (row2 < a.n) load_row32(v, a.LU + row2 * a.ld + col0, vc);
-                else load_row32(v, a.LU, 0);
-                acc[slot(mm)][t] += dot32(v, vec + 32 * q);
-            }
-            __syncthreads();  // vec is rewritten by the next consumed block
-            if (fin && ++mi < nown) target();
-        }
-        __syncthreads();
     }
 }
 
@@ -890,11 +952,10 @@ __global__ void f2d_kernel(const float *a, double *b, int64_t n, const int *err)
 
 size_t lu_solve_lowp_bytes(int64_t n) {
     CountingArena c;
-    const int64_t nblk = ceil_div(std::max<int64_t>(n, 1), kNB);
     c.take<float>(n);
     c.take<float>(n);
     c.take<float>(n);
-    c.take<int>(2 * nblk + 1);
+    c.take<int>(1);
     return c.bytes();
 }
 
@@ -906,21 +967,27 @@ int lu_solve_lowp_apply(int64_t n, const float *LU, int64_t ld, const float *din
     float *bf = ar.take<float>(n);
     float *y = ar.take<float>(n);
     float *z = ar.take<float>(n);
-    int *flags = ar.take<int>(2 * nblk + 1);
-    FLG_REQUIRE(bf && y && z && flags, "workspace too small for the low-precision solve");
+    int *err = ar.take<int>(1);
+    FLG_REQUIRE(bf && y && z && err, "workspace too small for the low-precision solve");
     const int G = (int)std::min<int64_t>(nblk, sm_count());
-    FLG_REQUIRE(nblk <= (int64_t)kApplyMaxOwn * G, "system too large for the low-precision solve (%lld blocks)",
-                (long long)nblk);
     d2f_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(b, bf, n);
     FLG_LAUNCH_CHECK();
-    FLG_CUDA(cudaMemsetAsync(flags, 0, sizeof(int) * (2 * nblk + 1), st));
-    ApplyArgs aa{LU, ld, n, dinv, dinv + nblk * kNB * kNB, bf, y, z, flags, flags + nblk, flags + 2 * nblk};
+    // y and z adjacent: one fill with the unset pattern
+    FLG_CUDA(cudaMemsetAsync(y, 0xff, sizeof(float) * (size_t)(z + n - y), st));
+    FLG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
+    ApplyArgs aa{LU, ld, n, dinv, dinv + nblk * kNB * kNB, bf, y, z, err};
     void *args[] = {&aa};
+    static bool attr_set = false;
+    if (!attr_set) {
+        FLG_CUDA(cudaFuncSetAttribute(lowp_apply_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kApplySmem));
+        attr_set = true;
+    }
     prof_begin(FLG_SLOT_LU_SOLVE, st);
-    FLG_CUDA(cudaLaunchCooperativeKernel((void *)lowp_apply_kernel, dim3(G), dim3(kApplyThreads), args, 0, st));
+    FLG_CUDA(cudaLaunchCooperativeKernel((void *)lowp_apply_kernel, dim3(G), dim3(kApplyThreads), args, kApplySmem,
+                                         st));
     count_launch();
     prof_end(FLG_SLOT_LU_SOLVE, st);
-    f2d_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(z, x, n, flags + 2 * nblk);
+    f2d_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(z, x, n, err);
     FLG_LAUNCH_CHECK();
     return FLG_OK;
 }
