@@ -142,14 +142,15 @@ __global__ void __launch_bounds__(256) panel_f64_kernel(PanelArgs a) {
             for (int q = threadIdx.x; q < kb; q += blockDim.x) a.diagbuf[buf * kb + q] = P[(g - r0) * kb + q];
         __threadfence();
         if (!grid_sync(a.bar, nblk)) return;
-        // global argmax
-        if (threadIdx.x == 0) {
+        // global argmax over the CTAs' candidates: warp 0, lane-strided, then a shuffle
+        // reduction (largest |value|, first row on ties)
+        if (threadIdx.x < 32) {
             double bv = -1.0;
             long long br = LLONG_MAX;
             int wc = -1;
-            for (int q = 0; q < nblk; q++) {
-                const double v = ((volatile double *)a.slot_val)[buf * nblk + q];
-                const long long r = ((volatile long long *)a.slot_row)[buf * nblk + q];
+            for (int q = threadIdx.x; q < nblk; q += 32) {
+                const double v = __ldcg(a.slot_val + buf * nblk + q);
+                const long long r = __ldcg(a.slot_row + buf * nblk + q);
                 if (r == LLONG_MAX) continue;
                 if (v > bv || (v == bv && r < br)) {
                     bv = v;
@@ -157,13 +158,22 @@ __global__ void __launch_bounds__(256) panel_f64_kernel(PanelArgs a) {
                     wc = q;
                 }
             }
-            if (wc < 0) {  // no finite candidate: keep row g
-                br = g;
-                wc = -1;
+            for (int o = 16; o > 0; o >>= 1) {
+                const double ov = __shfl_xor_sync(0xffffffffu, bv, o);
+                const long long orow = __shfl_xor_sync(0xffffffffu, br, o);
+                const int owc = __shfl_xor_sync(0xffffffffu, wc, o);
+                if (owc >= 0 && (wc < 0 || ov > bv || (ov == bv && orow < br))) {
+                    bv = ov;
+                    br = orow;
+                    wc = owc;
+                }
             }
-            s_p = br;
-            s_wc = wc;
-            if (c == 0) a.ipiv[g] = (int32_t)br;
+            if (threadIdx.x == 0) {
+                if (wc < 0) br = g;  // no finite candidate: keep row g
+                s_p = br;
+                s_wc = wc;
+                if (c == 0) a.ipiv[g] = (int32_t)br;
+            }
         }
         __syncthreads();
         const long long p = s_p;
@@ -283,6 +293,30 @@ __global__ void __launch_bounds__(256) dgemm_update_kernel(double *C, const doub
 }
 
 // ---- FP64 triangular solves (getrs) ------------------------------------------------
+// Row interchanges in LAPACK order (swap rows r and ipiv[r] for r = 0, 1, ...).
+// One CTA per right-hand side column; the column sits in shared memory while one
+// thread applies the swaps (they compose, so they are sequential), then goes back.
+constexpr int kPivSmemMax = 24576;  // doubles (192 KB)
+__global__ void __launch_bounds__(256) apply_pivots_smem_kernel(double *B, int64_t ldb, const int32_t *ipiv,
+                                                                int64_t n) {
+    extern __shared__ double col[];
+    const int64_t c = blockIdx.x;
+    for (int64_t r = threadIdx.x; r < n; r += blockDim.x) col[r] = B[r * ldb + c];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int64_t r = 0; r < n; r++) {
+            const int64_t p = ipiv[r];
+            if (p != r) {
+                const double t = col[r];
+                col[r] = col[p];
+                col[p] = t;
+            }
+        }
+    }
+    __syncthreads();
+    for (int64_t r = threadIdx.x; r < n; r += blockDim.x) B[r * ldb + c] = col[r];
+}
+// the same for columns too long for shared memory (one thread per column, global memory)
 __global__ void apply_pivots_kernel(double *B, int64_t ldb, int64_t nrhs, const int32_t *ipiv, int64_t n) {
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= nrhs) return;
@@ -296,25 +330,39 @@ __global__ void apply_pivots_kernel(double *B, int64_t ldb, int64_t nrhs, const 
     }
 }
 
-// solve the diagonal block [b0, b0+bs) in place (lower unit, or upper) for each rhs column
+// solve the diagonal block [b0, b0+bs) (bs <= 64) in place, lower unit or upper, for
+// right-hand side column blockIdx.x: the block goes to shared memory (coalesced), then
+// a column-oriented substitution with one thread per row and one barrier per column
 template <bool UPPER>
-__global__ void trsv_block_kernel(const double *LU, int64_t ld, double *B, int64_t ldb, int64_t nrhs, int64_t b0,
-                                  int bs) {
-    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= nrhs) return;
+__global__ void __launch_bounds__(64) trsv_block_kernel(const double *LU, int64_t ld, double *B, int64_t ldb,
+                                                        int64_t nrhs, int64_t b0, int bs) {
+    __shared__ double T[64][65];
+    __shared__ double x[64];
+    const int64_t c = blockIdx.x;
+    const int r = threadIdx.x;
+    for (int e = r; e < bs * bs; e += 64) {
+        const int i = e / bs, q = e - i * bs;
+        T[i][q] = LU[(b0 + i) * ld + b0 + q];
+    }
+    double v = r < bs ? B[(b0 + r) * ldb + c] : 0.0;
+    __syncthreads();
     if (!UPPER) {
-        for (int r = 0; r < bs; r++) {
-            double x = B[(b0 + r) * ldb + c];
-            for (int q = 0; q < r; q++) x = fma(-LU[(b0 + r) * ld + b0 + q], B[(b0 + q) * ldb + c], x);
-            B[(b0 + r) * ldb + c] = x;
+        for (int q = 0; q < bs; q++) {
+            if (r == q) x[q] = v;
+            __syncthreads();
+            if (r > q) v = fma(-T[r][q], x[q], v);
         }
     } else {
-        for (int r = bs - 1; r >= 0; r--) {
-            double x = B[(b0 + r) * ldb + c];
-            for (int q = r + 1; q < bs; q++) x = fma(-LU[(b0 + r) * ld + b0 + q], B[(b0 + q) * ldb + c], x);
-            B[(b0 + r) * ldb + c] = x / LU[(b0 + r) * ld + b0 + r];
+        for (int q = bs - 1; q >= 0; q--) {
+            if (r == q) {
+                v = v / T[q][q];
+                x[q] = v;
+            }
+            __syncthreads();
+            if (r < q) v = fma(-T[r][q], x[q], v);
         }
     }
+    if (r < bs) B[(b0 + r) * ldb + c] = v;
 }
 
 // B[rows r in [r0, r1)] -= LU[r, b0:b0+bs] * B[b0:b0+bs]; warp per (row, rhs)
@@ -1091,12 +1139,23 @@ extern "C" int flg_lu_solve_f64(int64_t n, int64_t nrhs, const double *LU, int64
     FLG_REQUIRE(n >= 0 && nrhs >= 0 && ld >= n && ldb >= nrhs, "bad LU solve arguments");
     if (n == 0 || nrhs == 0) return FLG_OK;
     cudaStream_t st = as_stream(stream);
-    apply_pivots_kernel<<<(unsigned)ceil_div(nrhs, 32), 32, 0, st>>>(B, ldb, nrhs, ipiv, n);
+    FLG_REQUIRE(nrhs <= 65535, "at most 65,535 right-hand sides per call");
+    if (n <= kPivSmemMax) {
+        static bool attr_set = false;
+        if (!attr_set) {
+            FLG_CUDA(cudaFuncSetAttribute(apply_pivots_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          kPivSmemMax * (int)sizeof(double)));
+            attr_set = true;
+        }
+        apply_pivots_smem_kernel<<<(unsigned)nrhs, 256, n * sizeof(double), st>>>(B, ldb, ipiv, n);
+    } else {
+        apply_pivots_kernel<<<(unsigned)ceil_div(nrhs, 32), 32, 0, st>>>(B, ldb, nrhs, ipiv, n);
+    }
     FLG_LAUNCH_CHECK();
     const int bsz = 64;
     for (int64_t b0 = 0; b0 < n; b0 += bsz) {
         const int bs = (int)std::min<int64_t>(bsz, n - b0);
-        trsv_block_kernel<false><<<(unsigned)ceil_div(nrhs, 32), 32, 0, st>>>(LU, ld, B, ldb, nrhs, b0, bs);
+        trsv_block_kernel<false><<<(unsigned)nrhs, 64, 0, st>>>(LU, ld, B, ldb, nrhs, b0, bs);
         FLG_LAUNCH_CHECK();
         if (b0 + bs < n) {
             const int64_t rows = n - b0 - bs;
@@ -1107,7 +1166,7 @@ extern "C" int flg_lu_solve_f64(int64_t n, int64_t nrhs, const double *LU, int64
     }
     for (int64_t b0 = ((n - 1) / bsz) * bsz; b0 >= 0; b0 -= bsz) {
         const int bs = (int)std::min<int64_t>(bsz, n - b0);
-        trsv_block_kernel<true><<<(unsigned)ceil_div(nrhs, 32), 32, 0, st>>>(LU, ld, B, ldb, nrhs, b0, bs);
+        trsv_block_kernel<true><<<(unsigned)nrhs, 64, 0, st>>>(LU, ld, B, ldb, nrhs, b0, bs);
         FLG_LAUNCH_CHECK();
         if (b0 > 0) {
             trsv_update_kernel<<<(unsigned)ceil_div(b0 * nrhs * 32, 256), 256, 0, st>>>(LU, ld, B, ldb, nrhs, b0, bs,

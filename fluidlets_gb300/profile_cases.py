@@ -103,7 +103,16 @@ def breakdown(a, kern):
     if a.n > 4096:  # the FP64 factorizations take seconds at this size
         return
     K = core._assemble_dev(kern, Xd, Xd, e, 1.0)
+    L.flg_profile_enable(1)
     _, t64 = t(lambda: core._lu_solve_dev(K.clone(), b))
+    slots = {}
+    for name, k in _lib.SLOT.items():
+        ms, n = ctypes.c_double(0), ctypes.c_int64(0)
+        L.flg_profile_read(k, ctypes.byref(ms), ctypes.byref(n))
+        if n.value:
+            slots[name] = (round(ms.value, 3), n.value)
+    L.flg_profile_enable(0)
+    print(f"[fp64] kernel slots (ms, launches): {slots}")
     torch.linalg.solve(K, b)  # library initialization outside the timing
     _, tcs = t(lambda: torch.linalg.solve(K, b))
     print(f"[fp64] LU factor+solve {t64:.2f} ms; cuSOLVER (torch.linalg.solve) {tcs:.2f} ms")
