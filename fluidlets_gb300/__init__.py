@@ -5,13 +5,14 @@ operator API (``evaluate``, ``assemble``, ``assemble_nearest``,
 ``resistance``, ``swimming_problem``), computed by hand-written CUDA kernels
 in ``libfluidlets_gb300.so``.
 """
-from .core import DENSE_MAX, SolveInfo, assemble, assemble_nearest, evaluate, nearest_neighbors, resistance
+from .core import DENSE_MAX, SolveInfo, assemble, assemble_nearest, evaluate, evaluate_grid, nearest_neighbors, resistance
 from .kernels import Brinkmanlet3D, Kernel, Stokeslet3D, VectorKernel, WallStokeslet3D
 from .stokeslet3d import stokeslet3d_velocity
 from .swimming import SwimmerShape, SwimState, Trajectory, swim, swimming_problem
 
 __version__ = "1.0.0"
 __all__ = [
+    "evaluate_grid",
     "stokeslet3d_velocity",
     "Kernel",
     "VectorKernel",

@@ -61,6 +61,8 @@ SIGNATURES = {
                                         c_int, _P, _P, _P, c_size_t, _P, POINTER(c_void_p)]),
     "flg_graph_launch": (c_int, [_P, _P]),
     "flg_graph_destroy": (c_int, [_P]),
+    "flg_grid_points": (c_int, [_P, c_int64, _P, c_int64, _P, c_int64, _P, _P]),
+    "flg_nearest_neighbors": (c_int, [_P, c_int64, _P, c_int64, _P, _P]),
     "flg_gemv_f64": (c_int, [c_int64, c_int64, _P, c_int64, _P, _P, _P]),
     "flg_gemv_f32": (c_int, [c_int64, c_int64, _P, c_int64, _P, _P, _P]),
     "flg_convert_f64_f32": (c_int, [c_int64, c_int64, _P, c_int64, _P, c_int64, _P]),

@@ -111,6 +111,35 @@ def evaluate(kernel, targets, sources, strengths, eps, mu=1.0, *, precision="fp6
     return _out(_evaluate_dev(kernel, X, Y, f, e, mu, precision), as_torch)
 
 
+def evaluate_grid(kernel, axes, sources, strengths, eps, mu=1.0, *, precision="fp64", field=False):
+    """Field on the structured grid ``axes = (x, y, z)`` (1-D coordinate arrays).
+
+    Equal to ``evaluate(kernel, grid, ...)`` with the grid the reference's examples build,
+    ``np.meshgrid(z, y, x, indexing="ij")`` raveled into ``c_[X, Y, Z]``
+    (``examples/glycocalyx_towers/run.py:48-51``): rows in VTK point order, x fastest.  The
+    grid points are generated on the device (no host grid array); ``field=True`` returns the
+    result shaped (nz, ny, nx, 3).
+    """
+    as_torch = dv.home(sources, strengths)
+    ax = [dv.to_dev(np.asarray(a, float) if not isinstance(a, torch.Tensor) else a, torch.float64).reshape(-1)
+          for a in axes]
+    if len(ax) != 3:
+        raise ValueError("axes must be three 1-D coordinate arrays (x, y, z)")
+    nx, ny, nz = (a.shape[0] for a in ax)
+    G = torch.empty((nx * ny * nz, 3), dtype=torch.float64, device=ax[0].device)
+    check(load().flg_grid_points(dv.ptr(ax[0]), nx, dv.ptr(ax[1]), ny, dv.ptr(ax[2]), nz, dv.ptr(G), dv.stream()),
+          "grid points")
+    Y = _points(sources, kernel.dim)
+    N = Y.shape[0]
+    e = _blob_widths(eps, N)
+    fc = dv.is_complex_value(strengths)
+    f = dv.to_dev(strengths, torch.complex128 if fc else torch.float64).reshape(N, 3)
+    u = _evaluate_dev(kernel, G, Y, f, e, mu, precision)
+    if field:
+        u = u.reshape(nz, ny, nx, 3)
+    return _out(u, as_torch)
+
+
 # ---- core/assemble.py:27-101 ------------------------------------------------
 def _assemble_dev(kernel, X, Y, e, mu, out_dtype=torch.float64, out=None, ld=None):
     kind, are, aim = kernel_params(kernel)
@@ -140,14 +169,25 @@ def assemble(kernel, targets, sources, eps, mu=1.0):
     return _out(_assemble_dev(kernel, X, Y, e, mu), as_torch)
 
 
-def nearest_neighbors(quad_points, force_points) -> np.ndarray:
+def _nearest_dev(Xq: torch.Tensor, x: torch.Tensor) -> torch.Tensor:
+    out = torch.empty(Xq.shape[0], dtype=torch.int64, device=Xq.device)
+    check(load().flg_nearest_neighbors(dv.ptr(Xq), Xq.shape[0], dv.ptr(x), x.shape[0], dv.ptr(out), dv.stream()),
+          "nearest_neighbors")
+    return out
+
+
+def nearest_neighbors(quad_points, force_points):
     """Index of the nearest force point for every quadrature point, shape (Q,) (``core/assemble.py:61-65``).
 
-    Host-side k-d tree (SciPy), as in the reference.
+    The reference queries a SciPy k-d tree on the host; here an exhaustive FP64 search on the
+    device gives the same indices (the first one on exact ties).
     """
-    from scipy.spatial import cKDTree
-
-    return cKDTree(np.asarray(force_points, float)).query(np.asarray(quad_points, float))[1]
+    as_torch = dv.home(quad_points, force_points)
+    Xq = _points(quad_points, 3)
+    x = _points(force_points, 3)
+    if Xq.shape[0] and not x.shape[0]:
+        raise ValueError("no force points to search")
+    return _out(_nearest_dev(Xq, x), as_torch)
 
 
 def _assemble_nearest_dev(kernel, X, Xq, nn, n_force, e, mu, out_dtype=torch.float64, out=None, ld=None):

@@ -659,6 +659,73 @@ int gemv_f32_presplit(int64_t n_rows, int64_t n_cols, const float *A, int64_t ld
 }
 }  // namespace flg
 
+// nearest force point of every quadrature point (the reference's k-d tree query,
+// core/assemble.py:61-65): exhaustive, FP64 squared distances, the first index
+// on ties; force points staged through shared memory in tiles of kNnTile
+constexpr int kNnTile = 1024;
+__global__ void __launch_bounds__(256) nearest_kernel(const double *quad, int64_t Q, const double *force, int64_t N,
+                                                      int64_t *out) {
+    __shared__ double fx[kNnTile], fy[kNnTile], fz[kNnTile];
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double px = 0.0, py = 0.0, pz = 0.0;
+    if (q < Q) px = quad[3 * q], py = quad[3 * q + 1], pz = quad[3 * q + 2];
+    double best = INFINITY;
+    int64_t bi = 0;
+    for (int64_t t0 = 0; t0 < N; t0 += kNnTile) {
+        const int nt = (int)min((int64_t)kNnTile, N - t0);
+        __syncthreads();
+        for (int k = threadIdx.x; k < nt; k += blockDim.x) {
+            fx[k] = force[3 * (t0 + k)];
+            fy[k] = force[3 * (t0 + k) + 1];
+            fz[k] = force[3 * (t0 + k) + 2];
+        }
+        __syncthreads();
+        for (int k = 0; k < nt; k++) {
+            const double dx = px - fx[k], dy = py - fy[k], dz = pz - fz[k];
+            const double d2 = dx * dx + dy * dy + dz * dz;
+            if (d2 < best) {
+                best = d2;
+                bi = t0 + k;
+            }
+        }
+    }
+    if (q < Q) out[q] = bi;
+}
+
+extern "C" int flg_nearest_neighbors(const double *quad, int64_t Q, const double *force, int64_t N, int64_t *out,
+                                     void *stream) {
+    FLG_REQUIRE(Q >= 0 && N >= 0, "negative sizes");
+    if (Q == 0) return FLG_OK;
+    FLG_REQUIRE(N > 0, "no force points to search");
+    FLG_REQUIRE(quad && force && out, "null pointer");
+    nearest_kernel<<<(unsigned)ceil_div(Q, 256), 256, 0, as_stream(stream)>>>(quad, Q, force, N, out);
+    FLG_LAUNCH_CHECK();
+    return FLG_OK;
+}
+
+// grid point (i, j, k) -> row i + nx (j + ny k): x fastest, then y, then z (VTK point order)
+__global__ void grid_points_kernel(const double *xa, int64_t nx, const double *ya, int64_t ny, const double *za,
+                                   int64_t nz, double *out) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nx * ny * nz) return;
+    const int64_t i = p % nx, j = (p / nx) % ny, k = p / (nx * ny);
+    out[3 * p] = xa[i];
+    out[3 * p + 1] = ya[j];
+    out[3 * p + 2] = za[k];
+}
+
+extern "C" int flg_grid_points(const double *x_axis, int64_t nx, const double *y_axis, int64_t ny,
+                               const double *z_axis, int64_t nz, double *points, void *stream) {
+    FLG_REQUIRE(nx >= 0 && ny >= 0 && nz >= 0, "negative grid size");
+    const int64_t np = nx * ny * nz;
+    if (np == 0) return FLG_OK;
+    FLG_REQUIRE(x_axis && y_axis && z_axis && points, "null pointer");
+    grid_points_kernel<<<(unsigned)ceil_div(np, 256), 256, 0, as_stream(stream)>>>(x_axis, nx, y_axis, ny, z_axis,
+                                                                                    nz, points);
+    FLG_LAUNCH_CHECK();
+    return FLG_OK;
+}
+
 extern "C" int flg_convert_f64_f32(int64_t n_rows, int64_t n_cols, const double *src, int64_t lds, float *dst,
                                    int64_t ldd, void *stream) {
     FLG_REQUIRE(n_rows >= 0 && n_cols >= 0 && lds >= n_cols && ldd >= n_cols, "bad conversion shape");

@@ -267,6 +267,20 @@ int flg_bucket_graph_create(int kind, double alpha_re, double alpha_im, const do
 int flg_graph_launch(void *graph_exec, void *stream);
 int flg_graph_destroy(void *graph_exec);
 
+/* Nearest force point of each quadrature point: out[q] = argmin_j |quad_q - force_j|
+ * (FP64, first index on ties); replaces the k-d tree query of
+ * core/assemble.py:61-65 (nearest_neighbors).  Exhaustive, O(Q N). */
+int flg_nearest_neighbors(const double *quad, int64_t Q, const double *force, int64_t N, int64_t *out, void *stream);
+
+/* ---- structured grids ----------------------------------------------------
+ * points (nx ny nz x 3, FP64) of the grid x_axis x y_axis x z_axis (device
+ * arrays), x fastest, then y, then z: the point order of the reference's
+ * examples (np.meshgrid(z, y, x, indexing="ij") raveled, e.g.
+ * examples/glycocalyx_towers/run.py:48-51) and of VTK structured grids.  A
+ * velocity field evaluated at these points (flg_evaluate) is in VTK order. */
+int flg_grid_points(const double *x_axis, int64_t nx, const double *y_axis, int64_t ny, const double *z_axis,
+                    int64_t nz, double *points, void *stream);
+
 /* ---- dense helpers --------------------------------------------------------
  * y = A x (FP64, row-major n_rows x n_cols, ld); used for residuals. */
 int flg_gemv_f64(int64_t n_rows, int64_t n_cols, const double *A, int64_t ld, const double *x, double *y,

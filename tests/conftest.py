@@ -29,6 +29,18 @@ def legacy_towers():
     return np.load(GOLDEN / "legacy_towers.npz")
 
 
+@pytest.fixture(scope="session")
+def legacy_grid():
+    return np.load(GOLDEN / "legacy_grid.npz")
+
+
+def legacy_grid_points(g):
+    """The 32^3 grid of tests/legacy/test_phase1_port.py:77-87, x fastest (meshgrid(z, y, x, 'ij'))."""
+    xs, ys, zs = (np.linspace(a[0], a[1], int(a[2])) for a in (g["x_axis"], g["y_axis"], g["z_axis"]))
+    Z, Y, X = np.meshgrid(zs, ys, xs, indexing="ij")
+    return (xs, ys, zs), np.c_[X.ravel(), Y.ravel(), Z.ravel()]
+
+
 def rel_err(a, b):
     a, b = np.asarray(a), np.asarray(b)
     return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))

@@ -11,7 +11,10 @@ Two kinds of fixture are written:
   blob width, 60 targets, V_stokeslet, V_image; 441 wall points with
   V_wall_total) and ``tests/legacy/data/towers.mat`` (441-point glycocalyx
   towers: positions, prescribed velocities, legacy GMRES forces, residual).
-  These pin ``tests/legacy/test_phase1_port.py:33-74``.
+  These pin ``tests/legacy/test_phase1_port.py:33-74``.  ``legacy_grid.npz`` is
+  ``legacy/sdc_cuda3/velocity_t_xyz_final.raw``, the 32^3 velocity grid the 2010
+  CUDA code wrote for the towers (float32, x fastest; background shear 0.1 z
+  included), pinning ``tests/legacy/test_phase1_port.py:77-87``.
 * ``reference_cases.npz`` -- outputs of the reference package ``fluidlets``
   (``src/fluidlets``) computed here.  Numba is not installed, so the reference
   is imported through a stand-in ``numba`` module whose ``njit`` returns the
@@ -62,6 +65,14 @@ def convert_legacy(ref: Path):
     np.savez_compressed(OUT / "legacy_sphere_drag.npz",
                         **{k: np.asarray(s[k], dtype=np.float64) for k in
                            ["F_free", "F_free_N", "F_par", "F_perp", "F_stokes", "H_list", "N_list", "h_list"]})
+
+
+def convert_legacy_grid(ref: Path):
+    raw = np.fromfile(ref / "legacy/sdc_cuda3/velocity_t_xyz_final.raw", "<f4").reshape(-1, 3)
+    # grid axes, blob width and shear rate of tests/legacy/test_phase1_port.py:16-18, 77-87
+    np.savez_compressed(OUT / "legacy_grid.npz", velocity=raw, x_axis=np.array([-1.0, 8.0, 32]),
+                        y_axis=np.array([-5.0, 25.0, 32]), z_axis=np.array([0.0, 20.0, 32]),
+                        delta=np.float64(0.5), shear=np.float64(0.1))
 
 
 def reference_cases(ref: Path):
@@ -159,6 +170,7 @@ def reference_cases(ref: Path):
 if __name__ == "__main__":
     ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
     convert_legacy(ref)
+    convert_legacy_grid(ref)
     reference_cases(ref)
     for p in sorted(OUT.glob("*.npz")):
         print(p.name, p.stat().st_size)

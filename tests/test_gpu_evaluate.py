@@ -3,7 +3,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from conftest import assert_close, rel_err
+from conftest import assert_close, legacy_grid_points, rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -155,3 +155,54 @@ def test_config2_density_mixed_accuracy_sample():
     assert np.abs(um[~interior]).max() < 1e-12
     u64 = fl.evaluate(fl.WallStokeslet3D(), T[idx], S, F, eps)
     assert_close(u64, ref, rtol=1e-11, atol_rel=1e-13)
+
+
+# ---- structured grids: the 32^3 legacy grid (tests/legacy/test_phase1_port.py:77-87) ----
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_grid_reproduces_2010_velocity_grid(legacy_towers, legacy_grid, precision):
+    t, g = legacy_towers, legacy_grid
+    axes, grid = legacy_grid_points(g)
+    V = fl.evaluate_grid(fl.WallStokeslet3D(), axes, t["x0"], t["Forces"], float(g["delta"]), precision=precision)
+    V[:, 0] += float(g["shear"]) * grid[:, 2]
+    stored = g["velocity"].astype(np.float64)
+    assert np.linalg.norm(V - stored) / np.linalg.norm(stored) < 1e-6  # float32 CUDA output
+
+
+def test_grid_equals_evaluate_on_meshgrid(legacy_towers, legacy_grid):
+    import torch
+
+    t, g = legacy_towers, legacy_grid
+    axes, grid = legacy_grid_points(g)
+    W = fl.WallStokeslet3D()
+    a = fl.evaluate_grid(W, axes, t["x0"], t["Forces"], 0.5)
+    b = fl.evaluate(W, grid, t["x0"], t["Forces"], 0.5)
+    assert np.array_equal(a, b)
+    f = fl.evaluate_grid(W, axes, t["x0"], t["Forces"], 0.5, field=True)
+    assert f.shape == (32, 32, 32, 3) and np.array_equal(f.reshape(-1, 3), a)
+    # ragged axes, torch in -> torch out
+    ax = (np.linspace(0, 1, 5), np.linspace(-1, 1, 3), np.array([0.5]))
+    src = torch.tensor(t["x0"][:50], device="cuda")
+    u = fl.evaluate_grid(W, ax, src, torch.tensor(t["Forces"][:50], device="cuda"), 0.5, field=True)
+    assert isinstance(u, torch.Tensor) and tuple(u.shape) == (1, 3, 5, 3)
+    Z, Y, X = np.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
+    ref = O.evaluate("wall", np.c_[X.ravel(), Y.ravel(), Z.ravel()], t["x0"][:50], t["Forces"][:50], 0.5)
+    assert_close(u.reshape(-1, 3).cpu().numpy(), ref, 1e-12)
+
+
+# ---- nearest-neighbour map (core/assemble.py:61-65) --------------------------------
+def test_nearest_neighbors_match_kdtree():
+    from scipy.spatial import cKDTree
+
+    from fluidlets_gb300.geometry import biflagellate_shape
+
+    rng = np.random.default_rng(7)
+    for Q, N in [(1, 1), (5000, 700), (3001, 2500)]:
+        quad, force = rng.normal(size=(Q, 3)), rng.normal(size=(N, 3))
+        got = fl.nearest_neighbors(quad, force)
+        assert got.dtype == np.int64 and got.shape == (Q,)
+        assert np.array_equal(got, cKDTree(force).query(quad)[1])
+    s = biflagellate_shape(0.3)
+    assert np.array_equal(fl.nearest_neighbors(s.X, s.x), cKDTree(s.x).query(s.X)[1])
+    assert fl.nearest_neighbors(np.zeros((0, 3)), force).shape == (0,)
+    with pytest.raises(ValueError):
+        fl.nearest_neighbors(quad, np.zeros((0, 3)))

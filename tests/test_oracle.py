@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from conftest import assert_close, rel_err
+from conftest import assert_close, legacy_grid_points, rel_err
 
 
 def test_stokeslet_matches_legacy_StokesletEval(legacy_kernels):
@@ -31,6 +31,18 @@ def test_tower_operator_residual_equals_legacy(legacy_towers):
     d = legacy_towers
     r = np.linalg.norm(O.evaluate("wall", d["x0"], d["x0"], d["Forces"], 0.5) - d["Vel"]) / np.linalg.norm(d["Vel"])
     assert abs(r - float(d["resid"])) < 1e-12
+
+
+def test_oracle_reproduces_2010_velocity_grid(legacy_towers, legacy_grid):
+    # tests/legacy/test_phase1_port.py:77-87 on every 16th point of the 32^3 grid (the full grid
+    # runs on the GPU): tower forces from the legacy GMRES, plus the background shear 0.1 z
+    t, g = legacy_towers, legacy_grid
+    _, grid = legacy_grid_points(g)
+    sel = np.arange(0, len(grid), 16)
+    V = O.evaluate("wall", grid[sel], t["x0"], t["Forces"], float(g["delta"]))
+    V[:, 0] += float(g["shear"]) * grid[sel, 2]
+    stored = g["velocity"][sel].astype(np.float64)
+    assert np.linalg.norm(V - stored) / np.linalg.norm(stored) < 1e-6  # float32 CUDA output
 
 
 @pytest.mark.parametrize("name,kind,alpha", [("stokeslet", "stokeslet", 0.0), ("wall", "wall", 0.0),
