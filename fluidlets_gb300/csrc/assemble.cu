@@ -244,6 +244,7 @@ struct SwimArgs {
     const double *x;
     int64_t N;
     double x0[3];
+    const double *x0_dev;  // when set, the origin is read from device memory (graph replays)
     const double *X;
     const int64_t *nearest;
     int64_t Q;
@@ -263,7 +264,9 @@ __global__ void swimmer_kernel(SwimArgs s) {
     const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t n3 = 3 * s.N;
     if (m < s.N) {
-        const double r0 = s.x[3 * m] - s.x0[0], r1 = s.x[3 * m + 1] - s.x0[1], r2 = s.x[3 * m + 2] - s.x0[2];
+        const double o0 = s.x0_dev ? s.x0_dev[0] : s.x0[0], o1 = s.x0_dev ? s.x0_dev[1] : s.x0[1],
+                     o2 = s.x0_dev ? s.x0_dev[2] : s.x0[2];
+        const double r0 = s.x[3 * m] - o0, r1 = s.x[3 * m + 1] - o1, r2 = s.x[3 * m + 2] - o2;
         // cross matrix C(v): C @ w = v x w  (swimming.py:33-40)
         const double C[9] = {0.0, -r2, r1, r2, 0.0, -r0, -r1, r0, 0.0};
         for (int a = 0; a < 3; a++)
@@ -547,10 +550,13 @@ extern "C" size_t flg_assemble_nearest_workspace(int64_t Q, int64_t n_force) {
     return c.bytes();
 }
 
-extern "C" int flg_assemble_nearest(int kind, double alpha_re, double alpha_im, const double *targets, int64_t M,
-                                    const double *quad, const int64_t *nearest, const double *eps, int64_t Q,
-                                    int64_t n_force, double mu_re, double mu_im, void *out, int out_type, int64_t ld,
-                                    void *work, size_t work_bytes, void *stream) {
+// bad_flag: null -> check the indices and synchronize (flg_assemble_nearest); else the
+// device int receives 1 if an index lies outside [0, n_force) and nothing waits
+// (out-of-range indices are skipped by every kernel, so the launch sequence is safe)
+static int assemble_nearest_impl(int kind, double alpha_re, double alpha_im, const double *targets, int64_t M,
+                                 const double *quad, const int64_t *nearest, const double *eps, int64_t Q,
+                                 int64_t n_force, double mu_re, double mu_im, void *out, int out_type, int64_t ld,
+                                 void *work, size_t work_bytes, void *stream, int *bad_flag) {
     AsmArgs a{};
     FLG_TRY(prepare(kind, alpha_re, alpha_im, mu_re, mu_im, out_type, a));
     FLG_REQUIRE(out_type != FLG_BF16, "assemble_nearest writes FLG_F64, FLG_C128 or FLG_F32");
@@ -565,6 +571,7 @@ extern "C" int flg_assemble_nearest(int kind, double alpha_re, double alpha_im, 
     int *idx = ar.take<int>(Q + 1);
     int *bad = ar.take<int>(1);
     FLG_REQUIRE(counts && off && idx && bad, "workspace too small (%zu bytes)", work_bytes);
+    if (bad_flag) bad = bad_flag;
     cudaStream_t st = as_stream(stream);
     FLG_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * (n_force + 1), st));
     FLG_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), st));
@@ -593,11 +600,30 @@ extern "C" int flg_assemble_nearest(int kind, double alpha_re, double alpha_im, 
     dispatch<LaunchNearest>(kind, kind == FLG_BRINKMANLET && alpha_im != 0.0, asm_grid(M, n_force), 128, st, na);
     FLG_LAUNCH_CHECK();
     prof_end(FLG_SLOT_ASSEMBLE, st);
+    if (bad_flag) return FLG_OK;
     int hbad = 0;
     FLG_CUDA(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
     FLG_CUDA(cudaStreamSynchronize(st));
     FLG_REQUIRE(hbad == 0, "nearest indices must lie in [0, n_force)");
     return FLG_OK;
+}
+
+extern "C" int flg_assemble_nearest(int kind, double alpha_re, double alpha_im, const double *targets, int64_t M,
+                                    const double *quad, const int64_t *nearest, const double *eps, int64_t Q,
+                                    int64_t n_force, double mu_re, double mu_im, void *out, int out_type, int64_t ld,
+                                    void *work, size_t work_bytes, void *stream) {
+    return assemble_nearest_impl(kind, alpha_re, alpha_im, targets, M, quad, nearest, eps, Q, n_force, mu_re, mu_im,
+                                 out, out_type, ld, work, work_bytes, stream, nullptr);
+}
+
+extern "C" int flg_assemble_nearest_async(int kind, double alpha_re, double alpha_im, const double *targets,
+                                          int64_t M, const double *quad, const int64_t *nearest, const double *eps,
+                                          int64_t Q, int64_t n_force, double mu_re, double mu_im, void *out,
+                                          int out_type, int64_t ld, int *bad_flag, void *work, size_t work_bytes,
+                                          void *stream) {
+    FLG_REQUIRE(bad_flag, "null flag");
+    return assemble_nearest_impl(kind, alpha_re, alpha_im, targets, M, quad, nearest, eps, Q, n_force, mu_re, mu_im,
+                                 out, out_type, ld, work, work_bytes, stream, bad_flag);
 }
 
 extern "C" int flg_swimmer_constraints(const double *x, int64_t N, const double *x0_host, const double *X,
@@ -607,7 +633,21 @@ extern "C" int flg_swimmer_constraints(const double *x, int64_t N, const double 
     FLG_REQUIRE(out_type == FLG_F64 || out_type == FLG_F32, "swimmer system is FLG_F64 or FLG_F32");
     FLG_REQUIRE(ld >= 3 * N + 6, "ld < 3N + 6");
     FLG_REQUIRE(x0_host && A && (N == 0 || x) && (Q == 0 || (X && nearest)), "null pointer");
-    SwimArgs s{x, N, {x0_host[0], x0_host[1], x0_host[2]}, X, nearest, Q, A, out_type, ld};
+    SwimArgs s{x, N, {x0_host[0], x0_host[1], x0_host[2]}, nullptr, X, nearest, Q, A, out_type, ld};
+    const int64_t threads = std::max<int64_t>(N, 36);
+    swimmer_kernel<<<(unsigned)ceil_div(threads, 128), 128, 0, as_stream(stream)>>>(s);
+    FLG_LAUNCH_CHECK();
+    return FLG_OK;
+}
+
+extern "C" int flg_swimmer_constraints_dev(const double *x, int64_t N, const double *x0_dev, const double *X,
+                                           const int64_t *nearest, int64_t Q, void *A, int out_type, int64_t ld,
+                                           void *stream) {
+    FLG_REQUIRE(N >= 0 && Q >= 0, "negative sizes");
+    FLG_REQUIRE(out_type == FLG_F64 || out_type == FLG_F32, "swimmer system is FLG_F64 or FLG_F32");
+    FLG_REQUIRE(ld >= 3 * N + 6, "ld < 3N + 6");
+    FLG_REQUIRE(x0_dev && A && (N == 0 || x) && (Q == 0 || (X && nearest)), "null pointer");
+    SwimArgs s{x, N, {0.0, 0.0, 0.0}, x0_dev, X, nearest, Q, A, out_type, ld};
     const int64_t threads = std::max<int64_t>(N, 36);
     swimmer_kernel<<<(unsigned)ceil_div(threads, 128), 128, 0, as_stream(stream)>>>(s);
     FLG_LAUNCH_CHECK();

@@ -1,35 +1,35 @@
-// graph.cu -- captured CUDA graphs of the bucket factorization (solve server).
+// graph.cu -- captured CUDA graphs of the mixed-precision factorizations.
 //
 // flg_bucket_graph_create captures, on the caller's stream and in thread-local
 // capture mode (other host threads keep launching and allocating freely),
 //   flg_assemble_bucket -> flg_convert_f64_f32 (x2: the factors' copy and the
 //   inner-matvec copy A32) -> flg_lu_factor_lowp_async
-// over fixed buffers, and instantiates it.  Replaying it with
+// over fixed buffers, and instantiates it (solve server).  Replaying it with
 // flg_graph_launch refactors whatever points are in the buffers; the real
 // point count is read from device memory by the assembly kernel, so one graph
 // serves every problem size of its bucket.
+//
+// flg_swimmer_graph_create does the same for the free-swimmer system of one
+// shape size (force and quadrature point counts), for the stages of swim():
+//   flg_nearest_neighbors -> flg_assemble_nearest_async ->
+//   flg_swimmer_constraints_dev -> FP32 copies -> flg_lu_factor_lowp_async.
+#include <algorithm>
+
 #include "flg_common.cuh"
 
-extern "C" int flg_bucket_graph_create(int kind, double alpha_re, double alpha_im, const double *points,
-                                       const double *eps, const int64_t *n_real, int64_t n_cap, double mu_re,
-                                       double *K, float *A32, float *K32, int64_t ld32, int mode, float *dinv,
-                                       int *flags, void *work, size_t work_bytes, void *stream, void **graph_exec) {
+// One eager pass of `seq` (sets kernel attributes and any lazily initialized
+// state outside the capture), then capture it on `stream` in thread-local mode
+// and instantiate.
+template <class F>
+static int capture_graph(void *stream, F &&seq, void **graph_exec) {
     FLG_REQUIRE(graph_exec, "null graph handle");
     FLG_REQUIRE(stream, "graph capture needs a non-default stream");
     *graph_exec = nullptr;
     cudaStream_t st = flg::as_stream(stream);
-    const int64_t n = 3 * n_cap;
-    // one eager pass: sets kernel attributes and any lazily initialized state outside the capture
-    FLG_TRY(flg_assemble_bucket(kind, alpha_re, alpha_im, points, eps, n_real, n_cap, mu_re, K, FLG_F64, n, stream));
-    FLG_TRY(flg_convert_f64_f32(n, n, K, n, K32, ld32, stream));
-    if (A32) FLG_TRY(flg_convert_f64_f32(n, n, K, n, A32, ld32, stream));
-    FLG_TRY(flg_lu_factor_lowp_async(n, K32, ld32, mode, dinv, flags, work, work_bytes, stream));
+    FLG_TRY(seq());
     FLG_CUDA(cudaStreamSynchronize(st));
     FLG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    int s = flg_assemble_bucket(kind, alpha_re, alpha_im, points, eps, n_real, n_cap, mu_re, K, FLG_F64, n, stream);
-    if (s == FLG_OK) s = flg_convert_f64_f32(n, n, K, n, K32, ld32, stream);
-    if (s == FLG_OK && A32) s = flg_convert_f64_f32(n, n, K, n, A32, ld32, stream);
-    if (s == FLG_OK) s = flg_lu_factor_lowp_async(n, K32, ld32, mode, dinv, flags, work, work_bytes, stream);
+    int s = seq();
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(st, &g);
     if (s != FLG_OK || e != cudaSuccess || g == nullptr) {
@@ -47,6 +47,46 @@ extern "C" int flg_bucket_graph_create(int kind, double alpha_re, double alpha_i
     }
     *graph_exec = (void *)ge;
     return FLG_OK;
+}
+
+extern "C" int flg_bucket_graph_create(int kind, double alpha_re, double alpha_im, const double *points,
+                                       const double *eps, const int64_t *n_real, int64_t n_cap, double mu_re,
+                                       double *K, float *A32, float *K32, int64_t ld32, int mode, float *dinv,
+                                       int *flags, void *work, size_t work_bytes, void *stream, void **graph_exec) {
+    const int64_t n = 3 * n_cap;
+    auto seq = [&]() -> int {
+        FLG_TRY(flg_assemble_bucket(kind, alpha_re, alpha_im, points, eps, n_real, n_cap, mu_re, K, FLG_F64, n,
+                                    stream));
+        FLG_TRY(flg_convert_f64_f32(n, n, K, n, K32, ld32, stream));
+        if (A32) FLG_TRY(flg_convert_f64_f32(n, n, K, n, A32, ld32, stream));
+        return flg_lu_factor_lowp_async(n, K32, ld32, mode, dinv, flags, work, work_bytes, stream);
+    };
+    return capture_graph(stream, seq, graph_exec);
+}
+
+extern "C" size_t flg_swimmer_graph_workspace(int64_t N, int64_t Q, int mode) {
+    return std::max(flg_assemble_nearest_workspace(Q, N), flg_lu_factor_lowp_workspace(3 * N + 6, mode));
+}
+
+extern "C" int flg_swimmer_graph_create(int kind, double alpha_re, double alpha_im, const double *x, int64_t N,
+                                        const double *x0, const double *X, const double *eps, int64_t Q,
+                                        int64_t *nearest, int recompute_nearest, double mu_re, double *A, float *A32,
+                                        float *K32, int64_t ld32, int mode, float *dinv, int *flags, void *work,
+                                        size_t work_bytes, void *stream, void **graph_exec) {
+    FLG_REQUIRE(N > 0 && Q >= 0 && flags && A && K32 && dinv, "bad swimmer graph arguments");
+    const int64_t n = 3 * N + 6;
+    FLG_REQUIRE(work_bytes >= flg_swimmer_graph_workspace(N, Q, mode), "workspace too small for the swimmer graph");
+    auto seq = [&]() -> int {
+        if (recompute_nearest) FLG_TRY(flg_nearest_neighbors(X, Q, x, N, nearest, stream));
+        FLG_TRY(flg_assemble_nearest_async(kind, alpha_re, alpha_im, x, N, X, nearest, eps, Q, N, mu_re, 0.0, A,
+                                           FLG_F64, n, flags + 2, work, work_bytes, stream));
+        FLG_TRY(flg_swimmer_constraints_dev(x, N, x0, X, nearest, Q, A, FLG_F64, n, stream));
+        FLG_TRY(flg_convert_f64_f32(n, n, A, n, K32, ld32, stream));
+        if (A32) FLG_TRY(flg_convert_f64_f32(n, n, A, n, A32, ld32, stream));
+        // the workspace is reused by the LU: the assembly is done with it by then (stream order)
+        return flg_lu_factor_lowp_async(n, K32, ld32, mode, dinv, flags, work, work_bytes, stream);
+    };
+    return capture_graph(stream, seq, graph_exec);
 }
 
 extern "C" int flg_graph_launch(void *graph_exec, void *stream) {

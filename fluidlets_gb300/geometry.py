@@ -78,6 +78,9 @@ def biflagellate_shape(t: float, n_body: int = 96, fine: int = 4, segments: int 
     attached at the front (x = 0.6, z = +-0.1), pointing along +x and beating in the x-z plane as
     travelling sine waves z = +-(0.1 + A sin(k s - w t) s/L) of amplitude A = 0.2 and wavelength 1;
     force points at the segment ends, `fine` quadrature points per segment.  Returns a SwimmerShape.
+    With amplitude >= 0.1 the two mirror-image flagella cross during the beat (the system is
+    near-singular at those instants): fine for instantaneous solves, but integrate a trajectory
+    with amplitude < 0.1.
     """
     from .swimming import SwimmerShape
 

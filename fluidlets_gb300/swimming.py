@@ -22,9 +22,9 @@ import numpy as np
 import torch
 
 from . import _device as dv
-from ._lib import F64, check, load
+from ._lib import F64, LU_MODE, check, load
 from .core import _assemble_nearest_dev, _gmres_ir_dense_dev, _lowp_factor_dev, _lu_solve_dev, _prec, nearest_neighbors
-from .kernels import Stokeslet3D
+from .kernels import Stokeslet3D, kernel_params
 
 
 @dataclass
@@ -90,6 +90,85 @@ def swimming_problem(shape: SwimmerShape, x0, B, eps, mu=1.0, kernel=None, neare
     return SwimState(sol[3 * N:3 * N + 3], sol[3 * N + 3:], sol[:3 * N].reshape(N, 3), x, X, nearest)
 
 
+class SwimmerPlan:
+    """Device buffers and a captured CUDA graph of the mixed-precision swimmer system for one
+    shape size (N force points, Q quadrature points): nearest map -> nearest-neighbour
+    assembly -> constraint rows -> FP32 copies -> tensor-core LU (``flg_swimmer_graph_create``).
+    Each ``solve`` writes the stage's points into the buffers, replays the graph and refines
+    with FP64 GMRES-IR; ``swim(..., precision="mixed")`` keeps one plan for all stages."""
+
+    def __init__(self, kernel, N, Q, eps, mu=1.0, lu="tf32", nearest=None):
+        L = load()
+        dev = dv.require_cuda()
+        if complex(mu).imag != 0.0:
+            raise ValueError("swimming needs a real viscosity")
+        self.N, self.Q, self.n = N, Q, 3 * N + 6
+        n = self.n
+        self.stream = torch.cuda.Stream(device=dev)
+        f64 = dict(dtype=torch.float64, device=dev)
+        self.x = torch.zeros((N, 3), **f64)
+        self.X = torch.zeros((Q, 3), **f64)
+        self.x0 = torch.zeros(3, **f64)
+        self.e = torch.from_numpy(np.broadcast_to(np.asarray(eps, float), (Q,)).copy()).to(dev)
+        self.fixed = nearest is not None
+        self.nn = (torch.from_numpy(np.asarray(nearest, np.int64)).to(dev) if self.fixed
+                   else torch.zeros(Q, dtype=torch.int64, device=dev))
+        self.A = torch.empty((n, n), **f64)
+        self.ld32 = (n + 31) // 32 * 32
+        self.K32 = torch.empty((n, self.ld32), dtype=torch.float32, device=dev)
+        self.A32 = torch.empty((n, self.ld32), dtype=torch.float32, device=dev)
+        self.dinv = torch.empty(L.flg_lu_lowp_dinv_elems(n), dtype=torch.float32, device=dev)
+        self.flags = torch.zeros(3, dtype=torch.int32, device=dev)
+        mode = LU_MODE[lu]
+        wb = L.flg_swimmer_graph_workspace(N, Q, mode)
+        self.ws = dv.workspace(wb)
+        kind, are, aim = kernel_params(kernel)
+        self.graph = ctypes.c_void_p(0)
+        st = ctypes.c_void_p(self.stream.cuda_stream)
+        with torch.cuda.stream(self.stream):
+            check(L.flg_swimmer_graph_create(kind, are, aim, dv.ptr(self.x), N, dv.ptr(self.x0), dv.ptr(self.X),
+                                             dv.ptr(self.e), Q, dv.ptr(self.nn), 0 if self.fixed else 1,
+                                             float(complex(mu).real), dv.ptr(self.A), dv.ptr(self.A32),
+                                             dv.ptr(self.K32), self.ld32, mode, dv.ptr(self.dinv), dv.ptr(self.flags),
+                                             dv.ptr(self.ws), wb, st, ctypes.byref(self.graph)), "swimmer graph")
+        self.stream.synchronize()
+
+    def solve(self, x, X, x0, rhs, rtol=1e-10):
+        """(U, Omega, forces, nearest) for world-frame force points x, quadrature points X,
+        origin x0 and right-hand side rhs (3N + 6)."""
+        L = load()
+        with torch.cuda.stream(self.stream):
+            self.x.copy_(torch.from_numpy(np.ascontiguousarray(x, float)))
+            self.X.copy_(torch.from_numpy(np.ascontiguousarray(X, float)))
+            self.x0.copy_(torch.from_numpy(np.asarray(x0, float)))
+            b = torch.from_numpy(np.ascontiguousarray(rhs, float)).to(self.x.device)
+            check(L.flg_graph_launch(self.graph, ctypes.c_void_p(self.stream.cuda_stream)), "swimmer graph replay")
+            fl = self.flags.cpu()
+            if int(fl[2]):
+                raise ValueError("nearest indices must lie in [0, n_force)")
+            if int(fl[1]):
+                raise RuntimeError("tensor-core update: an mbarrier wait timed out")
+            if int(fl[0]):
+                raise np.linalg.LinAlgError(f"zero or non-finite pivot at row {int(fl[0]) - 1} in the low-precision LU")
+            sol, *_ = _gmres_ir_dense_dev(self.A, self.K32, self.ld32, self.dinv, b, rtol * 1e-2, 60, 200,
+                                          required=rtol, A32=self.A32)
+            sol = dv.to_host(sol)
+            nn = self.nn.cpu().numpy()
+        N = self.N
+        return sol[3 * N:3 * N + 3], sol[3 * N + 3:], sol[:3 * N].reshape(N, 3), nn
+
+    def close(self):
+        if self.graph:
+            load().flg_graph_destroy(self.graph)
+            self.graph = ctypes.c_void_p(0)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 @dataclass
 class Trajectory:
     t: np.ndarray
@@ -100,7 +179,8 @@ class Trajectory:
 def swim(shape_at: Callable[[float], SwimmerShape], t_span, eps, mu=1.0, x0=(0, 0, 0), B0=None, kernel=None,
          t_eval=None, rtol=1e-6, atol=1e-9, fixed_nearest=False, *, precision="fp64") -> Trajectory:
     """Integrate a free swimmer's position and orientation (``swimming.py:112-148``): RK45
-    (SciPy ``solve_ivp``) over instantaneous solves on the device."""
+    (SciPy ``solve_ivp``, as the reference) over instantaneous solves on the device; with
+    ``precision="mixed"`` every stage replays one captured system graph (SwimmerPlan)."""
     from scipy.integrate import solve_ivp
 
     B0 = np.eye(3) if B0 is None else np.asarray(B0, float)
@@ -108,12 +188,28 @@ def swim(shape_at: Callable[[float], SwimmerShape], t_span, eps, mu=1.0, x0=(0, 
     if fixed_nearest:
         s0 = shape_at(t_span[0])
         nearest = nearest_neighbors(s0.X, s0.x)
+    mixed = _prec(precision) == 1
+    plans = {}  # (N, Q) -> SwimmerPlan: one captured system graph reused by every stage
 
     def rhs(t, z):
         b1, b2 = z[3:6], z[6:9]
         Bm = np.c_[b1, b2, np.cross(b1, b2)]
-        st = swimming_problem(shape_at(t), z[:3], Bm, eps, mu, kernel, nearest, precision=precision)
-        return np.concatenate([st.U, np.cross(st.Omega, b1), np.cross(st.Omega, b2)])
+        shape = shape_at(t)
+        if not mixed:
+            st = swimming_problem(shape, z[:3], Bm, eps, mu, kernel, nearest, precision=precision)
+            U, Om = st.U, st.Omega
+        else:
+            key = (len(shape.x), len(shape.X))
+            if key not in plans:
+                plans[key] = SwimmerPlan(Stokeslet3D() if kernel is None else kernel, key[0], key[1], eps, mu,
+                                         nearest=nearest)
+            x0 = z[:3]
+            xw = x0 + np.asarray(shape.x, float) @ Bm.T
+            Xw = x0 + np.asarray(shape.X, float) @ Bm.T
+            r = np.zeros(3 * key[0] + 6)
+            r[:3 * key[0]] = (np.asarray(shape.v, float) @ Bm.T).ravel()
+            U, Om, _, _ = plans[key].solve(xw, Xw, x0, r)
+        return np.concatenate([U, np.cross(Om, b1), np.cross(Om, b2)])
 
     z0 = np.concatenate([np.asarray(x0, float), B0[:, 0], B0[:, 1]])
     sol = solve_ivp(rhs, t_span, z0, t_eval=t_eval, rtol=rtol, atol=atol)

@@ -148,6 +148,13 @@ int flg_assemble_nearest(int kind, double alpha_re, double alpha_im,
                          int64_t n_force, double mu_re, double mu_im,
                          void *out, int out_type, int64_t ld,
                          void *work, size_t work_bytes, void *stream);
+/* The same without a host synchronization (CUDA-graph capturable): *bad_flag
+ * (device int, zeroed here) becomes 1 if a nearest index lies outside
+ * [0, n_force); such indices are skipped.  No counterpart in the reference. */
+int flg_assemble_nearest_async(int kind, double alpha_re, double alpha_im, const double *targets, int64_t M,
+                               const double *quad, const int64_t *nearest, const double *eps, int64_t Q,
+                               int64_t n_force, double mu_re, double mu_im, void *out, int out_type, int64_t ld,
+                               int *bad_flag, void *work, size_t work_bytes, void *stream);
 
 /* ---- free-swimmer system (swimming.py:66-102) ----------------------------
  * Fills the (3N+6) x (3N+6) system of Gallagher & Smith (2018) Eq. 8 around an
@@ -159,6 +166,10 @@ int flg_assemble_nearest(int kind, double alpha_re, double alpha_im,
 int flg_swimmer_constraints(const double *x, int64_t N, const double *x0_host,
                             const double *X, const int64_t *nearest, int64_t Q,
                             void *A, int out_type, int64_t ld, void *stream);
+/* The same with the origin x0 read from device memory (x0_dev, 3 doubles), so
+ * that a captured graph picks up a new origin on every replay. */
+int flg_swimmer_constraints_dev(const double *x, int64_t N, const double *x0_dev, const double *X,
+                                const int64_t *nearest, int64_t Q, void *A, int out_type, int64_t ld, void *stream);
 
 /* ---- dense LU ------------------------------------------------------------
  * Replaces the LU branch of fluidlets.resistance (core/solve.py:64-67,
@@ -264,6 +275,20 @@ int flg_bucket_graph_create(int kind, double alpha_re, double alpha_im, const do
                             const int64_t *n_real, int64_t n_cap, double mu_re, double *K, float *A32, float *K32,
                             int64_t ld32, int mode, float *dinv, int *flags, void *work, size_t work_bytes,
                             void *stream, void **graph_exec);
+/* Captured graph of the free-swimmer system (swimming.py:66-102) for N force
+ * points and Q quadrature points, over fixed device buffers: x (N x 3), x0 (3),
+ * X (Q x 3), eps (Q), nearest (Q; recomputed from x and X on every replay when
+ * recompute_nearest != 0) -> A ((3N+6)^2 FP64, ld 3N+6) -> FP32 copies A32
+ * (optional) and K32 (ld32) -> tensor-core LU of K32 with dinv.  flags[0..1]
+ * as flg_lu_factor_lowp_async, flags[2] = 1 on an invalid nearest index.
+ * Workspace: flg_swimmer_graph_workspace(N, Q, mode).  Each stage of swim()
+ * writes its points into the buffers and replays the graph. */
+size_t flg_swimmer_graph_workspace(int64_t N, int64_t Q, int mode);
+int flg_swimmer_graph_create(int kind, double alpha_re, double alpha_im, const double *x, int64_t N,
+                             const double *x0, const double *X, const double *eps, int64_t Q, int64_t *nearest,
+                             int recompute_nearest, double mu_re, double *A, float *A32, float *K32, int64_t ld32,
+                             int mode, float *dinv, int *flags, void *work, size_t work_bytes, void *stream,
+                             void **graph_exec);
 int flg_graph_launch(void *graph_exec, void *stream);
 int flg_graph_destroy(void *graph_exec);
 

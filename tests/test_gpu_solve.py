@@ -369,3 +369,42 @@ def test_trajectory_of_steady_slip_swimmer():
     assert np.allclose(tr.x0[-1], [0, 0, 1.0], atol=1e-7)
     angle = 0.25 * 2.0
     assert np.allclose(tr.B[-1][:, 0], [np.cos(angle), np.sin(angle), 0], atol=1e-7)
+
+
+def test_swimmer_plan_replays_match_direct_solves():
+    """One captured swimmer graph, replayed for several stages (new points, origin, orientation),
+    equals the FP64 swimming_problem of each stage."""
+    from fluidlets_gb300.geometry import biflagellate_shape
+    from fluidlets_gb300.swimming import SwimmerPlan
+
+    rng = np.random.default_rng(3)
+    s0 = biflagellate_shape(0.0)
+    plan = SwimmerPlan(fl.Stokeslet3D(), len(s0.x), len(s0.X), 0.02)
+    for t in (0.0, 0.37, 0.81):
+        s = biflagellate_shape(t)
+        x0 = rng.normal(size=3)
+        B = np.linalg.qr(rng.normal(size=(3, 3)))[0]
+        B *= np.sign(np.linalg.det(B))
+        ref = fl.swimming_problem(s, x0, B, 0.02)
+        xw, Xw = x0 + s.x @ B.T, x0 + s.X @ B.T
+        rhs = np.zeros(3 * len(s.x) + 6)
+        rhs[:3 * len(s.x)] = (s.v @ B.T).ravel()
+        U, Om, F, nn = plan.solve(xw, Xw, x0, rhs)
+        assert np.array_equal(nn, ref.nearest)
+        assert rel_err(U, ref.U) < 1e-9 and rel_err(Om, ref.Omega) < 1e-9 and rel_err(F, ref.forces) < 1e-9
+    plan.close()
+
+
+def test_trajectory_mixed_precision_swim():
+    # the steady slip swimmer of tests/test_swimming.py:58-69 through the captured-graph stages
+    V = np.array([0.0, 0.0, 0.5])
+    Wb = np.array([0.0, 0.0, 0.25])
+
+    def shape_at(t):
+        x = cube_sphere(3)
+        return fl.SwimmerShape(x=x, v=-(V + np.cross(Wb, x)), X=cube_sphere(6))
+
+    tr = fl.swim(shape_at, (0.0, 2.0), 0.05, t_eval=[2.0], rtol=1e-9, atol=1e-12, precision="mixed")
+    assert np.allclose(tr.x0[-1], [0, 0, 1.0], atol=1e-7)
+    angle = 0.25 * 2.0
+    assert np.allclose(tr.B[-1][:, 0], [np.cos(angle), np.sin(angle), 0], atol=1e-7)
