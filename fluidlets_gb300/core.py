@@ -242,7 +242,8 @@ class SolveInfo:
 
 
 def _lu_solve_dev(K: torch.Tensor, U: torch.Tensor) -> torch.Tensor:
-    """Dense FP64 LU with partial pivoting (getrf + getrs) on the device; K is overwritten."""
+    """Dense FP64 LU with partial pivoting (getrf + getrs) on the device; K is overwritten.
+    U holds one right-hand side (n values, returned flat) or several as the columns of (n, k)."""
     n = K.shape[0]
     L = load()
     if K.is_complex():
@@ -268,8 +269,9 @@ def _lu_solve_dev(K: torch.Tensor, U: torch.Tensor) -> torch.Tensor:
         B = torch.stack([U.real, U.imag], 1).contiguous()
         check(L.flg_lu_solve_f64(n, 2, dv.ptr(K), n, dv.ptr(piv), dv.ptr(B), 2, dv.stream()), "LU solve")
         return torch.complex(B[:, 0], B[:, 1])
-    check(L.flg_lu_solve_f64(n, 1, dv.ptr(K), n, dv.ptr(piv), dv.ptr(B), 1, dv.stream()), "LU solve")
-    return B.reshape(-1)
+    nrhs = B.shape[1]
+    check(L.flg_lu_solve_f64(n, nrhs, dv.ptr(K), n, dv.ptr(piv), dv.ptr(B), nrhs, dv.stream()), "LU solve")
+    return B.reshape(-1) if nrhs == 1 else B
 
 
 def _lowp_factor_dev(K: torch.Tensor, lu_mode: str):

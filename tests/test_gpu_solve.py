@@ -408,3 +408,61 @@ def test_trajectory_mixed_precision_swim():
     assert np.allclose(tr.x0[-1], [0, 0, 1.0], atol=1e-7)
     angle = 0.25 * 2.0
     assert np.allclose(tr.B[-1][:, 0], [np.cos(angle), np.sin(angle), 0], atol=1e-7)
+
+
+# ---- rigid bodies: mobility problem and grand resistance matrix ----------------------------
+def _oracle_mobility(X, eps, F, T, c, kind="stokeslet"):
+    # tutorials/03_mobility_resistance_swimming.ipynb (sedimenting sphere) with rotation and torque
+    N = len(X)
+    r = X - c
+    A = np.zeros((3 * N + 6, 3 * N + 6))
+    A[:3 * N, :3 * N] = O.assemble(kind, X, X, eps)
+    for k in range(N):
+        A[3 * k:3 * k + 3, 3 * N:3 * N + 3] = -np.eye(3)
+        A[3 * k:3 * k + 3, 3 * N + 3:] = O.cross_matrix(r[k])
+        A[3 * N:3 * N + 3, 3 * k:3 * k + 3] = np.eye(3)
+        A[3 * N + 3:, 3 * k:3 * k + 3] = O.cross_matrix(X[k])
+    rhs = np.r_[np.zeros(3 * N), F, T + np.cross(c, F)]
+    s = np.linalg.solve(A, rhs)
+    return s[3 * N:3 * N + 3], s[3 * N + 3:], s[:3 * N].reshape(N, 3)
+
+
+def test_settling_sphere_mobility():
+    X = cube_sphere(8)
+    F = -6 * np.pi * np.array([0.0, 0.0, 1.0])
+    U, Om, f = fl.rigid_body_mobility(fl.Stokeslet3D(), X, 0.05, F)
+    assert np.allclose(U, [0, 0, -1], atol=0.03) and np.abs(Om).max() < 1e-10
+    Ur, Omr, fr = _oracle_mobility(X, 0.05, F, np.zeros(3), X.mean(0))
+    assert rel_err(U, Ur) < 1e-10 and rel_err(f, fr) < 1e-9
+    Um, Omm, fm = fl.rigid_body_mobility(fl.Stokeslet3D(), X, 0.05, F, precision="mixed")
+    assert rel_err(Um, Ur) < 1e-9 and rel_err(fm, fr) < 1e-8
+
+
+def test_resistance_matrix_sphere_and_consistency():
+    X = cube_sphere(8)
+    R = fl.resistance_matrix(fl.Stokeslet3D(), X, 0.05)
+    assert np.abs(R - R.T).max() < 1e-9 * np.abs(R).max()           # Lorentz reciprocity
+    assert np.allclose(np.diag(R)[:3], 6 * np.pi, rtol=0.03)         # Stokes drag 6 pi mu a
+    assert np.allclose(np.diag(R)[3:], 8 * np.pi, rtol=0.05)         # rotation 8 pi mu a^3
+    assert np.abs(R[:3, 3:]).max() < 1e-9 * np.abs(R).max()
+    K = O.assemble("stokeslet", X, X, 0.05)
+    c = X.mean(0)
+    cols = []
+    for j in range(6):
+        u = np.zeros((len(X), 3))
+        if j < 3:
+            u[:, j] = 1.0
+        else:
+            u = np.cross(np.eye(3)[j - 3], X - c)
+        f = np.linalg.solve(K, u.ravel()).reshape(-1, 3)
+        cols.append(np.r_[f.sum(0), np.cross(X - c, f).sum(0)])
+    Ro = np.array(cols).T
+    assert rel_err(R, Ro) < 1e-10
+    assert rel_err(fl.resistance_matrix(fl.Stokeslet3D(), X, 0.05, precision="mixed"), Ro) < 1e-9
+    # an off-centre ellipsoid near a wall: the mobility solution satisfies R [U; Omega] = [F; T]
+    E = cube_sphere(6) * np.array([1.5, 1.0, 0.7]) + np.array([0.0, 0.0, 2.0])
+    W = fl.WallStokeslet3D()
+    F, T = np.array([0.3, -1.0, 0.5]), np.array([0.2, 0.1, -0.4])
+    U, Om, _ = fl.rigid_body_mobility(W, E, 0.05, F, T)
+    RE = fl.resistance_matrix(W, E, 0.05)
+    assert rel_err(RE @ np.r_[U, Om], np.r_[F, T]) < 1e-9
