@@ -69,6 +69,10 @@ SIGNATURES = {
                                          c_double, _P, _P, _P, c_int64, c_int, _P, _P, _P, c_size_t, _P,
                                          POINTER(c_void_p)]),
     "flg_grid_points": (c_int, [_P, c_int64, _P, c_int64, _P, c_int64, _P, _P]),
+    "flg_fibonacci_sphere": (c_int, [c_int64, c_double, POINTER(c_double), _P, _P]),
+    "flg_cube_sphere": (c_int, [c_int64, c_double, POINTER(c_double), _P, _P]),
+    "flg_mean_nn_spacing_workspace": (c_size_t, [c_int64]),
+    "flg_mean_nn_spacing": (c_int, [_P, c_int64, _P, _P, c_size_t, _P]),
     "flg_nearest_neighbors": (c_int, [_P, c_int64, _P, c_int64, _P, _P]),
     "flg_gemv_f64": (c_int, [c_int64, c_int64, _P, c_int64, _P, _P, _P]),
     "flg_gemv_f32": (c_int, [c_int64, c_int64, _P, c_int64, _P, _P, _P]),

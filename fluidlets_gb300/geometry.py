@@ -3,7 +3,8 @@
 ``fibonacci_sphere`` is the golden-angle spiral of the reference's
 ``geometry/spheres.py:7-13``; ``cube_sphere`` its six-patch sphere (33-52).
 ``spheroid`` and ``workload_*`` generate the synthetic, seeded inputs of the
-benchmark configurations.
+benchmark configurations.  The ``*_device`` functions build the same point sets
+(and the mean nearest-neighbour spacing) on the GPU, as CUDA tensors.
 """
 from __future__ import annotations
 
@@ -108,3 +109,45 @@ def biflagellate_shape(t: float, n_body: int = 96, fine: int = 4, segments: int 
         vs.append(v)
         Xs.append(pf)
     return SwimmerShape(x=np.vstack(xs), v=np.vstack(vs), X=np.vstack(Xs))
+
+
+# ---- the same on the device -------------------------------------------------------------
+def _sphere_device(fn, count, n, radius, center):
+    import ctypes
+
+    import torch
+
+    from . import _device as dv
+    from ._lib import check, load
+
+    out = torch.empty((count, 3), dtype=torch.float64, device=dv.require_cuda())
+    c = (ctypes.c_double * 3)(*np.asarray(center, float).reshape(3))
+    check(getattr(load(), fn)(n, float(radius), c, dv.ptr(out), dv.stream()), fn)
+    return out
+
+
+def fibonacci_sphere_device(n: int, radius: float = 1.0, center=(0.0, 0.0, 0.0)):
+    """fibonacci_sphere generated on the GPU (a CUDA tensor)."""
+    return _sphere_device("flg_fibonacci_sphere", n, n, radius, center)
+
+
+def cube_sphere_device(n: int, radius: float = 1.0, center=(0.0, 0.0, 0.0)):
+    """cube_sphere generated on the GPU (a CUDA tensor)."""
+    return _sphere_device("flg_cube_sphere", 6 * n * n, n, radius, center)
+
+
+def mean_nn_spacing_device(points) -> float:
+    """mean_nn_spacing on the GPU (exhaustive nearest-neighbour search)."""
+    import torch
+
+    from . import _device as dv
+    from ._lib import check, load
+
+    P = dv.to_dev(points, torch.float64).reshape(-1, 3)
+    L = load()
+    n = P.shape[0]
+    nb = L.flg_mean_nn_spacing_workspace(n)
+    ws = dv.workspace(nb)
+    m = torch.empty(1, dtype=torch.float64, device=P.device)
+    check(L.flg_mean_nn_spacing(dv.ptr(P), n, dv.ptr(m), dv.ptr(ws), nb, dv.stream()), "mean_nn_spacing")
+    return float(m.item())

@@ -297,6 +297,19 @@ int flg_graph_destroy(void *graph_exec);
  * core/assemble.py:61-65 (nearest_neighbors).  Exhaustive, O(Q N). */
 int flg_nearest_neighbors(const double *quad, int64_t Q, const double *force, int64_t N, int64_t *out, void *stream);
 
+/* ---- geometry on the device --------------------------------------------------
+ * The reference's sphere discretizations, same arithmetic in the same order:
+ * flg_fibonacci_sphere writes n points (geometry/spheres.py:7-13, golden-angle
+ * spiral), flg_cube_sphere 6 n^2 points (geometry/spheres.py:33-52, six-patch
+ * sphere); center is a host array of 3, out (device) is (points x 3) FP64.
+ * flg_mean_nn_spacing: the mean distance from each point to its nearest other
+ * point (*mean on the device; workspace flg_mean_nn_spacing_workspace(n)),
+ * which the workloads use to choose blob widths. */
+int flg_fibonacci_sphere(int64_t n, double radius, const double *center, double *out, void *stream);
+int flg_cube_sphere(int64_t n, double radius, const double *center, double *out, void *stream);
+size_t flg_mean_nn_spacing_workspace(int64_t n);
+int flg_mean_nn_spacing(const double *points, int64_t n, double *mean, void *work, size_t work_bytes, void *stream);
+
 /* ---- structured grids ----------------------------------------------------
  * points (nx ny nz x 3, FP64) of the grid x_axis x y_axis x z_axis (device
  * arrays), x fastest, then y, then z: the point order of the reference's

@@ -206,3 +206,19 @@ def test_nearest_neighbors_match_kdtree():
     assert fl.nearest_neighbors(np.zeros((0, 3)), force).shape == (0,)
     with pytest.raises(ValueError):
         fl.nearest_neighbors(quad, np.zeros((0, 3)))
+
+
+# ---- geometry on the device (geometry/spheres.py) --------------------------------------------
+def test_device_spheres_match_reference_formulas():
+    from fluidlets_gb300 import geometry as G
+
+    for n in (1, 3, 12, 40):
+        d = G.cube_sphere_device(n, 0.7, (0.1, -2.0, 3.0)).cpu().numpy()
+        assert np.array_equal(d, G.cube_sphere(n, 0.7, (0.1, -2.0, 3.0)))  # sqrt and division: exact
+    for n in (1, 2, 1536, 65536):
+        d = G.fibonacci_sphere_device(n, 2.0, (1.0, 0.0, -1.0)).cpu().numpy()
+        h = G.fibonacci_sphere(n, 2.0, (1.0, 0.0, -1.0))
+        assert np.abs(d - h).max() <= 8 * np.finfo(float).eps  # CUDA's acos/sin/cos vs the C library's
+    rng = np.random.default_rng(5)
+    for P in (G.fibonacci_sphere(2000), rng.uniform(-1, 1, (3001, 3)), G.cube_sphere(12)):
+        assert abs(G.mean_nn_spacing_device(P) - G.mean_nn_spacing(P)) <= 1e-13 * G.mean_nn_spacing(P)
