@@ -221,6 +221,21 @@ struct Gmres {
         return FLG_OK;
     }
 
+    // r = b - A x, or r = b without the operator when x is all zeros (the start of an
+    // iterative refinement; the FP64 kernel sum that would give A 0 costs a full matvec)
+    int residual_from(const T *b, const T *x) {
+        int nz = 0;
+        FLG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
+        any_nonzero_kernel<<<grid(n * (S<T>::complex ? 2 : 1)), 256, 0, st>>>((const double *)x,
+                                                                             n * (S<T>::complex ? 2 : 1), flag);
+        FLG_LAUNCH_CHECK();
+        FLG_CUDA(cudaMemcpyAsync(&nz, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+        FLG_CUDA(cudaStreamSynchronize(st));
+        if (nz) return residual(b, x);
+        FLG_CUDA(cudaMemcpyAsync(r, b, sizeof(T) * n, cudaMemcpyDeviceToDevice, st));
+        return FLG_OK;
+    }
+
     static void lartg(H f, H g, double &c, H &s, H &rr) {
         if constexpr (!S<T>::complex) {
             if (g == 0.0) {
@@ -505,7 +520,7 @@ static int gmres_run(int kind, double are, double aim, const double *X, const do
     double prev = INFINITY;
     int stall = 0;
     for (int o = 0; o <= max_outer; o++) {
-        FLG_TRY(g.residual(b, x));
+        FLG_TRY(o == 0 ? g.residual_from(b, x) : g.residual(b, x));
         FLG_TRY(g.norm(g.r, &rn));
         *resid = rn / bn;
         if (rn <= rtol * bn) return FLG_OK;
@@ -619,7 +634,7 @@ extern "C" int flg_gmres_ir_dense(int64_t n, const double *A, int64_t ld, const 
     double rn = 0.0, prev = INFINITY;
     int stall = 0;
     for (int o = 0; o <= 60; o++) {
-        FLG_TRY(g.residual(b, x));
+        FLG_TRY(o == 0 ? g.residual_from(b, x) : g.residual(b, x));
         FLG_TRY(g.norm(g.r, &rn));
         *resid = rn / bn;
         if (rn <= rtol * bn) return FLG_OK;
