@@ -515,7 +515,7 @@ __device__ __forceinline__ void warp_lu32(float *P, float *Xb, float *Yb, int la
 }
 
 __global__ void __launch_bounds__(512) diag_lowp_kernel(float *A, int64_t ld, int64_t k0, int nb, float *Linv,
-                                                        float *Uinv, int *info) {
+                                                        float *Uinv, float *UinvT, int *info) {
     extern __shared__ __align__(16) float sm[];
     float *D = sm, *X = sm + kNB * kLD, *Y = sm + 2 * kNB * kLD;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, nthr = blockDim.x, nwarp = nthr >> 5;
@@ -605,6 +605,8 @@ __global__ void __launch_bounds__(512) diag_lowp_kernel(float *A, int64_t ld, in
         *reinterpret_cast<float4 *>(Linv + r * kNB + c4) = *reinterpret_cast<const float4 *>(X + r * kLD + c4);
         *reinterpret_cast<float4 *>(Uinv + r * kNB + c4) = *reinterpret_cast<const float4 *>(Y + r * kLD + c4);
     }
+    if (UinvT)  // the transposed copy: the K-major operand of the tensor-core L panel
+        for (int e = tid; e < kNB * kNB; e += nthr) UinvT[e] = Y[(e & (kNB - 1)) * kLD + (e >> 7)];
 }
 
 // Panels of one LU step, in place, in one launch (CTA x < ntu: U tiles, else L tiles):
@@ -738,7 +740,8 @@ __global__ void transpose_f32_kernel(const float *src, int64_t lds, float *dst, 
 // tensor-core update (tc_gemm.cu): C (m x nc, ldc) -= Lp (m x K, ldl) * Ut^T (nc x K, ldu), K % 128 == 0
 size_t tc_update_bytes(int64_t m, int64_t nc, int64_t K, int mode);
 int tc_update(float *C, int64_t ldc, const float *Lp, int64_t ldl, const float *Ut, int64_t ldu, int64_t m,
-              int64_t nc, int64_t K, int mode, void *work, size_t work_bytes, cudaStream_t st, int *err_dev);
+              int64_t nc, int64_t K, int mode, void *work, size_t work_bytes, cudaStream_t st, int *err_dev,
+              bool store = false);
 
 static int sgemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, float alpha, const float *A, int64_t lda,
                  const float *B, int64_t ldb, float beta, float *C, int64_t ldc) {
@@ -1225,6 +1228,8 @@ extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mod
     size_t tcb;
     lowp_carve(ar, n, mode, &U12, &L21, &UtB, &tcw, &tcb);
     FLG_REQUIRE(U12 && L21 && UtB && (tcb == 0 || tcw), "workspace too small for LU (%zu bytes)", work_bytes);
+    // the tensor-core panels use the partial-block scratch: U12 for A12^T, L21 for Uinv^T
+    float *T12 = U12, *UinvT = L21;
     int *dinfo = flags;  // [0] first bad pivot, [1] tensor-core wait timed out
     const size_t dsmem = kDiagSmem;
     static bool attr_set = false;  // set once, so a later call can be captured in a graph
@@ -1241,7 +1246,9 @@ extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mod
             const int64_t k = k0 / kNB;
             const int nb = (int)std::min<int64_t>(kNB, n - k0);
             prof_begin(FLG_SLOT_LU_DIAG, st);
-            diag_lowp_kernel<<<1, 512, dsmem, st>>>(A, ld, k0, nb, Linv + k * kNB * kNB, Uinv + k * kNB * kNB, dinfo);
+            const bool tcp = tc && nb == kNB && n - (k0 + nb) > 0;  // tensor-core panels
+            diag_lowp_kernel<<<1, 512, dsmem, st>>>(A, ld, k0, nb, Linv + k * kNB * kNB, Uinv + k * kNB * kNB,
+                                                    tcp ? UinvT : nullptr, dinfo);
             FLG_LAUNCH_CHECK();
             prof_end(FLG_SLOT_LU_DIAG, st);
             const int64_t c0 = k0 + nb, nr = n - c0;
@@ -1250,7 +1257,22 @@ extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mod
             // (nb < kNB only for the last block, which has no trailing part)
             float *A12 = A + k0 * ld + c0, *A21 = A + c0 * ld + k0, *A22 = A + c0 * ld + c0;
             float *Ut = UtB + (c0 - K0) * kOuterW + (k0 - K0);  // row: column - K0; K offset: k0 - K0
-            if (nb == kNB) {
+            if (tcp) {
+                // panels on the tensor cores (TF32 in both tensor-core modes):
+                //   Ut = A12^T Linv^T (the K-major copy the updates read), then A12 = Ut^T;
+                //   L21 = A21 Uinv, in place (each tile's rows are read in full before they are stored)
+                const dim3 tb(32, 8);
+                transpose_f32_kernel<<<dim3((unsigned)ceil_div(nr, 32), kNB / 32), tb, 0, st>>>(A12, ld, T12, kNB,
+                                                                                                 kNB, nr);
+                FLG_LAUNCH_CHECK();
+                FLG_TRY(tc_update(Ut, kOuterW, T12, kNB, Linv + k * kNB * kNB, kNB, nr, kNB, kNB, FLG_LU_TF32, tcw,
+                                  tcb, st, dinfo + 1, true));
+                transpose_f32_kernel<<<dim3(kNB / 32, (unsigned)ceil_div(nr, 32)), tb, 0, st>>>(Ut, kOuterW, A12, ld,
+                                                                                                 nr, kNB);
+                FLG_LAUNCH_CHECK();
+                FLG_TRY(tc_update(A21, ld, A21, ld, UinvT, kNB, nr, kNB, kNB, FLG_LU_TF32, tcw, tcb, st, dinfo + 1,
+                                  true));
+            } else if (nb == kNB) {
                 // U12 = Linv A12 (+ its K-major copy), L21 = A21 Uinv: one launch, in place
                 const int ntu = (int)ceil_div(nr, 32), ntl = (int)ceil_div(nr, 32);
                 lowp_panel_kernel<<<ntu + ntl, 256, 0, st>>>(A, ld, k0, nr, Linv + k * kNB * kNB, Uinv + k * kNB * kNB,

@@ -1,6 +1,7 @@
 // tc_gemm.cu -- tcgen05 tensor-core rank-K update for the low-precision LU.
 //
 //   C (m x nc, FP32, row-major, ldc)  -=  A (m x K) * B^T,  B given as Bt (nc x K)
+//   (or, in store mode, C = A * B^T)
 //
 // Both operands are K-major (K contiguous per row, K a multiple of 128).  A
 // persistent kernel, one CTA per SM, walks the 128 x 256 tiles of C:
@@ -89,6 +90,12 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, u
         "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(x), "r"(y)
         : "memory");
 }
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, const void *src, int x, int y) {
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.tile.bulk_group [%0, {%2, %3}], [%1];" ::"l"(
+                     (uint64_t)map),
+                 "r"(smem_u32(src)), "r"(x), "r"(y)
+                 : "memory");
+}
 __device__ __forceinline__ void tma_reduce_add_2d(const CUtensorMap *map, const void *src, int x, int y) {
     asm volatile("cp.reduce.async.bulk.tensor.2d.global.shared::cta.add.tile.bulk_group [%0, {%2, %3}], [%1];" ::"l"(
                      (uint64_t)map),
@@ -117,7 +124,7 @@ template <int MODE>
 __global__ void __launch_bounds__(TC_THREADS, 1) tc_update_kernel(const __grid_constant__ CUtensorMap tmA,
                                                                   const __grid_constant__ CUtensorMap tmB,
                                                                   const __grid_constant__ CUtensorMap tmC, int m,
-                                                                  int nc, int nkb, int *err) {
+                                                                  int nc, int nkb, int store, int *err) {
     constexpr int KBLK = MODE == FLG_LU_TF32 ? 32 : 64;  // elements per 128-byte row
     constexpr int KSTEP_BYTES = 32;                       // one MMA consumes 32 bytes of each row
     constexpr uint32_t IDESC = tc_idesc(MODE == FLG_LU_TF32 ? 2u : 1u);
@@ -259,16 +266,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_update_kernel(const __grid_c
                 if (nst >= 2 && lane == 0) asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
                 __syncwarp();
                 // row `lane`, 16-byte chunk c at chunk position c ^ (row % 8) (128-byte swizzle)
+                const float sg = store ? 1.0f : -1.0f;  // C = acc, or C += -acc
 #pragma unroll
                 for (int c = 0; c < 8; c++) {
-                    const float4 w = make_float4(-__uint_as_float(v[4 * c]), -__uint_as_float(v[4 * c + 1]),
-                                                 -__uint_as_float(v[4 * c + 2]), -__uint_as_float(v[4 * c + 3]));
+                    const float4 w = make_float4(sg * __uint_as_float(v[4 * c]), sg * __uint_as_float(v[4 * c + 1]),
+                                                 sg * __uint_as_float(v[4 * c + 2]), sg * __uint_as_float(v[4 * c + 3]));
                     *reinterpret_cast<float4 *>(box + lane * 128 + ((c ^ (lane & 7)) << 4)) = w;
                 }
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 __syncwarp();
                 if (lane == 0) {
-                    tma_reduce_add_2d(&tmC, box, n0 + ch * 32, m0 + q * 32);
+                    if (store) tma_store_2d(&tmC, box, n0 + ch * 32, m0 + q * 32);
+                    else tma_reduce_add_2d(&tmC, box, n0 + ch * 32, m0 + q * 32);
                     asm volatile("cp.async.bulk.commit_group;" ::: "memory");
                 }
             }
@@ -372,7 +381,8 @@ size_t tc_update_bytes(int64_t m, int64_t nc, int64_t K, int mode) {
 // the workspace and the call synchronizes to check it; the LU passes its own
 // flag and checks it once at the end of the factorization.
 int tc_update(float *C, int64_t ldc, const float *Lp, int64_t ldl, const float *Ut, int64_t ldu, int64_t m,
-              int64_t nc, int64_t K, int mode, void *work, size_t work_bytes, cudaStream_t st, int *err_dev) {
+              int64_t nc, int64_t K, int mode, void *work, size_t work_bytes, cudaStream_t st, int *err_dev,
+              bool store) {
     FLG_REQUIRE(mode == FLG_LU_TF32 || mode == FLG_LU_BF16, "tensor-core mode must be TF32 or BF16");
     FLG_REQUIRE(m >= 0 && nc >= 0 && m < (1LL << 31) && nc < (1LL << 31), "bad tensor-core update shape");
     FLG_REQUIRE(K > 0 && K % 128 == 0 && K <= (1 << 20), "tensor-core update depth must be a multiple of 128");
@@ -411,9 +421,11 @@ int tc_update(float *C, int64_t ldc, const float *Lp, int64_t ldl, const float *
     }
     const int nkb = (int)(K / (mode == FLG_LU_TF32 ? 32 : 64));
     if (mode == FLG_LU_TF32) {
-        tc_update_kernel<FLG_LU_TF32><<<grid, TC_THREADS, TC_SMEM, st>>>(ma, mb, mc, (int)m, (int)nc, nkb, err);
+        tc_update_kernel<FLG_LU_TF32><<<grid, TC_THREADS, TC_SMEM, st>>>(ma, mb, mc, (int)m, (int)nc, nkb,
+                                                                          store ? 1 : 0, err);
     } else {
-        tc_update_kernel<FLG_LU_BF16><<<grid, TC_THREADS, TC_SMEM, st>>>(ma, mb, mc, (int)m, (int)nc, nkb, err);
+        tc_update_kernel<FLG_LU_BF16><<<grid, TC_THREADS, TC_SMEM, st>>>(ma, mb, mc, (int)m, (int)nc, nkb,
+                                                                          store ? 1 : 0, err);
     }
     FLG_LAUNCH_CHECK();
     if (err_dev) return FLG_OK;
@@ -434,5 +446,6 @@ extern "C" int flg_tc_rank_update(float *C, int64_t ldc, const float *A, int64_t
                                   int64_t m, int64_t nc, int mode, void *work, size_t work_bytes, void *stream) {
     FLG_REQUIRE(ldb == 128, "Bt must be compact (ldb == 128)");
     FLG_REQUIRE(lda >= 128 && ldc >= nc, "bad leading dimensions");
-    return flg::tc_update(C, ldc, A, lda, Bt, 128, m, nc, 128, mode, work, work_bytes, flg::as_stream(stream), nullptr);
+    return flg::tc_update(C, ldc, A, lda, Bt, 128, m, nc, 128, mode, work, work_bytes, flg::as_stream(stream), nullptr,
+                          false);
 }
