@@ -794,6 +794,8 @@ struct ApplyArgs {
     const float *Linv, *Uinv;
     const float *b;  // right-hand side (FP32, n)
     float *y, *x;    // forward / backward results (n), preset to kUnset
+    float *part;     // team partial sums [2 passes][blocks][T][128], preset to kUnset
+    int T;           // CTAs per owned block (team size)
     int *err;        // a wait ran out
 };
 
@@ -927,9 +929,10 @@ __global__ void __launch_bounds__(kApplyThreads) lowp_apply_kernel(ApplyArgs a) 
     __shared__ __align__(16) float tvec[4 * kQP];   // t_i of the block being finalized (kQP layout)
     __shared__ int abort_s;
     const int t = threadIdx.x, r = t >> 2, q = t & 3;
-    const int G = gridDim.x, c = blockIdx.x;
+    const int T = a.T, tm = blockIdx.x % T;   // team member (0 = leader, which finalizes)
+    const int GO = gridDim.x / T, o = blockIdx.x / T;  // owner slots, this CTA's slot
     const int nblk = (int)ceil_div(a.n, kNB);
-    const int nown = c < nblk ? (nblk - 1 - c) / G + 1 : 0;
+    const int nown = o < nblk ? (nblk - 1 - o) / GO + 1 : 0;
     if (t == 0) abort_s = 0;
     __syncthreads();
     for (int pass = 0; pass < 2 && nown > 0; pass++) {
@@ -939,49 +942,78 @@ __global__ void __launch_bounds__(kApplyThreads) lowp_apply_kernel(ApplyArgs a) 
         float *out_v = fwd ? a.y : a.x;  // this pass publishes into out_v and consumes from it
         // owned blocks in order: ascending forward, descending backward
         for (int mi = 0; mi < nown; mi++) {
-            const int i = c + (fwd ? mi : nown - 1 - mi) * G;
+            const int i = o + (fwd ? mi : nown - 1 - mi) * GO;
             const int64_t row = (int64_t)i * kNB + r;
             const bool rok = row < a.n;
             float Dr[32];
-            load_row32_early(Dr, D + (int64_t)i * kNB * kNB + r * kNB + 32 * q);
             float rhs = 0.0f;
-            if (rok) rhs = fwd ? load_f32_early(a.b + row) : __uint_as_float(ld_relaxed_u32(a.y + row));
-            // consume blocks jfirst, jfirst + dir, ..., i - dir (nc of them), kRing slices ahead
+            if (tm == 0) {
+                load_row32_early(Dr, D + (int64_t)i * kNB * kNB + r * kNB + 32 * q);
+                if (rok) rhs = fwd ? load_f32_early(a.b + row) : __uint_as_float(ld_relaxed_u32(a.y + row));
+            }
+            // blocks to consume: k = 0 .. nc - 1 (block jfirst + dir k); member tm takes
+            // k = tm, tm + T, ... below nc - 1, the leader also the critical k = nc - 1
             const int jfirst = fwd ? 0 : nblk - 1;
             const int nc = fwd ? i : nblk - 1 - i;
-            auto issue = [&](int k) {
-                const int j = jfirst + dir * k;
+            auto count = [&](int m) { return nc - 1 > m ? (nc - 1 - m + T - 1) / T : 0; };
+            const int cnt = count(tm) + ((tm == 0 && nc >= 1) ? 1 : 0);
+            auto kth = [&](int u) { return u < count(tm) ? tm + u * T : nc - 1; };
+            auto issue = [&](int u) {
+                const int j = jfirst + dir * kth(u);
                 const int64_t col0 = (int64_t)j * kNB + 32 * q;
                 const int valid = rok ? (int)max((int64_t)0, min((int64_t)32, a.n - col0)) : 0;
-                ring_issue(ring + (k % kRing) * (kApplyThreads * 32), rok ? a.LU + row * a.ld + col0 : a.LU, valid);
+                ring_issue(ring + (u % kRing) * (kApplyThreads * 32), rok ? a.LU + row * a.ld + col0 : a.LU, valid);
                 asm volatile("cp.async.commit_group;" ::: "memory");
             };
-            auto probe = [&](int k) {
-                const int64_t e = (int64_t)(jfirst + dir * k) * kNB + t;
+            auto probe = [&](int u) {
+                const int64_t e = (int64_t)(jfirst + dir * kth(u)) * kNB + t;
                 return (t < kNB && e < a.n) ? ld_relaxed_u32(out_v + e) : 0u;
             };
             float acc = 0.0f;
             int issued = 0;
-            for (; issued < min(kRing, nc); issued++) issue(issued);
-            unsigned pc = nc > 0 ? probe(0) : 0u;
-            for (int k = 0; k < nc; k++) {
-                // slice k has landed once at most (issued - k - 1) newer groups are pending
-                const int pend = issued - k - 1;
+            for (; issued < min(kRing, cnt); issued++) issue(issued);
+            unsigned pc = cnt > 0 ? probe(0) : 0u;
+            for (int u = 0; u < cnt; u++) {
+                // slice u has landed once at most (issued - u - 1) newer groups are pending
+                const int pend = issued - u - 1;
                 if (pend >= 2) asm volatile("cp.async.wait_group 2;" ::: "memory");
                 else if (pend == 1) asm volatile("cp.async.wait_group 1;" ::: "memory");
                 else asm volatile("cp.async.wait_group 0;" ::: "memory");
-                const unsigned pn = k + 1 < nc ? probe(k + 1) : 0u;
-                if (!fetch_block(vec, out_v, jfirst + dir * k, a.n, pc, a.err, &abort_s)) {
+                const unsigned pn = u + 1 < cnt ? probe(u + 1) : 0u;
+                if (!fetch_block(vec, out_v, jfirst + dir * kth(u), a.n, pc, a.err, &abort_s)) {
                     asm volatile("cp.async.wait_all;" ::: "memory");
                     return;
                 }
-                acc += ring_dot(ring + (k % kRing) * (kApplyThreads * 32), vec + q * kQP);
+                acc += ring_dot(ring + (u % kRing) * (kApplyThreads * 32), vec + q * kQP);
                 __syncthreads();  // vec is rewritten next
-                if (issued < nc) issue(issued++);  // reuses slot k % kRing, just read by this thread
+                if (issued < cnt) issue(issued++);  // reuses slot u % kRing, just read by this thread
                 pc = pn;
             }
+            float tot = row_sum4(acc);
+            float *pslot = a.part + ((int64_t)(pass * nblk + i) * T) * kNB;
+            if (tm > 0) {  // a member hands its partial sums to the leader
+                if (count(tm) > 0 && q == 0 && rok) st_relaxed_f32(pslot + tm * kNB + r, tot);
+                continue;
+            }
+            // the leader adds the members' partial sums (each row polled by its q == 0 thread)
+            if (q == 0 && rok) {
+                for (int m = 1; m < T; m++) {
+                    if (count(m) == 0) continue;
+                    unsigned uv;
+                    const long long t0 = clock64();
+                    while ((uv = ld_relaxed_u32(pslot + m * kNB + r)) == kUnset) {
+                        if (*(volatile int *)a.err || clock64() - t0 > kSpinLimit) {
+                            atomicExch(a.err, 1);
+                            abort_s = 1;
+                            break;
+                        }
+                    }
+                    tot += __uint_as_float(uv);
+                }
+            }
+            __syncthreads();
+            if (*(volatile int *)&abort_s) return;
             // finalize block i: t_i = rhs_i - sum, out_i = D_i t_i, published element by element
-            const float tot = row_sum4(acc);
             if (q == 0) tvec[qpos(r)] = rok ? rhs - tot : 0.0f;
             __syncthreads();
             const float out = row_sum4(dot32q(Dr, tvec + q * kQP));
@@ -1001,11 +1033,17 @@ __global__ void f2d_kernel(const float *a, double *b, int64_t n, const int *err)
     if (i < n) b[i] = *err ? __longlong_as_double(0x7ff8000000000000LL) : (double)a[i];
 }
 
+constexpr int kApplyMaxTeam = 8;
+// CTAs per owned block: spare SMs share the consumption of each block row
+static int apply_team(int64_t nblk) {
+    return (int)std::max<int64_t>(1, std::min<int64_t>(kApplyMaxTeam, sm_count() / std::max<int64_t>(nblk, 1)));
+}
+
 size_t lu_solve_lowp_bytes(int64_t n) {
     CountingArena c;
+    const int64_t nblk = ceil_div(std::max<int64_t>(n, 1), kNB);
     c.take<float>(n);
-    c.take<float>(n);
-    c.take<float>(n);
+    c.take<float>(3 * n + 2 * nblk * kApplyMaxTeam * kNB);  // y, x, team partials: one sentinel fill
     c.take<int>(1);
     return c.bytes();
 }
@@ -1016,17 +1054,18 @@ int lu_solve_lowp_apply(int64_t n, const float *LU, int64_t ld, const float *din
     Arena ar(work, work_bytes);
     const int64_t nblk = ceil_div(n, kNB);
     float *bf = ar.take<float>(n);
-    float *y = ar.take<float>(n);
-    float *z = ar.take<float>(n);
+    float *yz = ar.take<float>(3 * n + 2 * nblk * kApplyMaxTeam * kNB);
     int *err = ar.take<int>(1);
-    FLG_REQUIRE(bf && y && z && err, "workspace too small for the low-precision solve");
-    const int G = (int)std::min<int64_t>(nblk, sm_count());
+    FLG_REQUIRE(bf && yz && err, "workspace too small for the low-precision solve");
+    float *y = yz, *z = yz + n, *part = yz + 2 * n;
+    const int T = apply_team(nblk);
+    const int G = (int)std::min<int64_t>(nblk, sm_count() / T) * T;  // T CTAs per owner slot
     d2f_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(b, bf, n);
     FLG_LAUNCH_CHECK();
-    // y and z adjacent: one fill with the unset pattern
-    FLG_CUDA(cudaMemsetAsync(y, 0xff, sizeof(float) * (size_t)(z + n - y), st));
+    // y, z and the partials: one fill with the unset pattern
+    FLG_CUDA(cudaMemsetAsync(yz, 0xff, sizeof(float) * (size_t)(2 * n + 2 * nblk * T * kNB), st));
     FLG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
-    ApplyArgs aa{LU, ld, n, dinv, dinv + nblk * kNB * kNB, bf, y, z, err};
+    ApplyArgs aa{LU, ld, n, dinv, dinv + nblk * kNB * kNB, bf, y, z, part, T, err};
     void *args[] = {&aa};
     static bool attr_set = false;
     if (!attr_set) {
