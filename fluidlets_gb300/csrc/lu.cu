@@ -810,19 +810,6 @@ __device__ __forceinline__ void st_relaxed_f32(float *p, float v) {
     asm volatile("st.relaxed.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(u) : "memory");
 }
 
-// 32-wide slice of a row (`valid` leading entries exist; zeros for the rest)
-__device__ __forceinline__ void load_row32(float (&v)[32], const float *p, int valid) {
-    if (valid >= 32) {
-#pragma unroll
-        for (int c = 0; c < 32; c += 4) {
-            const float4 w = __ldg(reinterpret_cast<const float4 *>(p + c));
-            v[c] = w.x, v[c + 1] = w.y, v[c + 2] = w.z, v[c + 3] = w.w;
-        }
-    } else {
-#pragma unroll
-        for (int c = 0; c < 32; c++) v[c] = c < valid ? __ldg(p + c) : 0.0f;
-    }
-}
 // sum over the four threads of a row (consecutive lanes)
 __device__ __forceinline__ float row_sum4(float v) {
     v += __shfl_xor_sync(0xffffffffu, v, 1);

@@ -191,13 +191,14 @@ int flg_lu_solve_f64(int64_t n, int64_t nrhs, const double *LU, int64_t ld, cons
 
 /* Low-precision LU without pivoting for the mixed-precision path: A is FP32
  * (n x n, ld; ld a multiple of 4 so every row starts on a 16-byte boundary),
- * factored in place (unit L, U) in blocks of FLG_LU_LOWP_BLOCK with the
- * trailing updates on the tcgen05 tensor cores (mode FLG_LU_TF32 or
- * FLG_LU_BF16; FLG_LU_FP32 uses CUDA cores).  dinv (FP32, size
- * flg_lu_lowp_dinv_elems(n)) receives the inverses of the diagonal blocks
- * of L and U, used by flg_lu_solve_lowp.  Only used as a preconditioner of
- * FP64 GMRES iterative refinement, so accuracy is recovered in FP64.
- * info as above (a zero or non-finite pivot).  Synchronizes `stream`. */
+ * factored in place (unit L, U) in blocks of FLG_LU_LOWP_BLOCK.  With mode
+ * FLG_LU_TF32 or FLG_LU_BF16 the panels (TF32) and the trailing updates (the
+ * mode's type; rank 128 inside 512-column outer panels, rank 512 for the rest)
+ * run on the tcgen05 tensor cores; FLG_LU_FP32 uses CUDA cores throughout.
+ * dinv (FP32, size flg_lu_lowp_dinv_elems(n)) receives the inverses of the
+ * diagonal blocks of L and U, used by flg_lu_solve_lowp.  Only used as a
+ * preconditioner of FP64 GMRES iterative refinement, so accuracy is recovered
+ * in FP64.  info as above (a zero or non-finite pivot).  Synchronizes `stream`. */
 #define FLG_LU_LOWP_BLOCK 128
 int64_t flg_lu_lowp_dinv_elems(int64_t n);
 size_t flg_lu_factor_lowp_workspace(int64_t n, int mode);
@@ -210,7 +211,8 @@ int flg_lu_factor_lowp(int64_t n, float *A, int64_t ld, int mode, float *dinv, i
 int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mode, float *dinv, int *flags,
                              void *work, size_t work_bytes, void *stream);
 /* x = (L U)^{-1} b in FP32 for one FP64 right-hand side (converted on the
- * fly), result written as FP64. */
+ * fly), result written as FP64: one cooperative launch, a dataflow over the
+ * 128-row blocks with bounded waits (a timed-out wait makes x NaN). */
 size_t flg_lu_solve_lowp_workspace(int64_t n);
 int flg_lu_solve_lowp(int64_t n, const float *LU, int64_t ld, const float *dinv, const double *b, double *x,
                       void *work, size_t work_bytes, void *stream);
