@@ -118,6 +118,26 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def ranks_throughput(dist, local_ms, units_per_rank, world, device=None, reduce="max"):
+    """Whole-job throughput of `world` independent replicas: every rank processed
+    units_per_rank units; the job took as long as the slowest rank (reduce="max" over the
+    ranks' times; "min" over per-rank throughputs for the end-to-end figure).  Returns
+    (units per second, the time in ms that it is based on)."""
+    import torch
+
+    if reduce == "max":
+        t = torch.tensor([float(local_ms)], dtype=torch.float64, device=device)
+        if dist is not None:
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        return units_per_rank * world / (ms * 1e-3), ms
+    rate = torch.tensor([units_per_rank * world / (float(local_ms) * 1e-3)], dtype=torch.float64, device=device)
+    if dist is not None:
+        dist.all_reduce(rate, op=dist.ReduceOp.MIN)
+    r = float(rate.item())
+    return r, units_per_rank * world / r * 1e3
+
+
 def make_workload(seed):
     from fluidlets_gb300.geometry import wall_sum_workload
 
@@ -277,11 +297,7 @@ def run_ours(args):
     near_ms, near_n = ctypes.c_double(0), ctypes.c_int64(0)
     L.flg_profile_read(_lib.SLOT["near_f64"], ctypes.byref(near_ms), ctypes.byref(near_n))
     L.flg_profile_enable(0)
-    if dist:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = pairs * args.steps * world / (total_ms * 1e-3)
+    value, total_ms = ranks_throughput(dist, total_ms, pairs * args.steps, world, dev)
 
     # e2e through the public API: pinned host inputs, host output
     Th, Sh, Fh = (torch.from_numpy(a).pin_memory() for a in (T, S, F))
@@ -298,11 +314,7 @@ def run_ours(args):
     assert out_h.device.type == "cpu"
     h2d = (T.nbytes + S.nbytes + F.nbytes)
     d2h = out_h.numel() * out_h.element_size()
-    e2e_value = pairs * world / e2e_s
-    if dist:
-        t = torch.tensor([e2e_value], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MIN)
-        e2e_value = float(t.item()) * 1.0
+    e2e_value, _ = ranks_throughput(dist, e2e_s * 1e3, pairs, world, dev, reduce="min")
 
     far_avg_ms = far_ms.value / max(far_n.value, 1)
     achieved = FLOPS_PER_PAIR * pairs / (far_avg_ms * 1e-3) / 1e12
