@@ -272,4 +272,50 @@ __device__ __forceinline__ void wall_apply(const WallGeo<T> &g, T f0, T f1, T f2
     u[2] = fmaT(g.W2, u2b, u[2]);
 }
 
+// Far-field wall pair in FP32 for the kernel sum, without the per-pair factor 2 t h:
+// the source height h is folded into the packed strengths and 2 t is applied per
+// target after each source tile, so every output accumulates with fused
+// multiply-adds.  A near pair (QF < thr) gets s = 0, which zeroes every term
+// exactly (the reciprocal is of sF + s >= sF > 0).  sF^2 + sF s + s^2 is formed as
+// (sF + s)^2 - sF s from the reciprocal's denominator (all terms positive).
+struct WallFar {
+    float d0, d1, dm, dp, cxy, cz, Z3, s5x3;
+};
+__device__ __forceinline__ WallFar wall_far_geo(float tx, float ty, float tz, float sx, float sy, float h, float e2,
+                                                float thr) {
+    WallFar g;
+    g.d0 = sub_rn(tx, sx);
+    g.d1 = sub_rn(ty, sy);
+    g.dm = sub_rn(tz, h);
+    g.dp = tz + h;
+    const float rq = __fmaf_rn(g.d1, g.d1, __fmaf_rn(g.d0, g.d0, e2));
+    const float QF = __fmaf_rn(g.dm, g.dm, rq);
+    const float QI = fmaf(g.dp, g.dp, rq);
+    const float sF = rsq(QF);
+    float s = rsq(QI);
+    s = (QF < thr) ? 0.0f : s;
+    const float p = sF * s, q = sF + s;
+    const float Z1 = (p * (p + p)) * rcp(q);
+    g.Z3 = Z1 * fmaf(q, q, -p);
+    const float s2 = s * s, s3 = s2 * s, s5 = s3 * s2;
+    const float base = fmaf(e2, g.Z3, Z1) - s3;
+    const float e2s5 = e2 * s5;
+    g.cxy = fmaf(e2s5, 3.0f, base);
+    g.cz = fmaf(e2s5, -3.0f, base);
+    g.s5x3 = 3.0f * s5;
+    return g;
+}
+// u += the pair's velocity for the h-scaled strengths (f0, f1, f2), without the factor 2 t
+__device__ __forceinline__ void wall_far_acc(const WallFar &g, float f0, float f1, float f2, float *u) {
+    const float D = fmaf(g.d1, f1, g.d0 * f0);
+    const float fdF = fmaf(g.dm, f2, D);
+    const float P = fmaf(g.dp, f2, -D);
+    const float t1 = g.Z3 * fdF;
+    const float v = g.s5x3 * P;
+    const float Bxy = t1 - v;
+    u[0] = fmaf(g.d0, Bxy, fmaf(g.cxy, f0, u[0]));
+    u[1] = fmaf(g.d1, Bxy, fmaf(g.cxy, f1, u[1]));
+    u[2] = fmaf(g.cz, f2, fmaf(g.dm, t1, fmaf(-g.dp, v, u[2])));
+}
+
 }  // namespace flg

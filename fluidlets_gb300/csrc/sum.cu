@@ -219,9 +219,11 @@ __device__ __forceinline__ void pair_f32_far(float tx, float ty, float tz, float
                                              const float4 &q, const float4 &r, float are, float aim, float *u) {
     // p = {x, y, z, e2}; q = {f0, f1, f2, thr}; r = {f0i, f1i, f2i, 0}
     if constexpr (KIND == FLG_WALL) {
-        WallGeo<float> g = wall_geo<float, true>(tx, ty, tz, tz2, p.x, p.y, p.z, p.w, q.w);
-        wall_apply(g, q.x, q.y, q.z, u);
-        if constexpr (NF == 2) wall_apply(g, r.x, r.y, r.z, u + 3);
+        // strengths arrive scaled by the source height; the caller applies 2 t per tile
+        (void)tz2;
+        const WallFar g = wall_far_geo(tx, ty, tz, p.x, p.y, p.z, p.w, q.w);
+        wall_far_acc(g, q.x, q.y, q.z, u);
+        if constexpr (NF == 2) wall_far_acc(g, r.x, r.y, r.z, u + 3);
     } else {
         float d0 = sub_rn(tx, p.x), d1 = sub_rn(ty, p.y), d2 = sub_rn(tz, p.z);
         float Q = free_Q_f32(d0, d1, d2, p.w);
@@ -320,7 +322,7 @@ __global__ void __launch_bounds__(kF32Threads) far_f32_kernel(FarArgs a) {
 #pragma unroll
         for (int t = 0; t < TPT; t++)
 #pragma unroll
-            for (int c = 0; c < OUTW; c++) acc[t][c] += (double)u[t][c];
+            for (int c = 0; c < OUTW; c++) acc[t][c] += (double)(KIND == FLG_WALL ? tz2[t] * u[t][c] : u[t][c]);
     }
 #pragma unroll
     for (int t = 0; t < TPT; t++) {
@@ -344,21 +346,25 @@ __global__ void pack_geometry_kernel(const double *src, const double *eps, int64
     packed[j * NQ + 1].w = __fmul_rn(17.0f, e2);  // |d|^2 < 16 eps^2  <=>  QF < 17 eps^2
 }
 
-__global__ void pack_strengths_kernel(const double *f, int64_t N, int NF, float4 *packed) {
+// src (wall kernel only): the strengths are scaled by the source height z_j, the factor of
+// the wall pair that depends on the source alone (see wall_far_geo)
+__global__ void pack_strengths_kernel(const double *f, const double *src, int64_t N, int NF, float4 *packed) {
     const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= N) return;
     const int NQ = 1 + NF;
     float4 *q = packed + j * NQ + 1;
     const double *fj = f + (int64_t)3 * NF * j;
+    const double h = src ? src[3 * j + 2] : 1.0;
     if (NF == 1) {
-        q->x = __double2float_rn(fj[0]);
-        q->y = __double2float_rn(fj[1]);
-        q->z = __double2float_rn(fj[2]);
+        q->x = __double2float_rn(h * fj[0]);
+        q->y = __double2float_rn(h * fj[1]);
+        q->z = __double2float_rn(h * fj[2]);
     } else {  // interleaved complex (re, im) per component
-        q->x = __double2float_rn(fj[0]);
-        q->y = __double2float_rn(fj[2]);
-        q->z = __double2float_rn(fj[4]);
-        q[1] = make_float4(__double2float_rn(fj[1]), __double2float_rn(fj[3]), __double2float_rn(fj[5]), 0.0f);
+        q->x = __double2float_rn(h * fj[0]);
+        q->y = __double2float_rn(h * fj[2]);
+        q->z = __double2float_rn(h * fj[4]);
+        q[1] = make_float4(__double2float_rn(h * fj[1]), __double2float_rn(h * fj[3]), __double2float_rn(h * fj[5]),
+                           0.0f);
     }
 }
 
@@ -725,7 +731,8 @@ static int launch_sum(const SumRun &r, const SumLayout &L, int precision, const 
         return FLG_OK;
     }
     // mixed: strengths into the packed slots, FP32 far field, FP64 near field + combine
-    pack_strengths_kernel<<<(unsigned)ceil_div(r.N, 256), 256, 0, st>>>(r.f, r.N, NF, p->packed);
+    pack_strengths_kernel<<<(unsigned)ceil_div(r.N, 256), 256, 0, st>>>(r.f, KIND == FLG_WALL ? r.src : nullptr,
+                                                                       r.N, NF, p->packed);
     FLG_LAUNCH_CHECK();
     constexpr int TPT = (NF == 1 && !CK) ? FLG_FAR_TPT : 1;
     FarArgs fa{r.tg, r.M, p->packed, r.N, L.split_len, (float)r.alpha_re, (float)r.alpha_im, p->partial};
