@@ -17,6 +17,9 @@ KIND = {"stokeslet": 0, "wall": 1, "brinkman": 2}
 PREC = {"fp64": 0, "mixed": 1}
 F64, C128, F32, BF16 = 0, 1, 2, 3
 LU_MODE = {"tf32": 0, "bf16": 1, "fp32": 2}
+# tensor-core modes with a forced tile width of the trailing updates ("tf32:128": 128 x 128 tiles)
+LU_TILE = {128: 0x100, 256: 0x200}
+LU_MODE.update({f"{p}:{t}": LU_MODE[p] | b for p in ("tf32", "bf16") for t, b in LU_TILE.items()})
 
 # name -> (restype, argtypes); mirrors include/fluidlets_gb300.h
 _P = c_void_p

@@ -741,7 +741,7 @@ __global__ void transpose_f32_kernel(const float *src, int64_t lds, float *dst, 
 size_t tc_update_bytes(int64_t m, int64_t nc, int64_t K, int mode);
 int tc_update(float *C, int64_t ldc, const float *Lp, int64_t ldl, const float *Ut, int64_t ldu, int64_t m,
               int64_t nc, int64_t K, int mode, void *work, size_t work_bytes, cudaStream_t st, int *err_dev,
-              bool store = false);
+              bool store = false, int tile = 0);
 
 static int sgemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, float alpha, const float *A, int64_t lda,
                  const float *B, int64_t ldb, float beta, float *C, int64_t ldc) {
@@ -1230,7 +1230,11 @@ static void lowp_carve(Ar &ar, int64_t n, int mode, float **U12, float **L21, fl
     *tcw = ar.template take<char>(*tcb);
 }
 
+// precision part of an LU mode (the tile bits masked off)
+static int lu_prec(int mode) { return mode & ~(FLG_LU_TILE_N128 | FLG_LU_TILE_N256); }
+
 extern "C" size_t flg_lu_factor_lowp_workspace(int64_t n, int mode) {
+    mode = lu_prec(mode);
     CountingArena c;
     float *a, *b, *d;
     char *w;
@@ -1242,7 +1246,12 @@ extern "C" size_t flg_lu_factor_lowp_workspace(int64_t n, int mode) {
 extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mode, float *dinv, int *flags, void *work,
                                         size_t work_bytes, void *stream) {
     FLG_REQUIRE(n >= 0 && ld >= n && flags, "bad LU arguments");
-    FLG_REQUIRE(mode == FLG_LU_TF32 || mode == FLG_LU_BF16 || mode == FLG_LU_FP32, "unknown LU mode %d", mode);
+    const int tbits = mode & (FLG_LU_TILE_N128 | FLG_LU_TILE_N256);
+    FLG_REQUIRE(tbits != (FLG_LU_TILE_N128 | FLG_LU_TILE_N256), "two tile widths in LU mode %d", mode);
+    const int tile = tbits == FLG_LU_TILE_N128 ? 128 : tbits == FLG_LU_TILE_N256 ? 256 : 0;
+    mode = lu_prec(mode);
+    FLG_REQUIRE(mode == FLG_LU_TF32 || mode == FLG_LU_BF16 || (mode == FLG_LU_FP32 && tile == 0), "unknown LU mode %d",
+                mode | tbits);
     FLG_REQUIRE(ld % 4 == 0, "ld must be a multiple of 4 (16-byte rows)");
     cudaStream_t st = as_stream(stream);
     FLG_CUDA(cudaMemsetAsync(flags, 0, 2 * sizeof(int), st));
@@ -1316,18 +1325,19 @@ extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mod
                 FLG_TRY(sgemm(st, nr, nr, nb, -1.0f, A21, ld, A12, ld, 1.0f, A22, ld));
             } else if (E > c0) {
                 // rows > k0 x columns (k0, E)
-                FLG_TRY(tc_update(A22, ld, A21, ld, Ut, kOuterW, nr, E - c0, kNB, mode, tcw, tcb, st, dinfo + 1));
+                FLG_TRY(tc_update(A22, ld, A21, ld, Ut, kOuterW, nr, E - c0, kNB, mode, tcw, tcb, st, dinfo + 1,
+                                  false, tile));
                 // rows (k0, E) x columns >= E
                 if (n > E)
                     FLG_TRY(tc_update(A + c0 * ld + E, ld, A21, ld, Ut + (E - c0) * kOuterW, kOuterW, E - c0, n - E,
-                                      kNB, mode, tcw, tcb, st, dinfo + 1));
+                                      kNB, mode, tcw, tcb, st, dinfo + 1, false, tile));
             }
             prof_end(FLG_SLOT_LU_UPDATE, st);
         }
         if (tc && n > E) {  // the deferred rank-(E - K0) update of rows and columns >= E (E - K0 = kOuterW here)
             prof_begin(FLG_SLOT_LU_UPDATE, st);
             FLG_TRY(tc_update(A + E * ld + E, ld, A + E * ld + K0, ld, UtB + (E - K0) * kOuterW, kOuterW, n - E, n - E,
-                              E - K0, mode, tcw, tcb, st, dinfo + 1));
+                              E - K0, mode, tcw, tcb, st, dinfo + 1, false, tile));
             prof_end(FLG_SLOT_LU_UPDATE, st);
         }
     }

@@ -4,14 +4,14 @@
 //   (or, in store mode, C = A * B^T)
 //
 // Both operands are K-major (K contiguous per row, K a multiple of 128).  A
-// persistent kernel, one CTA per SM, walks the 128 x 256 tiles of C:
+// persistent kernel, one CTA per SM, walks the 128 x BN tiles of C (BN = 256,
+// or 128 for narrow or small updates, chosen per call):
 //   * warp 0 (one lane) streams K-blocks of A and B (128 B = 32 TF32 or 64 BF16
 //     per row) with TMA (cp.async.bulk.tensor, 128-byte swizzle) into a
-//     4-stage shared-memory ring guarded by mbarriers;
-//   * warp 1 (one lane) issues tcgen05.mma (cta_group::1, M = 128, N = 256;
-//     kind::tf32, or kind::f16 with BF16 operands) into one of two 256-column
-//     TMEM accumulators (all 512 columns) and releases each stage with
-//     tcgen05.commit;
+//     shared-memory ring guarded by mbarriers (4 stages at BN = 256, 6 at 128);
+//   * warp 1 (one lane) issues tcgen05.mma (cta_group::1, M = 128, N = BN;
+//     kind::tf32, or kind::f16 with BF16 operands) into one of two BN-column
+//     TMEM accumulators and releases each stage with tcgen05.commit;
 //   * warps 2-5 drain the other accumulator (tcgen05.ld, 32 TMEM lanes each),
 //     stage -acc in 32 x 32 swizzled boxes and add them to C with TMA
 //     reduce-add (cp.reduce.async.bulk.tensor): C is never read by the SM and
@@ -30,14 +30,21 @@
 
 namespace flg {
 
-constexpr int TC_BM = 128, TC_BN = 256, TC_STAGES = 4, TC_THREADS = 192, TC_EPI_WARPS = 4;
+constexpr int TC_BM = 128, TC_THREADS = 192, TC_EPI_WARPS = 4;
 constexpr int TC_A_BYTES = TC_BM * 128;   // A tile of a K-block: 128 rows x 128 B
-constexpr int TC_B_BYTES = TC_BN * 128;   // B tile of a K-block: 256 rows x 128 B
 constexpr int TC_STG_BYTES = 32 * 128;    // one 32 x 32 FP32 staging box
-constexpr uint32_t TC_TMEM_COLS = 2 * TC_BN;  // two 256-column accumulators: all of TMEM
 constexpr long long TC_WAIT_LIMIT = 2000000000LL;  // ~1 s of SM clock per wait
-constexpr size_t TC_SMEM = 1024 + TC_STAGES * (TC_A_BYTES + TC_B_BYTES) + TC_EPI_WARPS * 2 * TC_STG_BYTES;
-static_assert(TC_SMEM <= 232448 - 256, "shared memory per CTA");
+
+// tile width BN: ring depth, B tile bytes (BN rows x 128 B), TMEM columns (two accumulators)
+template <int BN>
+struct TcTile {
+    static_assert(BN == 128 || BN == 256, "tile width");
+    static constexpr int STAGES = BN == 256 ? 4 : 6;
+    static constexpr int B_BYTES = BN * 128;
+    static constexpr uint32_t TMEM_COLS = 2 * BN;
+    static constexpr size_t SMEM = 1024 + STAGES * (TC_A_BYTES + B_BYTES) + TC_EPI_WARPS * 2 * TC_STG_BYTES;
+    static_assert(SMEM <= 232448 - 256, "shared memory per CTA");
+};
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -115,19 +122,21 @@ __device__ __forceinline__ uint64_t sw128_desc(const void *p) {
     return d;
 }
 
-// instruction descriptor: D = F32, A/B format (TF32 = 2, BF16 = 1), K-major A and B, M = 128, N = 256
-__host__ __device__ constexpr uint32_t tc_idesc(uint32_t fmt) {
-    return (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(TC_BN >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
+// instruction descriptor: D = F32, A/B format (TF32 = 2, BF16 = 1), K-major A and B, M = 128, N = bn
+__host__ __device__ constexpr uint32_t tc_idesc(uint32_t fmt, int bn) {
+    return (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(bn >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
 }
 
-template <int MODE>
+template <int MODE, int TC_BN>
 __global__ void __launch_bounds__(TC_THREADS, 1) tc_update_kernel(const __grid_constant__ CUtensorMap tmA,
                                                                   const __grid_constant__ CUtensorMap tmB,
                                                                   const __grid_constant__ CUtensorMap tmC, int m,
                                                                   int nc, int nkb, int store, int *err) {
     constexpr int KBLK = MODE == FLG_LU_TF32 ? 32 : 64;  // elements per 128-byte row
     constexpr int KSTEP_BYTES = 32;                       // one MMA consumes 32 bytes of each row
-    constexpr uint32_t IDESC = tc_idesc(MODE == FLG_LU_TF32 ? 2u : 1u);
+    constexpr uint32_t IDESC = tc_idesc(MODE == FLG_LU_TF32 ? 2u : 1u, TC_BN);
+    constexpr int TC_STAGES = TcTile<TC_BN>::STAGES, TC_B_BYTES = TcTile<TC_BN>::B_BYTES;
+    constexpr uint32_t TC_TMEM_COLS = TcTile<TC_BN>::TMEM_COLS;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t *sA = smem, *sB = smem + TC_STAGES * TC_A_BYTES, *stg = sB + TC_STAGES * TC_B_BYTES;
@@ -377,16 +386,48 @@ size_t tc_update_bytes(int64_t m, int64_t nc, int64_t K, int mode) {
     return c.bytes();
 }
 
+// Tile width for an m x nc update: the one whose waves over the SMs take the
+// least time, a 128 x BN tile costing about (128 + BN) units (operand bytes per
+// K-block).  BN = 256 reads 25 % fewer operand bytes per output; BN = 128 gives
+// twice the tiles for small updates and wastes nothing on updates of 128 columns.
+int tc_pick_tile(int64_t m, int64_t nc, int sms) {
+    const int64_t ty = ceil_div(m, TC_BM);
+    const int64_t w256 = ceil_div(ty * ceil_div(nc, 256), sms), w128 = ceil_div(ty * ceil_div(nc, 128), sms);
+    return w128 * (128 + 128) < w256 * (128 + 256) ? 128 : 256;
+}
+
+template <int MODE, int BN>
+static int tc_launch(const CUtensorMap &ma, const CUtensorMap &mb, const CUtensorMap &mc, int64_t m, int64_t nc,
+                     int nkb, bool store, int *err, int sms, cudaStream_t st) {
+    static bool attr_set = false;  // set once, so a later call can be captured in a graph
+    if (!attr_set) {
+        FLG_CUDA(cudaFuncSetAttribute(tc_update_kernel<MODE, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)TcTile<BN>::SMEM));
+        attr_set = true;
+    }
+    const int64_t ntiles = ceil_div(m, TC_BM) * ceil_div(nc, BN);
+    FLG_REQUIRE(ntiles < (1LL << 31), "too many tiles");
+    const unsigned grid = (unsigned)std::min<int64_t>(ntiles, sms);
+    tc_update_kernel<MODE, BN><<<grid, TC_THREADS, TcTile<BN>::SMEM, st>>>(ma, mb, mc, (int)m, (int)nc, nkb,
+                                                                           store ? 1 : 0, err);
+    FLG_LAUNCH_CHECK();
+    return FLG_OK;
+}
+
 // err_dev: device flag raised on a timed-out wait.  When null, the flag lives in
 // the workspace and the call synchronizes to check it; the LU passes its own
-// flag and checks it once at the end of the factorization.
+// flag and checks it once at the end of the factorization.  tile: 0 picks the
+// tile width (tc_pick_tile), 128 or 256 forces it.
 int tc_update(float *C, int64_t ldc, const float *Lp, int64_t ldl, const float *Ut, int64_t ldu, int64_t m,
               int64_t nc, int64_t K, int mode, void *work, size_t work_bytes, cudaStream_t st, int *err_dev,
-              bool store) {
+              bool store, int tile) {
     FLG_REQUIRE(mode == FLG_LU_TF32 || mode == FLG_LU_BF16, "tensor-core mode must be TF32 or BF16");
     FLG_REQUIRE(m >= 0 && nc >= 0 && m < (1LL << 31) && nc < (1LL << 31), "bad tensor-core update shape");
     FLG_REQUIRE(K > 0 && K % 128 == 0 && K <= (1 << 20), "tensor-core update depth must be a multiple of 128");
+    FLG_REQUIRE(tile == 0 || tile == 128 || tile == 256, "tile width must be 128 or 256 (or 0 to choose)");
     if (m == 0 || nc == 0) return FLG_OK;
+    const int sms = sm_count_of_current_device();
+    const int bn = tile ? tile : tc_pick_tile(m, nc, sms);
     Arena ar(work, work_bytes);
     int *own = ar.take<int>(1);
     int *err = err_dev ? err_dev : own;
@@ -394,7 +435,7 @@ int tc_update(float *C, int64_t ldc, const float *Lp, int64_t ldl, const float *
     CUtensorMap ma, mb, mc;
     if (mode == FLG_LU_TF32) {
         FLG_TRY(make_operand_map(&ma, Lp, m, K, ldl, mode, TC_BM));
-        FLG_TRY(make_operand_map(&mb, Ut, nc, K, ldu, mode, TC_BN));
+        FLG_TRY(make_operand_map(&mb, Ut, nc, K, ldu, mode, bn));
     } else {
         __nv_bfloat16 *La = ar.take<__nv_bfloat16>((size_t)m * K);
         __nv_bfloat16 *Ub = ar.take<__nv_bfloat16>((size_t)nc * K);
@@ -404,30 +445,19 @@ int tc_update(float *C, int64_t ldc, const float *Lp, int64_t ldl, const float *
         f32_to_bf16_rows_kernel<<<(unsigned)ceil_div(nc * K, 256), 256, 0, st>>>(Ut, ldu, Ub, nc, K);
         FLG_LAUNCH_CHECK();
         FLG_TRY(make_operand_map(&ma, La, m, K, K, mode, TC_BM));
-        FLG_TRY(make_operand_map(&mb, Ub, nc, K, K, mode, TC_BN));
+        FLG_TRY(make_operand_map(&mb, Ub, nc, K, K, mode, bn));
     }
     FLG_TRY(make_c_map(&mc, C, m, nc, ldc));
     if (!err_dev) FLG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
-    const int64_t ntiles = ceil_div(m, TC_BM) * ceil_div(nc, TC_BN);
-    FLG_REQUIRE(ntiles < (1LL << 31), "too many tiles");
-    const unsigned grid = (unsigned)std::min<int64_t>(ntiles, sm_count_of_current_device());
-    static bool attr_set = false;  // set once, so a later call can be captured in a graph
-    if (!attr_set) {
-        FLG_CUDA(cudaFuncSetAttribute(tc_update_kernel<FLG_LU_TF32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)TC_SMEM));
-        FLG_CUDA(cudaFuncSetAttribute(tc_update_kernel<FLG_LU_BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)TC_SMEM));
-        attr_set = true;
-    }
     const int nkb = (int)(K / (mode == FLG_LU_TF32 ? 32 : 64));
-    if (mode == FLG_LU_TF32) {
-        tc_update_kernel<FLG_LU_TF32><<<grid, TC_THREADS, TC_SMEM, st>>>(ma, mb, mc, (int)m, (int)nc, nkb,
-                                                                          store ? 1 : 0, err);
-    } else {
-        tc_update_kernel<FLG_LU_BF16><<<grid, TC_THREADS, TC_SMEM, st>>>(ma, mb, mc, (int)m, (int)nc, nkb,
-                                                                          store ? 1 : 0, err);
-    }
-    FLG_LAUNCH_CHECK();
+    int rc;
+    if (mode == FLG_LU_TF32)
+        rc = bn == 128 ? tc_launch<FLG_LU_TF32, 128>(ma, mb, mc, m, nc, nkb, store, err, sms, st)
+                       : tc_launch<FLG_LU_TF32, 256>(ma, mb, mc, m, nc, nkb, store, err, sms, st);
+    else
+        rc = bn == 128 ? tc_launch<FLG_LU_BF16, 128>(ma, mb, mc, m, nc, nkb, store, err, sms, st)
+                       : tc_launch<FLG_LU_BF16, 256>(ma, mb, mc, m, nc, nkb, store, err, sms, st);
+    FLG_TRY(rc);
     if (err_dev) return FLG_OK;
     int herr = 0;
     FLG_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -447,5 +477,5 @@ extern "C" int flg_tc_rank_update(float *C, int64_t ldc, const float *A, int64_t
     FLG_REQUIRE(ldb == 128, "Bt must be compact (ldb == 128)");
     FLG_REQUIRE(lda >= 128 && ldc >= nc, "bad leading dimensions");
     return flg::tc_update(C, ldc, A, lda, Bt, 128, m, nc, 128, mode, work, work_bytes, flg::as_stream(stream), nullptr,
-                          false);
+                          false, 0);
 }

@@ -16,9 +16,10 @@ its points into the plan's buffers, replays the graph and runs FP64 GMRES-IR
 on the padded system; padded rows are identity and padded right-hand sides
 zero, so the solution is exactly that of the unpadded system (the forces
 agree with a solve of the request alone to rounding).  The per-bucket choice
-of tensor-core precision (TF32 or BF16) is made by a small autotuner that
-times both on the first request of the bucket and keeps the faster one that
-converges.  Swimmer requests run the mixed-precision swimmer solve on the
+of tensor-core precision (TF32 or BF16) and of the trailing updates' tile
+width (128 x 128, 128 x 256, or chosen per update from its shape) is made by a
+small autotuner that times the six combinations on the first request of the
+bucket and keeps the fastest one that converges.  Swimmer requests run the mixed-precision swimmer solve on the
 slot's stream without a graph.
 """
 from __future__ import annotations
@@ -39,6 +40,9 @@ from ._lib import F64, LU_MODE, check, load
 from .kernels import Stokeslet3D, kernel_params
 
 BUCKET_BASE = 128
+# LU modes the autotuner times per bucket: precision, and the tile width of the trailing updates
+# (no suffix: chosen per update from its shape)
+TUNE_CANDIDATES = ("tf32", "tf32:128", "tf32:256", "bf16", "bf16:128", "bf16:256")
 
 
 def bucket_of(n_points: int) -> int:
@@ -111,7 +115,8 @@ class BucketPlan:
         self.dinv = torch.empty(L.flg_lu_lowp_dinv_elems(n), dtype=torch.float32, device=dev)
         self.flags = torch.zeros(2, dtype=torch.int32, device=dev)
         mode = LU_MODE[lu]
-        self.lu_bytes = L.flg_lu_factor_lowp_workspace(n, mode)
+        # sized for either tensor-core precision, so the autotuner can switch modes on one plan
+        self.lu_bytes = max(L.flg_lu_factor_lowp_workspace(n, LU_MODE[m]) for m in ("tf32", "bf16"))
         self.lu_ws = dv.workspace(self.lu_bytes)
         self.b = torch.zeros(n, dtype=torch.float64, device=dev)
         self.x = torch.zeros(n, dtype=torch.float64, device=dev)
@@ -129,6 +134,12 @@ class BucketPlan:
         check(L.flg_convert_f64_f32(self.n, self.n, dv.ptr(self.K), self.n, dv.ptr(self.A32), self.ld32, st), "convert")
         check(L.flg_lu_factor_lowp_async(self.n, dv.ptr(self.K32), self.ld32, self.mode, dv.ptr(self.dinv),
                                          dv.ptr(self.flags), dv.ptr(self.lu_ws), self.lu_bytes, st), "LU")
+
+    def set_lu(self, lu: str):
+        """Switch the LU mode of an uncaptured plan (the autotuner's candidates)."""
+        if self.graph is not None:
+            raise RuntimeError("the LU mode of a captured plan is fixed")
+        self.lu, self.mode = lu, LU_MODE[lu]
 
     def capture(self):
         """Capture assembly -> FP32 copy -> tensor-core LU as a CUDA graph (in the library,
@@ -212,10 +223,10 @@ class SolveServer:
         self._free = {}               # plan key -> [free BucketPlan], most recently used last
         self._lru = []                # free plans, least recently used first
         self._busy = [False] * slots
-        self._tuned = {}              # (kernel kind, bucket) -> "tf32" | "bf16"
+        self._tuned = {}              # (kernel kind, bucket) -> LU mode name, e.g. "tf32:256"
         self._closed = False
         self.stats = {"graph_replays": 0, "eager_factors": 0, "captures": 0, "capture_errors": [], "plans_built": 0,
-                      "plans_evicted": 0}
+                      "plans_evicted": 0, "tuned": {}}
         self._dev = self._device()
         self._threads = [threading.Thread(target=self._worker, args=(s,), daemon=True) for s in range(slots)]
         for t in self._threads:
@@ -355,20 +366,8 @@ class SolveServer:
             torch.as_tensor(np.asarray(req.eps, dtype=np.float64)).to(dev)
         if plan is None:
             lu = self._lu_for(req, b)
-            if lu is None:  # autotune this bucket: time TF32 and BF16, keep the faster that converges
-                best = None
-                for mode in ("tf32", "bf16"):
-                    p = BucketPlan(req.kernel, b, req.mu, mode, stream)
-                    stream.synchronize()  # only this slot's stream: another slot may be capturing a graph
-                    t0 = time.perf_counter()
-                    p.factor(X, e)
-                    x, it, outer, resid = p.solve(U, self.rtol)
-                    stream.synchronize()
-                    dt = time.perf_counter() - t0
-                    if resid <= self.rtol and (best is None or dt < best[0]):
-                        best = (dt, mode)
-                    del p
-                lu = best[1] if best else "tf32"
+            if lu is None:  # autotune this bucket (precision x tile width), keep the fastest that converges
+                lu = self._autotune(req, b, stream, X, e, U)
                 with self._cv:
                     self._tuned[(kernel_params(req.kernel)[0], b)] = lu
             plan = BucketPlan(req.kernel, b, req.mu, lu, stream)
@@ -389,6 +388,30 @@ class SolveServer:
         # resid: the refinement's last ||U - K F|| / ||U|| with the FP64 K (padding rows are identity
         # with zero right-hand side, so this is the residual of the unpadded system)
         return Result(F.cpu().numpy(), resid, 0, 0, 0, slot, b, plan.lu, outer), plan
+
+    def _autotune(self, req, b, stream, X, e, U):
+        """Time factor + solve of this request for every candidate LU mode on one eager plan
+        (one untimed run each first); the fastest whose residual meets rtol wins."""
+        p = BucketPlan(req.kernel, b, req.mu, "tf32", stream)
+        best = None
+        for lu in TUNE_CANDIDATES:
+            p.set_lu(lu)
+            dt = math.inf
+            for rep in range(2):
+                stream.synchronize()  # only this slot's stream: another slot may be capturing a graph
+                t0 = time.perf_counter()
+                p.factor(X, e)
+                x, it, outer, resid = p.solve(U, self.rtol)
+                stream.synchronize()
+                if rep:
+                    dt = time.perf_counter() - t0
+            if resid <= self.rtol and (best is None or dt < best[0]):
+                best = (dt, lu)
+        del p
+        lu = best[1] if best else "tf32"
+        with self._cv:
+            self.stats["tuned"][f"{kernel_params(req.kernel)[0]}:{b}"] = lu
+        return lu
 
     def _swimmer(self, stream, req):
         from .swimming import swimming_problem

@@ -64,6 +64,11 @@ extern "C" {
 #define FLG_LU_TF32 0     /* tcgen05 kind::tf32, FP32 accumulate in TMEM     */
 #define FLG_LU_BF16 1     /* tcgen05 kind::f16 (bf16 operands), FP32 accum   */
 #define FLG_LU_FP32 2     /* FP32 CUDA cores (no tensor cores)               */
+/* Optional tile-width bits OR-ed into a tensor-core LU mode: the trailing
+ * updates run on 128 x 128 or 128 x 256 output tiles.  Without either bit the
+ * width is chosen per update from its shape and the SM count. */
+#define FLG_LU_TILE_N128 0x100
+#define FLG_LU_TILE_N256 0x200
 
 /* ---- library ------------------------------------------------------------ */
 int flg_version(void);                          /* major*10000 + minor*100 + patch */
@@ -195,6 +200,8 @@ int flg_lu_solve_f64(int64_t n, int64_t nrhs, const double *LU, int64_t ld, cons
  * FLG_LU_TF32 or FLG_LU_BF16 the panels (TF32) and the trailing updates (the
  * mode's type; rank 128 inside 512-column outer panels, rank 512 for the rest)
  * run on the tcgen05 tensor cores; FLG_LU_FP32 uses CUDA cores throughout.
+ * A tensor-core mode may carry FLG_LU_TILE_N128 or FLG_LU_TILE_N256 (the tile
+ * width of the trailing updates; the workspace does not depend on it).
  * dinv (FP32, size flg_lu_lowp_dinv_elems(n)) receives the inverses of the
  * diagonal blocks of L and U, used by flg_lu_solve_lowp.  Only used as a
  * preconditioner of FP64 GMRES iterative refinement, so accuracy is recovered
