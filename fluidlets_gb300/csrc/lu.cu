@@ -383,11 +383,14 @@ __global__ void trsv_update_kernel(const double *LU, int64_t ld, double *B, int6
 // One CTA (16 warps) factors the nb x nb diagonal block (nb <= 128, padded with
 // the identity to 128) in shared memory, in 32 x 32 sub-blocks, and builds the
 // inverses of its L and U factors alongside (they precondition the panels and
-// the solves).  With X = inv(L) and Y = inv(U) started at the identity, step s:
-//   warp 0:  D[s][s] = L_ss U_ss in registers (lane = row, pivot row by
-//            shuffles); the same eliminations applied to the identity give
-//            inv(L_ss) -> X[s][s] (Gauss-Jordan), and a backward sweep gives
-//            inv(U_ss) -> Y[s][s];
+// the solves).  With X = inv(L) and Y = inv(U) started at zero, step s:
+//   warp 0:  D[s][s] = L_ss U_ss (lane = row, the pivot row broadcast through
+//            shared memory); the same sweep solves Y[s][s] U_ss = I row by row
+//            with the broadcast pivot rows, and publishes each column of L_ss;
+//   warp 1:  X[s][s] = inv(L_ss) column by column (lane = column), following
+//            warp 0's published columns (bounded waits);
+//   warps on the two other schedulers: store the block row s - 1 of D and X and
+//            the block column s - 1 of Y, which no later step changes;
 //   stage 1: U panel D[s][t] = X[s][s] D[s][t], L panel D[t][s] = D[t][s] Y[s][s]
 //            (t > s); X[s][q] = X[s][s] X[s][q], Y[q][s] = Y[q][s] Y[s][s] (q < s);
 //   stage 2: D[t][u] -= D[t][s] D[s][u] (t, u > s);
@@ -397,26 +400,133 @@ __global__ void trsv_update_kernel(const double *LU, int64_t ld, double *B, int6
 // L = L_0 L_1 L_2 L_3, U = U_3 U_2 U_1 U_0.)  Every stage-1/2 product is a
 // 32 x 32 x 32 block product split into two warp tasks (16-row or 16-column
 // halves, 4 x 4 outputs per lane, float4 operand loads); the row stride kLD
-// keeps rows 16-byte aligned and the loads free of bank conflicts.
+// keeps rows 16-byte aligned.
 constexpr int kSB = 32;          // sub-block
 constexpr int kNS = kNB / kSB;   // sub-blocks per side (4)
 constexpr int kLD = kNB + 4;     // shared-memory row stride (floats)
 constexpr size_t kDiagSmem = 3 * (size_t)kNB * kLD * sizeof(float);
+constexpr int kPub = 4;                   // columns of L published per flag update
+constexpr long long kDiagSpin = 1LL << 22;  // bounded wait of warp 1 on warp 0
 
 __device__ __forceinline__ float *sblk(float *M, int i, int j) { return M + i * kSB * kLD + j * kSB; }
+__device__ __forceinline__ const float *sblk(const float *M, int i, int j) { return M + i * kSB * kLD + j * kSB; }
+
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+__device__ __forceinline__ int ld_volatile_s32(const int *p) { return *(const volatile int *)p; }
+
+// Warp 0: row-per-lane LU of P (pivot row through R) and, in the same sweep, Y = inv(U) by rows
+// (Y U = I solved left to right with the pivot rows already broadcast); publishes column j of L
+// (multipliers, zero on and above the diagonal) to Lc[j][0..32) for warp 1, kPub columns at a time.
+__device__ __forceinline__ void lu32_fused(float *P, float *Yb, float *R, float *Lc, int *flag, int flag0, int lane,
+                                           int row0, int nb, int64_t k0, int *info) {
+    float a[kSB], y[kSB];
+#pragma unroll
+    for (int c4 = 0; c4 < kSB; c4 += 4) {
+        const float4 v = *reinterpret_cast<const float4 *>(P + lane * kLD + c4);
+        a[c4] = v.x, a[c4 + 1] = v.y, a[c4 + 2] = v.z, a[c4 + 3] = v.w;
+        y[c4] = y[c4 + 1] = y[c4 + 2] = y[c4 + 3] = 0.0f;
+    }
+    unsigned bad = 0;
+#pragma unroll
+    for (int j = 0; j < kSB; j++) {
+        float *Rb = R + (j & 1) * kSB;
+        if (lane == j) {
+#pragma unroll
+            for (int c4 = j & ~3; c4 < kSB; c4 += 4)
+                *reinterpret_cast<float4 *>(Rb + c4) = make_float4(a[c4], a[c4 + 1], a[c4 + 2], a[c4 + 3]);
+        }
+        __syncwarp();
+        const float piv = Rb[j];
+        const bool ok = piv != 0.0f && isfinite(piv);
+        bad |= (ok || row0 + j >= nb) ? 0u : (1u << j);
+        const float rp = ok ? rcp_approx(piv) : 0.0f;
+        // Y row `lane`: y[j] = (delta - sum_{k<j} Y_k U_kj) / U_jj, then the later sums
+        const float yj = (((lane == j) ? 1.0f : 0.0f) - y[j]) * rp;
+        y[j] = yj;
+        const float l = lane > j ? a[j] * rp : 0.0f;
+        if (lane > j) a[j] = l;
+        Lc[j * kSB + lane] = l;
+#pragma unroll
+        for (int c4 = (j + 1) & ~3; c4 < kSB; c4 += 4) {
+            const float4 v = *reinterpret_cast<const float4 *>(Rb + c4);
+            const float u[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                if (c4 + q > j) {
+                    a[c4 + q] = fmaf(-l, u[q], a[c4 + q]);
+                    y[c4 + q] = fmaf(yj, u[q], y[c4 + q]);
+                }
+        }
+        if (j % kPub == kPub - 1) {
+            __syncwarp();
+            if (lane == 0) {
+                __threadfence_block();
+                *(volatile int *)flag = flag0 + j + 1;
+            }
+        }
+    }
+    if (bad && lane == 0) atomicCAS(info, 0, (int)(k0 + row0 + __ffs(bad)));
+#pragma unroll
+    for (int c4 = 0; c4 < kSB; c4 += 4) {
+        *reinterpret_cast<float4 *>(P + lane * kLD + c4) = make_float4(a[c4], a[c4 + 1], a[c4 + 2], a[c4 + 3]);
+        *reinterpret_cast<float4 *>(Yb + lane * kLD + c4) = make_float4(y[c4], y[c4 + 1], y[c4 + 2], y[c4 + 3]);
+    }
+}
+
+// Warp 1: X = inv(L) column `lane`, right-looking forward substitution over the published columns
+// of L (waits, bounded, for each group of kPub; on a timeout raises info[1] and stops).
+__device__ __forceinline__ void linv32_follow(const float *Lc, float *Xb, const int *flag, int flag0, int lane,
+                                              int *info) {
+    float x[kSB];
+#pragma unroll
+    for (int i = 0; i < kSB; i++) x[i] = (i == lane) ? 1.0f : 0.0f;
+    bool alive = true;
+#pragma unroll
+    for (int k = 0; k < kSB; k++) {
+        if (k % kPub == 0) {
+            long long it = 0;
+            while (alive && ld_volatile_s32(flag) < flag0 + k + kPub) {
+                if (++it > kDiagSpin) {
+                    if (lane == 0) atomicExch(info + 1, 1);
+                    alive = false;
+                }
+            }
+            __syncwarp();
+            __threadfence_block();
+        }
+#pragma unroll
+        for (int i4 = (k + 1) & ~3; i4 < kSB; i4 += 4) {
+            const float4 v = *reinterpret_cast<const float4 *>(Lc + k * kSB + i4);
+            if (i4 > k) x[i4] = fmaf(-v.x, x[k], x[i4]);
+            if (i4 + 1 > k) x[i4 + 1] = fmaf(-v.y, x[k], x[i4 + 1]);
+            if (i4 + 2 > k) x[i4 + 2] = fmaf(-v.z, x[k], x[i4 + 2]);
+            if (i4 + 3 > k) x[i4 + 3] = fmaf(-v.w, x[k], x[i4 + 3]);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < kSB; i++) Xb[i * kLD + lane] = x[i];
+}
 
 // One warp: C (=|-=) A B over k = 32, C of (128 / CG) rows x (4 CG) columns, 4 x 4
-// per lane.  C may alias A when CG = 8 (row halves read only their own rows of A)
-// or B when CG = 4 (column halves read only their own columns of B): all operands
-// are read before the first store.
+// per lane.  Lane group g = lane / CG owns rows g + G i (G = 32 / CG groups), so the
+// 16-byte A loads of one instruction fall in distinct bank groups (row stride kLD).
+// C may alias A when CG = 8 (row halves read only their own rows of A) or B when
+// CG = 4 (column halves read only their own columns of B): all operands are read
+// before the first store.
 template <int CG, bool SUB>
 __device__ __forceinline__ void warp_mm(const float *A, const float *B, float *C, int lane) {
-    const int r0 = (lane / CG) * 4, c0 = (lane % CG) * 4;
+    constexpr int G = 32 / CG;
+    const int g = lane / CG, c0 = (lane % CG) * 4;
     float acc[4][4];
 #pragma unroll
     for (int i = 0; i < 4; i++) {
         if (SUB) {
-            const float4 v = *reinterpret_cast<const float4 *>(C + (r0 + i) * kLD + c0);
+            const float4 v = *reinterpret_cast<const float4 *>(C + (g + G * i) * kLD + c0);
             acc[i][0] = v.x, acc[i][1] = v.y, acc[i][2] = v.z, acc[i][3] = v.w;
         } else {
 #pragma unroll
@@ -428,7 +538,7 @@ __device__ __forceinline__ void warp_mm(const float *A, const float *B, float *C
         float a[4][4], b[4][4];
 #pragma unroll
         for (int i = 0; i < 4; i++) {
-            const float4 v = *reinterpret_cast<const float4 *>(A + (r0 + i) * kLD + k);
+            const float4 v = *reinterpret_cast<const float4 *>(A + (g + G * i) * kLD + k);
             a[i][0] = SUB ? -v.x : v.x, a[i][1] = SUB ? -v.y : v.y, a[i][2] = SUB ? -v.z : v.z,
             a[i][3] = SUB ? -v.w : v.w;
             const float4 w = *reinterpret_cast<const float4 *>(B + (k + i) * kLD + c0);
@@ -444,88 +554,55 @@ __device__ __forceinline__ void warp_mm(const float *A, const float *B, float *C
     __syncwarp();
 #pragma unroll
     for (int i = 0; i < 4; i++)
-        *reinterpret_cast<float4 *>(C + (r0 + i) * kLD + c0) = make_float4(acc[i][0], acc[i][1], acc[i][2], acc[i][3]);
+        *reinterpret_cast<float4 *>(C + (g + G * i) * kLD + c0) =
+            make_float4(acc[i][0], acc[i][1], acc[i][2], acc[i][3]);
     __syncwarp();
 }
 
-__device__ __forceinline__ float rcp_approx(float x) {
-    float r;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-}
-
-// One warp factors the 32 x 32 block P in place without pivoting and writes
-// inv(L) to Xb, inv(U) to Yb; lane = column, the column in registers.  Step j:
-// lane j forms the multipliers l_i = a_ij / a_jj (i > j) and broadcasts them;
-// columns c > j subtract l_i a_jc, and the same eliminations applied to the
-// identity build inv(L) (Gauss-Jordan).  inv(U) by column-oriented back
-// substitution, lane c solving U y = e_c.  A zero or non-finite pivot of a
-// real (not padding) row records its 1-based global index in *info.  The
-// reciprocal is the hardware approximation (1 ulp): this factorization only
-// preconditions FP64 iterative refinement.
-__device__ __forceinline__ void warp_lu32(float *P, float *Xb, float *Yb, int lane, int row0, int nb, int64_t k0,
-                                          int *info) {
-    constexpr unsigned kAll = 0xffffffffu;
-    float a[kSB], x[kSB];
+// store the finished parts of step s: rows [32s, 32s + 32) of the factored block and of inv(L),
+// columns [32s, 32s + 32) of inv(U) (and the same rows of its transpose); threads t0 .. t0 + nt
+__device__ __forceinline__ void diag_store_step(int s, const float *D, const float *X, const float *Y, float *A,
+                                                int64_t ld, int64_t k0, int nb, bool v4, float *Linv, float *Uinv,
+                                                float *UinvT, int t, int nt) {
+    const int r0 = s * kSB;
+    for (int e = t; e < kSB * kNB / 4; e += nt) {  // 32 rows x 32 float4
+        const int r = r0 + (e >> 5), c4 = (e & 31) * 4;
+        const float4 d = *reinterpret_cast<const float4 *>(D + r * kLD + c4);
+        if (v4) {
+            *reinterpret_cast<float4 *>(A + (k0 + r) * ld + k0 + c4) = d;
+        } else if (r < nb) {
+            const float w[4] = {d.x, d.y, d.z, d.w};
 #pragma unroll
-    for (int i = 0; i < kSB; i++) {
-        a[i] = P[i * kLD + lane];
-        x[i] = (i == lane) ? 1.0f : 0.0f;
-    }
-#pragma unroll
-    for (int j = 0; j < kSB; j++) {
-        float rp = 0.0f;
-        if (lane == j) {
-            const float piv = a[j];
-            const bool ok = piv != 0.0f && isfinite(piv);
-            if (!ok && row0 + j < nb) atomicCAS(info, 0, (int)(k0 + row0 + j + 1));
-            rp = ok ? rcp_approx(piv) : 0.0f;
+            for (int q = 0; q < 4; q++)
+                if (c4 + q < nb) A[(k0 + r) * ld + k0 + c4 + q] = w[q];
         }
-        const float ujc = a[j];  // row j of U in column `lane` (for lane > j)
-        const float xjc = x[j];
-#pragma unroll
-        for (int i = 0; i < kSB; i++) {
-            if (i <= j) continue;
-            const float l = __shfl_sync(kAll, a[i] * rp, j);
-            if (lane == j) a[i] = l;
-            else if (lane > j) a[i] = fmaf(-l, ujc, a[i]);
-            x[i] = fmaf(-l, xjc, x[i]);
+        *reinterpret_cast<float4 *>(Linv + r * kNB + c4) = *reinterpret_cast<const float4 *>(X + r * kLD + c4);
+    }
+    for (int e = t; e < kNB * kSB / 4; e += nt) {  // 128 rows x 8 float4 of column block s
+        const int r = e >> 3, c4 = r0 + (e & 7) * 4;
+        *reinterpret_cast<float4 *>(Uinv + r * kNB + c4) = *reinterpret_cast<const float4 *>(Y + r * kLD + c4);
+    }
+    if (UinvT)
+        for (int e = t; e < kSB * kNB; e += nt) {  // rows r0 .. r0 + 32 of the transpose
+            const int c = r0 + (e >> 7), r = e & (kNB - 1);
+            UinvT[c * kNB + r] = Y[r * kLD + c];
         }
-    }
-    float y[kSB];
-#pragma unroll
-    for (int i = 0; i < kSB; i++) {
-        P[i * kLD + lane] = a[i];
-        Xb[i * kLD + lane] = x[i];
-        y[i] = (i == lane) ? 1.0f : 0.0f;
-    }
-#pragma unroll
-    for (int i = kSB - 1; i >= 0; i--) {
-        const float piv = __shfl_sync(kAll, a[i], i);  // U[i][i]
-        const float rp = (piv != 0.0f && isfinite(piv)) ? rcp_approx(piv) : 0.0f;
-        y[i] *= rp;
-#pragma unroll
-        for (int k = 0; k < kSB; k++) {
-            if (k >= i) continue;
-            y[k] = fmaf(-__shfl_sync(kAll, a[k], i), y[i], y[k]);  // U[k][i]
-        }
-    }
-#pragma unroll
-    for (int i = 0; i < kSB; i++) Yb[i * kLD + lane] = y[i];
 }
 
 __global__ void __launch_bounds__(512) diag_lowp_kernel(float *A, int64_t ld, int64_t k0, int nb, float *Linv,
                                                         float *Uinv, float *UinvT, int *info) {
     extern __shared__ __align__(16) float sm[];
     float *D = sm, *X = sm + kNB * kLD, *Y = sm + 2 * kNB * kLD;
+    __shared__ __align__(16) float R[2 * kSB], Lc[kSB * kSB];
+    __shared__ int flag;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, nthr = blockDim.x, nwarp = nthr >> 5;
-    // 16-byte rows when the block is whole and aligned (ld % 4 == 0 is required by the caller)
+    if (tid == 0) flag = 0;
     const bool v4 = nb == kNB && (((uintptr_t)(A + k0 * ld + k0)) & 15) == 0;
     {
         const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
         float4 buf[8];
 #pragma unroll
-        for (int u = 0; u < 8; u++) {  // 4096 float4 = 128 x 128, eight per thread
+        for (int u = 0; u < 8; u++) {
             const int e = tid + u * 512, r = e >> 5, c4 = (e & 31) * 4;
             if (v4) {
                 buf[u] = __ldg(reinterpret_cast<const float4 *>(A + (k0 + r) * ld + k0 + c4));
@@ -549,16 +626,22 @@ __global__ void __launch_bounds__(512) diag_lowp_kernel(float *A, int64_t ld, in
     }
     __syncthreads();
     for (int s = 0; s < kNS; s++) {
-        const int m = kNS - 1 - s;  // sub-blocks after s
-        if (warp == 0) warp_lu32(sblk(D, s, s), sblk(X, s, s), sblk(Y, s, s), lane, s * kSB, nb, k0, info);
+        const int m = kNS - 1 - s;
+        if (warp == 0) {
+            lu32_fused(sblk(D, s, s), sblk(Y, s, s), R, Lc, &flag, s * kSB, lane, s * kSB, nb, k0, info);
+        } else if (warp == 1) {
+            linv32_follow(Lc, sblk(X, s, s), &flag, s * kSB, lane, info);
+        } else if (s > 0 && (warp & 3) >= 2) {  // warps on the other two schedulers store step s - 1
+            const int t = (warp >> 2) * 64 + (warp & 1) * 32 + lane;
+            diag_store_step(s - 1, D, X, Y, A, ld, k0, nb, v4, Linv, Uinv, UinvT, t, 256);
+        }
         __syncthreads();
-        // stage 1: 2m + 2s block products, two half tasks each
         for (int t = warp; t < 2 * (2 * m + 2 * s); t += nwarp) {
             const int b = t >> 1, h = (t & 1) * 16;
-            if (b < m) {  // U panel, C = B: column halves
+            if (b < m) {
                 float *C = sblk(D, s, s + 1 + b) + h;
                 warp_mm<4, false>(sblk(X, s, s), C, C, lane);
-            } else if (b < 2 * m) {  // L panel, C = A: row halves
+            } else if (b < 2 * m) {
                 float *C = sblk(D, s + 1 + (b - m), s) + h * kLD;
                 warp_mm<8, false>(C, sblk(Y, s, s), C, lane);
             } else if (b < 2 * m + s) {
@@ -570,43 +653,26 @@ __global__ void __launch_bounds__(512) diag_lowp_kernel(float *A, int64_t ld, in
             }
         }
         __syncthreads();
-        // stage 2: m^2 + 2 m (s + 1) block updates, row halves
         const int nD = m * m, nX = m * (s + 1);
         for (int t = warp; t < 2 * (nD + 2 * nX); t += nwarp) {
             const int b = t >> 1, h = (t & 1) * 16;
             if (b < nD) {
                 const int i = b / m, j = b - (b / m) * m;
                 warp_mm<8, true>(sblk(D, s + 1 + i, s) + h * kLD, sblk(D, s, s + 1 + j),
-                                 sblk(D, s + 1 + i, s + 1 + j) + h * kLD, lane);
+                                   sblk(D, s + 1 + i, s + 1 + j) + h * kLD, lane);
             } else if (b < nD + nX) {
                 const int i = (b - nD) / (s + 1), q = (b - nD) % (s + 1);
                 warp_mm<8, true>(sblk(D, s + 1 + i, s) + h * kLD, sblk(X, s, q), sblk(X, s + 1 + i, q) + h * kLD,
-                                 lane);
+                                   lane);
             } else {
                 const int q = (b - nD - nX) / m, j = (b - nD - nX) % m;
                 warp_mm<8, true>(sblk(Y, q, s) + h * kLD, sblk(D, s, s + 1 + j), sblk(Y, q, s + 1 + j) + h * kLD,
-                                 lane);
+                                   lane);
             }
         }
         __syncthreads();
     }
-#pragma unroll 2
-    for (int u = 0; u < 8; u++) {
-        const int e = tid + u * 512, r = e >> 5, c4 = (e & 31) * 4;
-        const float4 d = *reinterpret_cast<const float4 *>(D + r * kLD + c4);
-        if (v4) {
-            *reinterpret_cast<float4 *>(A + (k0 + r) * ld + k0 + c4) = d;
-        } else if (r < nb) {
-            const float w[4] = {d.x, d.y, d.z, d.w};
-#pragma unroll
-            for (int q = 0; q < 4; q++)
-                if (c4 + q < nb) A[(k0 + r) * ld + k0 + c4 + q] = w[q];
-        }
-        *reinterpret_cast<float4 *>(Linv + r * kNB + c4) = *reinterpret_cast<const float4 *>(X + r * kLD + c4);
-        *reinterpret_cast<float4 *>(Uinv + r * kNB + c4) = *reinterpret_cast<const float4 *>(Y + r * kLD + c4);
-    }
-    if (UinvT)  // the transposed copy: the K-major operand of the tensor-core L panel
-        for (int e = tid; e < kNB * kNB; e += nthr) UinvT[e] = Y[(e & (kNB - 1)) * kLD + (e >> 7)];
+    diag_store_step(kNS - 1, D, X, Y, A, ld, k0, nb, v4, Linv, Uinv, UinvT, tid, nthr);
 }
 
 // Panels of one LU step, in place, in one launch (CTA x < ntu: U tiles, else L tiles):
@@ -1360,7 +1426,7 @@ extern "C" int flg_lu_factor_lowp(int64_t n, float *A, int64_t ld, int mode, flo
     FLG_CUDA(cudaMemcpyAsync(hflags, flags, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
     FLG_CUDA(cudaStreamSynchronize(st));
     if (hflags[1]) {
-        set_error("tensor-core update: an mbarrier wait timed out");
+        set_error("a bounded device wait timed out (tensor-core update or diagonal block)");
         return FLG_ERR_CUDA;
     }
     *info = hflags[0];

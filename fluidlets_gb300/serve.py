@@ -183,7 +183,7 @@ class BucketPlan:
         self.x.zero_()
         flags = self.flags.cpu()
         if int(flags[1]):
-            raise RuntimeError("tensor-core update: an mbarrier wait timed out")
+            raise RuntimeError("low-precision LU: a bounded device wait timed out")
         if int(flags[0]):
             raise np.linalg.LinAlgError(f"zero pivot at row {int(flags[0]) - 1} in the low-precision LU")
         nbytes = L.flg_gmres_ir_dense_workspace(self.n, restart)

@@ -147,7 +147,7 @@ class SwimmerPlan:
             if int(fl[2]):
                 raise ValueError("nearest indices must lie in [0, n_force)")
             if int(fl[1]):
-                raise RuntimeError("tensor-core update: an mbarrier wait timed out")
+                raise RuntimeError("low-precision LU: a bounded device wait timed out")
             if int(fl[0]):
                 raise np.linalg.LinAlgError(f"zero or non-finite pivot at row {int(fl[0]) - 1} in the low-precision LU")
             sol, *_ = _gmres_ir_dense_dev(self.A, self.K32, self.ld32, self.dinv, b, rtol * 1e-2, 60, 200,

@@ -214,7 +214,8 @@ int flg_lu_factor_lowp(int64_t n, float *A, int64_t ld, int mode, float *dinv, i
 /* The same factorization without any host synchronization (so it can be
  * captured in a CUDA graph): the pivot / timeout flags are written to the
  * device array flags[2] (flags[0] = 1 + first bad pivot row, flags[1] = 1 if
- * a tensor-core wait timed out) for the caller to check after the stream. */
+ * a bounded device wait -- tensor-core pipeline or diagonal-block warps --
+ * timed out) for the caller to check after the stream. */
 int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mode, float *dinv, int *flags,
                              void *work, size_t work_bytes, void *stream);
 /* x = (L U)^{-1} b in FP32 for one FP64 right-hand side (converted on the
