@@ -389,13 +389,15 @@ __global__ void trsv_update_kernel(const double *LU, int64_t ld, double *B, int6
 //            with the broadcast pivot rows, and publishes each column of L_ss;
 //   warp 1:  X[s][s] = inv(L_ss) column by column (lane = column), following
 //            warp 0's published columns (bounded waits);
-//   warps on the two other schedulers: store the block row s - 1 of D and X and
-//            the block column s - 1 of Y, which no later step changes;
 //   stage 1: U panel D[s][t] = X[s][s] D[s][t], L panel D[t][s] = D[t][s] Y[s][s]
 //            (t > s); X[s][q] = X[s][s] X[s][q], Y[q][s] = Y[q][s] Y[s][s] (q < s);
 //   stage 2: D[t][u] -= D[t][s] D[s][u] (t, u > s);
 //            X[t][q] -= D[t][s] X[s][q] (t > s, q <= s);
 //            Y[q][u] -= Y[q][s] D[s][u] (q <= s, u > s).
+// Stage 2 looks ahead: warps 0 and 1 update D[s+1][s+1] alone and go on to step
+// s + 1, while the 8 warps of the two other schedulers do the rest of stage 2 and
+// store the block row s of D and X and the block column s of Y (no later step
+// changes them).
 // (X <- inv(L_s) X and Y <- Y inv(U_s) for the block-column / block-row factors
 // L = L_0 L_1 L_2 L_3, U = U_3 U_2 U_1 U_0.)  Every stage-1/2 product is a
 // 32 x 32 x 32 block product split into two warp tasks (16-row or 16-column
@@ -627,14 +629,9 @@ __global__ void __launch_bounds__(512) diag_lowp_kernel(float *A, int64_t ld, in
     __syncthreads();
     for (int s = 0; s < kNS; s++) {
         const int m = kNS - 1 - s;
-        if (warp == 0) {
-            lu32_fused(sblk(D, s, s), sblk(Y, s, s), R, Lc, &flag, s * kSB, lane, s * kSB, nb, k0, info);
-        } else if (warp == 1) {
-            linv32_follow(Lc, sblk(X, s, s), &flag, s * kSB, lane, info);
-        } else if (s > 0 && (warp & 3) >= 2) {  // warps on the other two schedulers store step s - 1
-            const int t = (warp >> 2) * 64 + (warp & 1) * 32 + lane;
-            diag_store_step(s - 1, D, X, Y, A, ld, k0, nb, v4, Linv, Uinv, UinvT, t, 256);
-        }
+        // factor D[s][s] (warp 0) and invert L_ss (warp 1); the other warps finish stage 2 of s - 1
+        if (warp == 0) lu32_fused(sblk(D, s, s), sblk(Y, s, s), R, Lc, &flag, s * kSB, lane, s * kSB, nb, k0, info);
+        else if (warp == 1) linv32_follow(Lc, sblk(X, s, s), &flag, s * kSB, lane, info);
         __syncthreads();
         for (int t = warp; t < 2 * (2 * m + 2 * s); t += nwarp) {
             const int b = t >> 1, h = (t & 1) * 16;
@@ -653,24 +650,36 @@ __global__ void __launch_bounds__(512) diag_lowp_kernel(float *A, int64_t ld, in
             }
         }
         __syncthreads();
-        const int nD = m * m, nX = m * (s + 1);
-        for (int t = warp; t < 2 * (nD + 2 * nX); t += nwarp) {
-            const int b = t >> 1, h = (t & 1) * 16;
-            if (b < nD) {
-                const int i = b / m, j = b - (b / m) * m;
-                warp_mm<8, true>(sblk(D, s + 1 + i, s) + h * kLD, sblk(D, s, s + 1 + j),
-                                   sblk(D, s + 1 + i, s + 1 + j) + h * kLD, lane);
-            } else if (b < nD + nX) {
-                const int i = (b - nD) / (s + 1), q = (b - nD) % (s + 1);
-                warp_mm<8, true>(sblk(D, s + 1 + i, s) + h * kLD, sblk(X, s, q), sblk(X, s + 1 + i, q) + h * kLD,
-                                   lane);
-            } else {
-                const int q = (b - nD - nX) / m, j = (b - nD - nX) % m;
-                warp_mm<8, true>(sblk(Y, q, s) + h * kLD, sblk(D, s, s + 1 + j), sblk(Y, q, s + 1 + j) + h * kLD,
-                                   lane);
+        if (m == 0) break;
+        if (warp < 2) {
+            // look-ahead: the block the next factorization needs, D[s+1][s+1] -= D[s+1][s] D[s][s+1],
+            // then on to step s + 1 while the other warps finish stage 2
+            warp_mm<8, true>(sblk(D, s + 1, s) + warp * 16 * kLD, sblk(D, s, s + 1),
+                             sblk(D, s + 1, s + 1) + warp * 16 * kLD, lane);
+            asm volatile("bar.sync 1, 64;" ::: "memory");
+        } else if ((warp & 3) >= 2) {
+            // the rest of stage 2 (m^2 - 1 blocks of D, m (s + 1) of X and of Y), then the stores of
+            // step s, on the 8 warps of the two schedulers that warps 0 and 1 do not use
+            const int w8 = (warp >> 2) * 2 + (warp & 1);
+            const int nD = m * m - 1, nX = m * (s + 1);
+            for (int t = w8; t < 2 * (nD + 2 * nX); t += 8) {
+                const int b = t >> 1, h = (t & 1) * 16;
+                if (b < nD) {
+                    const int i = (b + 1) / m, j = (b + 1) - ((b + 1) / m) * m;
+                    warp_mm<8, true>(sblk(D, s + 1 + i, s) + h * kLD, sblk(D, s, s + 1 + j),
+                                     sblk(D, s + 1 + i, s + 1 + j) + h * kLD, lane);
+                } else if (b < nD + nX) {
+                    const int i = (b - nD) / (s + 1), q = (b - nD) % (s + 1);
+                    warp_mm<8, true>(sblk(D, s + 1 + i, s) + h * kLD, sblk(X, s, q), sblk(X, s + 1 + i, q) + h * kLD,
+                                     lane);
+                } else {
+                    const int q = (b - nD - nX) / m, j = (b - nD - nX) % m;
+                    warp_mm<8, true>(sblk(Y, q, s) + h * kLD, sblk(D, s, s + 1 + j), sblk(Y, q, s + 1 + j) + h * kLD,
+                                     lane);
+                }
             }
+            diag_store_step(s, D, X, Y, A, ld, k0, nb, v4, Linv, Uinv, UinvT, w8 * 32 + lane, 256);
         }
-        __syncthreads();
     }
     diag_store_step(kNS - 1, D, X, Y, A, ld, k0, nb, v4, Linv, Uinv, UinvT, tid, nthr);
 }
