@@ -12,6 +12,10 @@
 // multi-vector dot products and two multi-vector updates on the device and
 // a single device-to-host copy of the new Hessenberg column.
 //
+// The iterative refinements (mixed-precision flg_gmres, flg_gmres_ir_dense)
+// pass their inner solves the known ||r|| and a zero start, which saves three
+// host round trips per inner solve without changing the arithmetic.
+//
 // Dot products are deterministic: fixed chunking, per-chunk block
 // reductions, then an in-order sum of the chunk partials.
 #include <algorithm>
@@ -222,8 +226,9 @@ struct Gmres {
     }
 
     // r = b - A x, or r = b without the operator when x is all zeros (the start of an
-    // iterative refinement; the FP64 kernel sum that would give A 0 costs a full matvec)
-    int residual_from(const T *b, const T *x) {
+    // iterative refinement; the FP64 kernel sum that would give A 0 costs a full matvec);
+    // *is_b tells which
+    int residual_from(const T *b, const T *x, bool *is_b) {
         int nz = 0;
         FLG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
         any_nonzero_kernel<<<grid(n * (S<T>::complex ? 2 : 1)), 256, 0, st>>>((const double *)x,
@@ -231,6 +236,7 @@ struct Gmres {
         FLG_LAUNCH_CHECK();
         FLG_CUDA(cudaMemcpyAsync(&nz, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
         FLG_CUDA(cudaStreamSynchronize(st));
+        *is_b = nz == 0;
         if (nz) return residual(b, x);
         FLG_CUDA(cudaMemcpyAsync(r, b, sizeof(T) * n, cudaMemcpyDeviceToDevice, st));
         return FLG_OK;
@@ -273,12 +279,115 @@ struct Gmres {
         }
     }
 
+    // host side of one restart cycle: Hessenberg, Givens rotations, least-squares solution
+    struct Scratch {
+        std::vector<H> h, S_, y, gs;
+        std::vector<double> gc;
+        std::vector<T> hbuf;
+        explicit Scratch(int m)
+            : h((size_t)m * (m + 1)), S_(m + 1), y(m + 1), gs(m), gc(m), hbuf(2 * (m + 2) + 2) {}
+    };
+
+    // One restart cycle from V[0] = v / beta (V[0] holds v on entry): Arnoldi with two
+    // classical Gram-Schmidt passes and Givens rotations until the estimated residual
+    // presid <= ptol, a breakdown, or m columns; then x += V y.  iters += columns.
+    int cycle(T *x, double beta, double ptol, int &iters, double &presid, bool &breakdown, Scratch &hs) {
+        const double eps = 2.220446049250313e-16;
+        std::vector<H> &h = hs.h, &S_ = hs.S_, &y = hs.y, &gs = hs.gs;
+        std::vector<double> &gc = hs.gc;
+        std::vector<T> &hbuf = hs.hbuf;
+        scale_kernel<T><<<grid(n), 256, 0, st>>>(V, n, 1.0 / beta);
+        FLG_LAUNCH_CHECK();
+        std::fill(S_.begin(), S_.end(), H(0.0));
+        S_[0] = beta;
+        breakdown = false;
+        int col = 0;
+        for (col = 0; col < m; col++) {
+            T *w = V + (int64_t)(col + 1) * n;
+            FLG_TRY(apply(V + (int64_t)col * n, w));
+            // device: [h1 (col+1) | h2 (col+1) | |w|^2 before | |w|^2 after]
+            T *h1d = hdev, *h2d = hdev + (col + 1), *nb = hdev + 2 * (col + 1), *na = nb + 1;
+            FLG_TRY(dots(w, 1, w, nb));
+            FLG_TRY(dots(V, col + 1, w, h1d));
+            gemv_sub_kernel<T><<<grid(n), 256, 0, st>>>(V, n, col + 1, h1d, w, n);
+            FLG_LAUNCH_CHECK();
+            FLG_TRY(dots(V, col + 1, w, h2d));
+            gemv_sub_kernel<T><<<grid(n), 256, 0, st>>>(V, n, col + 1, h2d, w, n);
+            FLG_LAUNCH_CHECK();
+            FLG_TRY(dots(w, 1, w, na));
+            FLG_CUDA(cudaMemcpyAsync(hbuf.data(), hdev, sizeof(T) * (2 * (col + 1) + 2), cudaMemcpyDeviceToHost,
+                                     st));
+            FLG_CUDA(cudaStreamSynchronize(st));
+            H *hc = &h[(size_t)col * (m + 1)];
+            for (int k = 0; k <= col; k++) hc[k] = S<T>::to_h(hbuf[k]) + S<T>::to_h(hbuf[col + 1 + k]);
+            double h0, h1n;
+            if constexpr (S<T>::complex) {
+                h0 = std::sqrt(std::max(hbuf[2 * (col + 1)].x, 0.0));
+                h1n = std::sqrt(std::max(hbuf[2 * (col + 1) + 1].x, 0.0));
+            } else {
+                h0 = std::sqrt(std::max(hbuf[2 * (col + 1)], 0.0));
+                h1n = std::sqrt(std::max(hbuf[2 * (col + 1) + 1], 0.0));
+            }
+            hc[col + 1] = h1n;
+            if (h1n <= eps * h0) {
+                hc[col + 1] = 0.0;
+                breakdown = true;
+            } else {
+                scale_kernel<T><<<grid(n), 256, 0, st>>>(w, n, 1.0 / h1n);
+                FLG_LAUNCH_CHECK();
+            }
+            for (int k = 0; k < col; k++) {
+                const double c = gc[k];
+                const H s = gs[k];
+                const H n0 = hc[k], n1 = hc[k + 1];
+                hc[k] = c * n0 + s * n1;
+                if constexpr (S<T>::complex) hc[k + 1] = -std::conj(s) * n0 + c * n1;
+                else hc[k + 1] = -s * n0 + c * n1;
+            }
+            double c;
+            H s, mag;
+            lartg(hc[col], hc[col + 1], c, s, mag);
+            gc[col] = c;
+            gs[col] = s;
+            hc[col] = mag;
+            hc[col + 1] = 0.0;
+            H t;
+            if constexpr (S<T>::complex) t = -std::conj(s) * S_[col];
+            else t = -s * S_[col];
+            S_[col] = c * S_[col];
+            S_[col + 1] = t;
+            presid = std::abs(t);
+            iters++;
+            if (presid <= ptol || breakdown) break;
+        }
+        if (col == m) col = m - 1;
+        // back substitution on the (col+1) x (col+1) upper triangle
+        if (h[(size_t)col * (m + 1) + col] == H(0.0)) S_[col] = 0.0;
+        for (int k = 0; k <= col; k++) y[k] = S_[k];
+        for (int k = col; k > 0; k--) {
+            if (y[k] != H(0.0)) {
+                y[k] /= h[(size_t)k * (m + 1) + k];
+                const H tk = y[k];
+                for (int q = 0; q < k; q++) y[q] -= tk * h[(size_t)k * (m + 1) + q];
+            }
+        }
+        if (y[0] != H(0.0)) y[0] /= h[0];
+        for (int k = 0; k <= col; k++) hbuf[k] = S<T>::from_h(y[k]);
+        FLG_CUDA(cudaMemcpyAsync(hdev, hbuf.data(), sizeof(T) * (col + 1), cudaMemcpyHostToDevice, st));
+        gemv_add_kernel<T><<<grid(n), 256, 0, st>>>(V, n, col + 1, hdev, x, n);
+        FLG_LAUNCH_CHECK();
+        return FLG_OK;
+    }
+
     // SciPy gmres on A x = b from the given x (x overwritten); iters += inner iterations.
     // Returns FLG_OK (converged), FLG_ERR_NOT_CONVERGED (maxiter cycles), or an error.
-    int solve(const T *b, T *x, double rtol, int maxiter, int &iters, double &rnorm_out) {
+    // A caller that knows ||b|| (bnorm >= 0) and that x is zero (x_zero) saves the host
+    // round trips that would find them out; the arithmetic is the same.
+    int solve(const T *b, T *x, double rtol, int maxiter, int &iters, double &rnorm_out, double bnorm = -1.0,
+              bool x_zero = false) {
         const double eps = 2.220446049250313e-16;
-        double bnrm2;
-        FLG_TRY(norm(b, &bnrm2));
+        double bnrm2 = bnorm;
+        if (bnrm2 < 0.0) FLG_TRY(norm(b, &bnrm2));
         if (bnrm2 == 0.0) {
             FLG_CUDA(cudaMemcpyAsync(x, b, sizeof(T) * n, cudaMemcpyDeviceToDevice, st));
             rnorm_out = 0.0;
@@ -293,28 +402,27 @@ struct Gmres {
         double ptol_max_factor = 1.0;
         double ptol = Mb_nrm2 * std::min(ptol_max_factor, atol / bnrm2);
         double presid = 0.0, rnorm = 0.0;
-        std::vector<H> h((size_t)m * (m + 1)), S_(m + 1), y(m + 1);
-        std::vector<double> gc(m);
-        std::vector<H> gs(m);
-        std::vector<T> hbuf(2 * (m + 2) + 2);
+        Scratch hs(m);
         bool have_r = false, r_is_b = false;
         for (int it = 0; it < maxiter; it++) {
             if (it == 0) {
                 int nz = 0;
-                FLG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
-                any_nonzero_kernel<<<grid(n * (S<T>::complex ? 2 : 1)), 256, 0, st>>>(
-                    (const double *)x, n * (S<T>::complex ? 2 : 1), flag);
-                FLG_LAUNCH_CHECK();
-                FLG_CUDA(cudaMemcpyAsync(&nz, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
-                FLG_CUDA(cudaStreamSynchronize(st));
+                if (!x_zero) {
+                    FLG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
+                    any_nonzero_kernel<<<grid(n * (S<T>::complex ? 2 : 1)), 256, 0, st>>>(
+                        (const double *)x, n * (S<T>::complex ? 2 : 1), flag);
+                    FLG_LAUNCH_CHECK();
+                    FLG_CUDA(cudaMemcpyAsync(&nz, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+                    FLG_CUDA(cudaStreamSynchronize(st));
+                }
                 if (nz) {
                     FLG_TRY(residual(b, x));
                 } else {
                     FLG_CUDA(cudaMemcpyAsync(r, b, sizeof(T) * n, cudaMemcpyDeviceToDevice, st));
                     r_is_b = true;
                 }
-                double rn0;
-                FLG_TRY(norm(r, &rn0));
+                double rn0 = bnrm2;  // r == b
+                if (!r_is_b) FLG_TRY(norm(r, &rn0));
                 if (rn0 < atol) {
                     rnorm_out = rn0;
                     return FLG_OK;
@@ -334,86 +442,8 @@ struct Gmres {
                 rnorm = 0.0;
                 break;
             }
-            scale_kernel<T><<<grid(n), 256, 0, st>>>(V, n, 1.0 / tmpn);
-            FLG_LAUNCH_CHECK();
-            std::fill(S_.begin(), S_.end(), H(0.0));
-            S_[0] = tmpn;
             bool breakdown = false;
-            int col = 0;
-            for (col = 0; col < m; col++) {
-                T *w = V + (int64_t)(col + 1) * n;
-                FLG_TRY(apply(V + (int64_t)col * n, w));
-                // device: [h1 (col+1) | h2 (col+1) | |w|^2 before | |w|^2 after]
-                T *h1d = hdev, *h2d = hdev + (col + 1), *nb = hdev + 2 * (col + 1), *na = nb + 1;
-                FLG_TRY(dots(w, 1, w, nb));
-                FLG_TRY(dots(V, col + 1, w, h1d));
-                gemv_sub_kernel<T><<<grid(n), 256, 0, st>>>(V, n, col + 1, h1d, w, n);
-                FLG_LAUNCH_CHECK();
-                FLG_TRY(dots(V, col + 1, w, h2d));
-                gemv_sub_kernel<T><<<grid(n), 256, 0, st>>>(V, n, col + 1, h2d, w, n);
-                FLG_LAUNCH_CHECK();
-                FLG_TRY(dots(w, 1, w, na));
-                FLG_CUDA(cudaMemcpyAsync(hbuf.data(), hdev, sizeof(T) * (2 * (col + 1) + 2), cudaMemcpyDeviceToHost,
-                                         st));
-                FLG_CUDA(cudaStreamSynchronize(st));
-                H *hc = &h[(size_t)col * (m + 1)];
-                for (int k = 0; k <= col; k++) hc[k] = S<T>::to_h(hbuf[k]) + S<T>::to_h(hbuf[col + 1 + k]);
-                double h0, h1n;
-                if constexpr (S<T>::complex) {
-                    h0 = std::sqrt(std::max(hbuf[2 * (col + 1)].x, 0.0));
-                    h1n = std::sqrt(std::max(hbuf[2 * (col + 1) + 1].x, 0.0));
-                } else {
-                    h0 = std::sqrt(std::max(hbuf[2 * (col + 1)], 0.0));
-                    h1n = std::sqrt(std::max(hbuf[2 * (col + 1) + 1], 0.0));
-                }
-                hc[col + 1] = h1n;
-                if (h1n <= eps * h0) {
-                    hc[col + 1] = 0.0;
-                    breakdown = true;
-                } else {
-                    scale_kernel<T><<<grid(n), 256, 0, st>>>(w, n, 1.0 / h1n);
-                    FLG_LAUNCH_CHECK();
-                }
-                for (int k = 0; k < col; k++) {
-                    const double c = gc[k];
-                    const H s = gs[k];
-                    const H n0 = hc[k], n1 = hc[k + 1];
-                    hc[k] = c * n0 + s * n1;
-                    if constexpr (S<T>::complex) hc[k + 1] = -std::conj(s) * n0 + c * n1;
-                    else hc[k + 1] = -s * n0 + c * n1;
-                }
-                double c;
-                H s, mag;
-                lartg(hc[col], hc[col + 1], c, s, mag);
-                gc[col] = c;
-                gs[col] = s;
-                hc[col] = mag;
-                hc[col + 1] = 0.0;
-                H t;
-                if constexpr (S<T>::complex) t = -std::conj(s) * S_[col];
-                else t = -s * S_[col];
-                S_[col] = c * S_[col];
-                S_[col + 1] = t;
-                presid = std::abs(t);
-                iters++;
-                if (presid <= ptol || breakdown) break;
-            }
-            if (col == m) col = m - 1;
-            // back substitution on the (col+1) x (col+1) upper triangle
-            if (h[(size_t)col * (m + 1) + col] == H(0.0)) S_[col] = 0.0;
-            for (int k = 0; k <= col; k++) y[k] = S_[k];
-            for (int k = col; k > 0; k--) {
-                if (y[k] != H(0.0)) {
-                    y[k] /= h[(size_t)k * (m + 1) + k];
-                    const H tk = y[k];
-                    for (int q = 0; q < k; q++) y[q] -= tk * h[(size_t)k * (m + 1) + q];
-                }
-            }
-            if (y[0] != H(0.0)) y[0] /= h[0];
-            for (int k = 0; k <= col; k++) hbuf[k] = S<T>::from_h(y[k]);
-            FLG_CUDA(cudaMemcpyAsync(hdev, hbuf.data(), sizeof(T) * (col + 1), cudaMemcpyHostToDevice, st));
-            gemv_add_kernel<T><<<grid(n), 256, 0, st>>>(V, n, col + 1, hdev, x, n);
-            FLG_LAUNCH_CHECK();
+            FLG_TRY(cycle(x, tmpn, ptol, iters, presid, breakdown, hs));
             FLG_TRY(residual(b, x));
             FLG_TRY(norm(r, &rnorm));
             if (rnorm <= atol) break;
@@ -520,8 +550,10 @@ static int gmres_run(int kind, double are, double aim, const double *X, const do
     double prev = INFINITY;
     int stall = 0;
     for (int o = 0; o <= max_outer; o++) {
-        FLG_TRY(o == 0 ? g.residual_from(b, x) : g.residual(b, x));
-        FLG_TRY(g.norm(g.r, &rn));
+        bool is_b = false;
+        FLG_TRY(o == 0 ? g.residual_from(b, x, &is_b) : g.residual(b, x));
+        if (is_b) rn = bn;
+        else FLG_TRY(g.norm(g.r, &rn));
         *resid = rn / bn;
         if (rn <= rtol * bn) return FLG_OK;
         if (o == max_outer || *iters >= restart * maxiter) break;
@@ -530,7 +562,7 @@ static int gmres_run(int kind, double are, double aim, const double *X, const do
         prev = rn;
         FLG_CUDA(cudaMemsetAsync(d, 0, sizeof(T) * n, st));
         double rin = 0.0;
-        int s2 = gi.solve(g.r, d, inner_rtol, std::max(1, maxiter), *iters, rin);
+        int s2 = gi.solve(g.r, d, inner_rtol, std::max(1, maxiter), *iters, rin, rn, true);
         if (s2 != FLG_OK && s2 != FLG_ERR_NOT_CONVERGED) return s2;
         add_kernel<T><<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(x, d, n);
         FLG_LAUNCH_CHECK();
@@ -634,8 +666,10 @@ extern "C" int flg_gmres_ir_dense(int64_t n, const double *A, int64_t ld, const 
     double rn = 0.0, prev = INFINITY;
     int stall = 0;
     for (int o = 0; o <= 60; o++) {
-        FLG_TRY(o == 0 ? g.residual_from(b, x) : g.residual(b, x));
-        FLG_TRY(g.norm(g.r, &rn));
+        bool is_b = false;
+        FLG_TRY(o == 0 ? g.residual_from(b, x, &is_b) : g.residual(b, x));
+        if (is_b) rn = bn;
+        else FLG_TRY(g.norm(g.r, &rn));
         *resid = rn / bn;
         if (rn <= rtol * bn) return FLG_OK;
         if (*iters >= restart * maxiter) break;
@@ -644,7 +678,7 @@ extern "C" int flg_gmres_ir_dense(int64_t n, const double *A, int64_t ld, const 
         prev = rn;
         FLG_CUDA(cudaMemsetAsync(d, 0, sizeof(double) * n, st));
         double rin;
-        int s2 = gi.solve(g.r, d, inner, maxiter, *iters, rin);
+        int s2 = gi.solve(g.r, d, inner, maxiter, *iters, rin, rn, true);
         if (s2 != FLG_OK && s2 != FLG_ERR_NOT_CONVERGED) return s2;
         add_kernel<double><<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(x, d, n);
         FLG_LAUNCH_CHECK();
