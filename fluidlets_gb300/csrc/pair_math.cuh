@@ -281,6 +281,7 @@ __device__ __forceinline__ void wall_apply(const WallGeo<T> &g, T f0, T f1, T f2
 struct WallFar {
     float d0, d1, dm, dp, cxy, cz, Z3, s5x3;
 };
+template <bool MASK = true>
 __device__ __forceinline__ WallFar wall_far_geo(float tx, float ty, float tz, float sx, float sy, float h, float e2,
                                                 float thr) {
     WallFar g;
@@ -293,7 +294,7 @@ __device__ __forceinline__ WallFar wall_far_geo(float tx, float ty, float tz, fl
     const float QI = fmaf(g.dp, g.dp, rq);
     const float sF = rsq(QF);
     float s = rsq(QI);
-    s = (QF < thr) ? 0.0f : s;
+    if (MASK) s = (QF < thr) ? 0.0f : s;  // (MASK false: the caller knows no pair of the tile is near)
     const float p = sF * s, q = sF + s;
     const float Z1 = (p * (p + p)) * rcp(q);
     g.Z3 = Z1 * fmaf(q, q, -p);

@@ -6,9 +6,13 @@
 //  FLG_PREC_FP64  sum_f64_kernel: one target per thread, sources staged in
 //                 shared memory in tiles of 128, FP64 arithmetic throughout.
 //  FLG_PREC_MIXED far_f32_kernel: TPT targets per thread, 256-source tiles of
-//                 packed FP32 sources (float4 x,y,z,eps^2 | f0,f1,f2,thr),
-//                 register-prefetched; pairs with r < 4 eps_j are masked out;
-//                 FP32 accumulation within a tile, FP64 across tiles.
+//                 packed FP32 sources (float4 x,y,z,eps^2 | f0,f1,f2,thr) in
+//                 cell order, register-prefetched; pairs with r < 4 eps_j are
+//                 masked out -- except in tiles whose bounding box lies
+//                 beyond every threshold from the box of the CTA's targets
+//                 (targets taken in cell order too, so that both boxes are
+//                 small), which run without the mask; FP32 accumulation
+//                 within a tile, FP64 across tiles.
 //                 near_f64_kernel: a uniform cell list (cell >= 4.2 max eps)
 //                 finds the masked pairs, which are summed in FP64 with the
 //                 same predicate, then the partial sums are combined.
@@ -32,6 +36,7 @@ constexpr int kF32Tile = 256;
 constexpr int kMaxCells = 1 << 20;
 constexpr int kBoundBlocks = 256;
 constexpr int kScanBlock = 1024;  // elements per scan block (one per thread)
+constexpr int64_t kSortTargetsMin = 32768;  // mixed sums bucket larger target sets by cell
 
 __host__ __device__ inline int out_width(int nf, bool ck) { return (nf == 2 || ck) ? 6 : 3; }
 
@@ -207,28 +212,30 @@ __global__ void finalize_kernel(FinalArgs a) {
 struct FarArgs {
     const double *tg;
     int64_t M;
+    const int *tperm;      // processing position -> target index (null: identity)
     const float4 *packed;  // [N][NQ]
+    const float4 *tile_box;  // [N / 256][2]
     int64_t N;
     int64_t split_len;
     float alpha_re, alpha_im;
-    double *partial;  // [S][M][OUTW]
+    double *partial;  // [S][M][OUTW], by processing position
 };
 
-template <int KIND, int NF, bool CK>
+template <int KIND, int NF, bool CK, bool MASK = true>
 __device__ __forceinline__ void pair_f32_far(float tx, float ty, float tz, float tz2, const float4 &p,
                                              const float4 &q, const float4 &r, float are, float aim, float *u) {
     // p = {x, y, z, e2}; q = {f0, f1, f2, thr}; r = {f0i, f1i, f2i, 0}
     if constexpr (KIND == FLG_WALL) {
         // strengths arrive scaled by the source height; the caller applies 2 t per tile
         (void)tz2;
-        const WallFar g = wall_far_geo(tx, ty, tz, p.x, p.y, p.z, p.w, q.w);
+        const WallFar g = wall_far_geo<MASK>(tx, ty, tz, p.x, p.y, p.z, p.w, q.w);
         wall_far_acc(g, q.x, q.y, q.z, u);
         if constexpr (NF == 2) wall_far_acc(g, r.x, r.y, r.z, u + 3);
     } else {
         float d0 = sub_rn(tx, p.x), d1 = sub_rn(ty, p.y), d2 = sub_rn(tz, p.z);
         float Q = free_Q_f32(d0, d1, d2, p.w);
         float s = rsq(Q);
-        s = (Q < q.w) ? 0.0f : s;  // near pair: summed in FP64 by near_f64_kernel
+        if (MASK) s = (Q < q.w) ? 0.0f : s;  // near pair: summed in FP64 by near_f64_kernel
         if constexpr (CK) {
             cpx<float> A, B;
             brink_AB_c<float>(s, Q, p.w, are, aim, A, B);
@@ -251,22 +258,59 @@ __device__ __forceinline__ void pair_f32_far(float tx, float ty, float tz, float
     }
 }
 
+// Code generation of the far-field kernel, measured on GB300 (all kernel kinds as fast or
+// faster than without them): at least 3 CTAs per SM (80 registers at most), and the
+// unmasked loop unrolled 4 deep.  0 CTAs leaves the register count to the compiler.
+#ifndef FLG_FAR_MINB
+#define FLG_FAR_MINB 3
+#endif
+#if FLG_FAR_MINB > 0
+#define FLG_FAR_BOUNDS __launch_bounds__(kF32Threads, FLG_FAR_MINB)
+#else
+#define FLG_FAR_BOUNDS __launch_bounds__(kF32Threads)
+#endif
+#ifndef FLG_FAR_UNROLL
+#define FLG_FAR_UNROLL 4
+#endif
+constexpr int kFarUnroll = FLG_FAR_UNROLL;
 template <int KIND, int NF, bool CK, int TPT>
-__global__ void __launch_bounds__(kF32Threads) far_f32_kernel(FarArgs a) {
+__global__ void FLG_FAR_BOUNDS far_f32_kernel(FarArgs a) {
     constexpr int NQ = 1 + NF;
     constexpr int OUTW = (NF == 2 || CK) ? 6 : 3;
     __shared__ float4 s_src[kF32Tile * NQ];
+    __shared__ float s_box[kF32Threads / 32][6];
     const int64_t base = (int64_t)blockIdx.x * (kF32Threads * TPT) + threadIdx.x;
     float tx[TPT], ty[TPT], tz[TPT], tz2[TPT];
+    float bl[3] = {INFINITY, INFINITY, INFINITY}, bh[3] = {-INFINITY, -INFINITY, -INFINITY};
 #pragma unroll
     for (int t = 0; t < TPT; t++) {
-        int64_t i = base + (int64_t)t * kF32Threads;
-        i = i < a.M ? i : a.M - 1;
+        int64_t k = base + (int64_t)t * kF32Threads;
+        k = k < a.M ? k : a.M - 1;
+        const int64_t i = a.tperm ? a.tperm[k] : k;
         tx[t] = __double2float_rn(a.tg[3 * i]);
         ty[t] = __double2float_rn(a.tg[3 * i + 1]);
         tz[t] = __double2float_rn(a.tg[3 * i + 2]);
         tz2[t] = 2.0f * tz[t];
+        bl[0] = fminf(bl[0], tx[t]), bl[1] = fminf(bl[1], ty[t]), bl[2] = fminf(bl[2], tz[t]);
+        bh[0] = fmaxf(bh[0], tx[t]), bh[1] = fmaxf(bh[1], ty[t]), bh[2] = fmaxf(bh[2], tz[t]);
     }
+    // bounding box of the CTA's targets (fminf/fmaxf leave out a NaN coordinate; the pairs of
+    // such a target compare false against every threshold, so both loops treat them alike)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            bl[c] = fminf(bl[c], __shfl_xor_sync(0xffffffffu, bl[c], o));
+            bh[c] = fmaxf(bh[c], __shfl_xor_sync(0xffffffffu, bh[c], o));
+        }
+    if ((threadIdx.x & 31) == 0)
+#pragma unroll
+        for (int c = 0; c < 3; c++) s_box[threadIdx.x >> 5][c] = bl[c], s_box[threadIdx.x >> 5][3 + c] = bh[c];
+    __syncthreads();
+#pragma unroll
+    for (int w = 0; w < kF32Threads / 32; w++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) bl[c] = fminf(bl[c], s_box[w][c]), bh[c] = fmaxf(bh[c], s_box[w][3 + c]);
     double acc[TPT][OUTW];
 #pragma unroll
     for (int t = 0; t < TPT; t++)
@@ -299,7 +343,29 @@ __global__ void __launch_bounds__(kF32Threads) far_f32_kernel(FarArgs a) {
         for (int t = 0; t < TPT; t++)
 #pragma unroll
             for (int c = 0; c < OUTW; c++) u[t][c] = 0.0f;
+        // no pair of the tile is near when the gap between the two boxes exceeds every
+        // threshold of the tile (QF >= gap^2 up to rounding, which the 2^-10 margin covers);
+        // the same decision in every thread of the CTA
+        bool far_tile = false;
         if (cnt == kF32Tile) {
+            const float4 lo = a.tile_box[2 * (jt / kF32Tile)], hi = a.tile_box[2 * (jt / kF32Tile) + 1];
+            const float gx = fmaxf(0.0f, fmaxf(lo.x - bh[0], bl[0] - hi.x));
+            const float gy = fmaxf(0.0f, fmaxf(lo.y - bh[1], bl[1] - hi.y));
+            const float gz = fmaxf(0.0f, fmaxf(lo.z - bh[2], bl[2] - hi.z));
+            far_tile = fmaf(gz, gz, fmaf(gy, gy, gx * gx)) > lo.w * (1.0f + 0x1p-10f);
+        }
+        if (far_tile) {
+#pragma unroll kFarUnroll
+            for (int k = 0; k < kF32Tile; k++) {
+                const float4 p = s_src[k * NQ];
+                const float4 q = s_src[k * NQ + 1];
+                const float4 r = NF == 2 ? s_src[k * NQ + (NQ - 1)] : zero4;
+#pragma unroll
+                for (int t = 0; t < TPT; t++)
+                    pair_f32_far<KIND, NF, CK, false>(tx[t], ty[t], tz[t], tz2[t], p, q, r, a.alpha_re, a.alpha_im,
+                                                      u[t]);
+            }
+        } else if (cnt == kF32Tile) {
 #pragma unroll 2
             for (int k = 0; k < kF32Tile; k++) {
                 const float4 p = s_src[k * NQ];
@@ -335,24 +401,59 @@ __global__ void __launch_bounds__(kF32Threads) far_f32_kernel(FarArgs a) {
     }
 }
 
-// pack FP64 sources into FP32 float4 slots
-__global__ void pack_geometry_kernel(const double *src, const double *eps, int64_t N, int NQ, float4 *packed) {
-    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= N) return;
+// pack FP64 sources into FP32 float4 slots, slot k holding source order[k] (cell order)
+__global__ void pack_geometry_kernel(const double *src, const double *eps, const int *order, int64_t N, int NQ,
+                                     float4 *packed) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    const int64_t j = order[k];
     const double e = eps[j];
     const float e2 = __double2float_rn(e * e);
-    packed[j * NQ] = make_float4(__double2float_rn(src[3 * j]), __double2float_rn(src[3 * j + 1]),
+    packed[k * NQ] = make_float4(__double2float_rn(src[3 * j]), __double2float_rn(src[3 * j + 1]),
                                  __double2float_rn(src[3 * j + 2]), e2);
-    packed[j * NQ + 1].w = __fmul_rn(17.0f, e2);  // |d|^2 < 16 eps^2  <=>  QF < 17 eps^2
+    packed[k * NQ + 1].w = __fmul_rn(17.0f, e2);  // |d|^2 < 16 eps^2  <=>  QF < 17 eps^2
 }
 
-// src (wall kernel only): the strengths are scaled by the source height z_j, the factor of
-// the wall pair that depends on the source alone (see wall_far_geo)
-__global__ void pack_strengths_kernel(const double *f, const double *src, int64_t N, int NF, float4 *packed) {
-    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= N) return;
+// per 256-source tile of the packed sources: bounding box of the FP32 coordinates and the
+// largest threshold, {lo x, y, z, max thr} {hi x, y, z, 0}
+__global__ void __launch_bounds__(256) tile_box_kernel(const float4 *packed, int64_t N, int NQ, float4 *box) {
+    __shared__ float st[7][8];
+    const int64_t k = (int64_t)blockIdx.x * 256 + threadIdx.x;
+    float v[7] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY, 0.0f};
+    if (k < N) {
+        const float4 p = packed[k * NQ];
+        v[0] = v[3] = p.x, v[1] = v[4] = p.y, v[2] = v[5] = p.z;
+        v[6] = packed[k * NQ + 1].w;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int c = 0; c < 7; c++) {
+            const float w = __shfl_xor_sync(0xffffffffu, v[c], o);
+            v[c] = (c < 3) ? fminf(v[c], w) : fmaxf(v[c], w);
+        }
+    if ((threadIdx.x & 31) == 0)
+#pragma unroll
+        for (int c = 0; c < 7; c++) st[c][threadIdx.x >> 5] = v[c];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < 8; w++)
+            for (int c = 0; c < 7; c++) v[c] = (c < 3) ? fminf(v[c], st[c][w]) : fmaxf(v[c], st[c][w]);
+        box[2 * blockIdx.x] = make_float4(v[0], v[1], v[2], v[6]);
+        box[2 * blockIdx.x + 1] = make_float4(v[3], v[4], v[5], 0.0f);
+    }
+}
+
+// slot k gets the strength of source order[k]; src (wall kernel only): the strengths are
+// scaled by the source height z_j, the factor of the wall pair that depends on the source
+// alone (see wall_far_geo)
+__global__ void pack_strengths_kernel(const double *f, const double *src, const int *order, int64_t N, int NF,
+                                      float4 *packed) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    const int64_t j = order[k];
     const int NQ = 1 + NF;
-    float4 *q = packed + j * NQ + 1;
+    float4 *q = packed + k * NQ + 1;
     const double *fj = f + (int64_t)3 * NF * j;
     const double h = src ? src[3 * j + 2] : 1.0;
     if (NF == 1) {
@@ -521,6 +622,7 @@ __global__ void cell_sort_kernel(const int *offsets, const CellGrid *g, int *sor
 struct NearArgs {
     const double *tg;
     int64_t M;
+    const int *tperm;  // processing position -> target index (null: identity), as in the far field
     const double *src;
     const double *eps;
     const double *f;
@@ -537,8 +639,9 @@ struct NearArgs {
 template <int KIND, int NF, bool CK>
 __global__ void __launch_bounds__(128) near_f64_kernel(NearArgs a) {
     constexpr int OUTW = (NF == 2 || CK) ? 6 : 3;
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.M) return;
+    const int64_t kt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;  // processing position
+    if (kt >= a.M) return;
+    const int64_t i = a.tperm ? a.tperm[kt] : kt;
     const CellGrid G = *a.grid;
     const double tx = a.tg[3 * i], ty = a.tg[3 * i + 1], tz = a.tg[3 * i + 2], tz2 = 2.0 * tz;
     const float fx = __double2float_rn(tx), fy = __double2float_rn(ty), fz = __double2float_rn(tz);
@@ -547,7 +650,7 @@ __global__ void __launch_bounds__(128) near_f64_kernel(NearArgs a) {
     for (int c = 0; c < OUTW; c++) u[c] = 0.0;
     // far partials, summed in split order
     for (int s = 0; s < a.fin.S; s++) {
-        const double *p = a.fin.partial + ((int64_t)s * a.M + i) * OUTW;
+        const double *p = a.fin.partial + ((int64_t)s * a.M + kt) * OUTW;
 #pragma unroll
         for (int c = 0; c < OUTW; c++) u[c] += p[c];
     }
@@ -566,8 +669,8 @@ __global__ void __launch_bounds__(128) near_f64_kernel(NearArgs a) {
                     const int b = a.offsets[c], e = a.offsets[c + 1];
                     for (int k = b; k < e; k++) {
                         const int j = a.sorted[k];
-                        const float4 p = a.packed[(int64_t)j * a.NQ];
-                        const float thr = a.packed[(int64_t)j * a.NQ + 1].w;
+                        const float4 p = a.packed[(int64_t)k * a.NQ];  // packed in cell order
+                        const float thr = a.packed[(int64_t)k * a.NQ + 1].w;
                         const float d0 = sub_rn(fx, p.x), d1 = sub_rn(fy, p.y), d2 = sub_rn(fz, p.z);
                         if (free_Q_f32(d0, d1, d2, p.w) < thr) {
                             const double ej = a.eps[j];
@@ -641,6 +744,7 @@ static void carve_plan(A &ar, int64_t M, int64_t N, const SumLayout &L, int prec
     p->partial = ar.template take<double>((size_t)std::max<int64_t>(L.S, 1) * M * L.outw);
     if (precision == FLG_PREC_MIXED) {
         p->packed = ar.template take<float4>((size_t)N * L.NQ);
+        p->tile_box = ar.template take<float4>(2 * (size_t)ceil_div(std::max<int64_t>(N, 1), kF32Tile));
         p->grid = ar.template take<CellGrid>(1);
         p->bounds = ar.template take<double>(kBoundBlocks * 7);
         p->cell_of = ar.template take<int>(N);
@@ -648,6 +752,11 @@ static void carve_plan(A &ar, int64_t M, int64_t N, const SumLayout &L, int prec
         p->offsets = ar.template take<int>(kMaxCells + 1);
         p->block_sums = ar.template take<int>(kMaxCells / kScanBlock + 1);
         p->sorted = ar.template take<int>(N);
+        if (M >= kSortTargetsMin) {
+            p->tcell = ar.template take<int>(M);
+            p->toffsets = ar.template take<int>(kMaxCells + 1);
+            p->tperm = ar.template take<int>(M);
+        }
     }
 }
 
@@ -665,7 +774,8 @@ int sum_plan_carve(void *work, size_t work_bytes, int64_t M, int64_t N, const Su
     if (M == 0 || N == 0) return FLG_OK;
     Arena ar(work, work_bytes);
     carve_plan(ar, M, N, L, precision, p);
-    const bool ok = p->partial != nullptr && (precision != FLG_PREC_MIXED || p->sorted != nullptr);
+    const bool ok = p->partial != nullptr && (precision != FLG_PREC_MIXED || p->sorted != nullptr) &&
+                    (precision != FLG_PREC_MIXED || M < kSortTargetsMin || p->tperm != nullptr);
     FLG_REQUIRE(ok, "workspace too small: %zu bytes given, %zu needed", work_bytes,
                 sum_workspace_bytes(0, M, N, L.nf, L.ck, precision));
     return FLG_OK;
@@ -677,8 +787,6 @@ int sum_plan_geometry(const double *src, const double *eps, int64_t N, const Sum
                       cudaStream_t st) {
     if (N == 0) return FLG_OK;
     const int tb = 256;
-    pack_geometry_kernel<<<(unsigned)ceil_div(N, tb), tb, 0, st>>>(src, eps, N, L.NQ, p->packed);
-    FLG_LAUNCH_CHECK();
     cell_bounds_kernel<<<kBoundBlocks, 256, 0, st>>>(src, eps, N, p->bounds);
     FLG_LAUNCH_CHECK();
     cell_setup_kernel<<<1, 32, 0, st>>>(p->bounds, kBoundBlocks, p->grid);
@@ -699,6 +807,33 @@ int sum_plan_geometry(const double *src, const double *eps, int64_t N, const Sum
     cell_scatter_kernel<<<(unsigned)ceil_div(N, tb), tb, 0, st>>>(p->cell_of, N, p->offsets, p->counts, p->sorted);
     FLG_LAUNCH_CHECK();
     cell_sort_kernel<<<kMaxCells / 256, 256, 0, st>>>(p->offsets, p->grid, p->sorted);
+    FLG_LAUNCH_CHECK();
+    // the FP32 sources in cell order, and the bounding box of each far-field tile of them
+    pack_geometry_kernel<<<(unsigned)ceil_div(N, tb), tb, 0, st>>>(src, eps, p->sorted, N, L.NQ, p->packed);
+    FLG_LAUNCH_CHECK();
+    tile_box_kernel<<<(unsigned)ceil_div(N, kF32Tile), 256, 0, st>>>(p->packed, N, L.NQ, p->tile_box);
+    FLG_LAUNCH_CHECK();
+    return FLG_OK;
+}
+
+// Processing order of a large target set: bucketed by the cell of the source grid they fall
+// in (a counting sort; the order within a cell does not matter, since a target's sum does
+// not depend on which CTA computes it).  Reuses the counting buffers of the source cell
+// list, which sum_plan_geometry no longer needs.
+static int sort_targets(const double *tg, int64_t M, const SumPlan *p, cudaStream_t st) {
+    const int tb = 256;
+    FLG_CUDA(cudaMemsetAsync(p->counts, 0, sizeof(int) * kMaxCells, st));
+    cell_count_kernel<<<(unsigned)ceil_div(M, tb), tb, 0, st>>>(tg, M, p->grid, p->tcell, p->counts);
+    FLG_LAUNCH_CHECK();
+    const int nb = kMaxCells / kScanBlock;
+    scan_block_kernel<<<nb, kScanBlock, 0, st>>>(p->counts, p->toffsets, p->block_sums, kMaxCells);
+    FLG_LAUNCH_CHECK();
+    scan_sums_kernel<<<1, kScanBlock, 0, st>>>(p->block_sums, nb);
+    FLG_LAUNCH_CHECK();
+    scan_add_kernel<<<nb, kScanBlock, 0, st>>>(p->toffsets, p->block_sums, kMaxCells);
+    FLG_LAUNCH_CHECK();
+    FLG_CUDA(cudaMemsetAsync(p->counts, 0, sizeof(int) * kMaxCells, st));
+    cell_scatter_kernel<<<(unsigned)ceil_div(M, tb), tb, 0, st>>>(p->tcell, M, p->toffsets, p->counts, p->tperm);
     FLG_LAUNCH_CHECK();
     return FLG_OK;
 }
@@ -732,16 +867,26 @@ static int launch_sum(const SumRun &r, const SumLayout &L, int precision, const 
     }
     // mixed: strengths into the packed slots, FP32 far field, FP64 near field + combine
     pack_strengths_kernel<<<(unsigned)ceil_div(r.N, 256), 256, 0, st>>>(r.f, KIND == FLG_WALL ? r.src : nullptr,
-                                                                       r.N, NF, p->packed);
+                                                                       p->sorted, r.N, NF, p->packed);
     FLG_LAUNCH_CHECK();
+    // targets in cell order: the sources' own order when the targets are the sources, a
+    // bucket sort for other large target sets, the given order for small ones
+    const int *tperm = nullptr;
+    if (r.tg == r.src && r.M == r.N) {
+        tperm = p->sorted;
+    } else if (r.M >= kSortTargetsMin && p->tperm) {
+        FLG_TRY(sort_targets(r.tg, r.M, p, st));
+        tperm = p->tperm;
+    }
     constexpr int TPT = (NF == 1 && !CK) ? FLG_FAR_TPT : 1;
-    FarArgs fa{r.tg, r.M, p->packed, r.N, L.split_len, (float)r.alpha_re, (float)r.alpha_im, p->partial};
+    FarArgs fa{r.tg, r.M, tperm, p->packed, p->tile_box, r.N, L.split_len, (float)r.alpha_re, (float)r.alpha_im,
+               p->partial};
     dim3 grid((unsigned)ceil_div(r.M, kF32Threads * TPT), (unsigned)L.S);
     prof_begin(FLG_SLOT_FAR_F32, st);
     far_f32_kernel<KIND, NF, CK, TPT><<<grid, kF32Threads, 0, st>>>(fa);
     FLG_LAUNCH_CHECK();
     prof_end(FLG_SLOT_FAR_F32, st);
-    NearArgs na{r.tg, r.M, r.src, r.eps, r.f, r.N, p->packed, L.NQ, p->grid, p->offsets, p->sorted,
+    NearArgs na{r.tg, r.M, tperm, r.src, r.eps, r.f, r.N, p->packed, L.NQ, p->grid, p->offsets, p->sorted,
                 r.alpha_re, r.alpha_im, fin};
     prof_begin(FLG_SLOT_NEAR_F64, st);
     near_f64_kernel<KIND, NF, CK><<<(unsigned)ceil_div(r.M, 128), 128, 0, st>>>(na);

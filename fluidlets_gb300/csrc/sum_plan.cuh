@@ -23,11 +23,13 @@ struct SumLayout {
 
 // device buffers carved from the caller's workspace
 struct SumPlan {
-    double *partial;  // [S][M][outw]
-    float4 *packed;   // [N][NQ] FP32 sources (mixed only)
+    double *partial;  // [S][M][outw], target in processing order
+    float4 *packed;   // [N][NQ] FP32 sources in cell order (mixed only)
+    float4 *tile_box; // [ceil(N / 256)][2]: lo x, y, z, max threshold | hi x, y, z
     CellGrid *grid;
     double *bounds;
     int *cell_of, *counts, *offsets, *block_sums, *sorted;
+    int *tcell, *toffsets, *tperm;  // targets bucketed by source cell (large target sets)
 };
 
 struct SumRun {
