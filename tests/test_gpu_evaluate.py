@@ -157,6 +157,44 @@ def test_config2_density_mixed_accuracy_sample():
     assert_close(u64, ref, rtol=1e-11, atol_rel=1e-13)
 
 
+@pytest.mark.parametrize("kind,alpha", [("wall", 0.0), ("stokeslet", 0.0), ("brinkman", 2.0)])
+def test_mixed_large_sets_in_cell_order(kind, alpha):
+    """Target sets large enough to be processed in cell order (a counting sort by source cell;
+    the sources' own order when the targets are the sources), where most far-field tiles run
+    without the near-pair mask: mixed vs the FP64 GPU sum, and the order of the given targets
+    does not change any result bit."""
+    from fluidlets_gb300.geometry import wall_sum_workload
+    T, S, F, eps = wall_sum_workload(24000, 40000, 2048, 0.02, seed=5)
+    k = kern(kind, alpha)
+    um = fl.evaluate(k, T, S, F, eps, precision="mixed")
+    u64 = fl.evaluate(k, T, S, F, eps)
+    interior = T[:, 2] > 0
+    assert rel_err(um[interior], u64[interior]) < 2e-6
+    if kind == "wall":
+        assert np.abs(um[~interior]).max() == 0.0
+    perm = np.random.default_rng(6).permutation(len(T))
+    assert np.array_equal(fl.evaluate(k, T[perm], S, F, eps, precision="mixed"), um[perm])
+    # targets = sources (40,000): the cell order of the sources themselves
+    X = np.r_[S, T[:16000]]
+    FX = np.random.default_rng(7).normal(size=X.shape)
+    assert rel_err(fl.evaluate(k, X, X, FX, eps, precision="mixed"), fl.evaluate(k, X, X, FX, eps)) < 2e-6
+
+
+def test_mixed_clustered_sources_keep_the_near_mask():
+    """Dense clusters (most tiles near most targets, every tile masked) next to a far cluster
+    (tiles unmasked): mixed vs FP64 on the same 40,000 targets."""
+    rng = np.random.default_rng(8)
+    a = rng.normal(scale=0.02, size=(30000, 3)) + [0, 0, 0.5]
+    b = rng.normal(scale=0.02, size=(10000, 3)) + [3.0, 0, 0.5]
+    S = np.r_[a, b]
+    F = rng.normal(size=S.shape)
+    T = np.r_[rng.normal(scale=0.02, size=(20000, 3)) + [0, 0, 0.5], rng.normal(scale=0.5, size=(20000, 3)) + [0, 0, 1.5]]
+    for k in (fl.WallStokeslet3D(), fl.Stokeslet3D()):
+        um = fl.evaluate(k, T, S, F, 0.004, precision="mixed")
+        u64 = fl.evaluate(k, T, S, F, 0.004)
+        assert rel_err(um, u64) < 5e-6
+
+
 # ---- structured grids: the 32^3 legacy grid (tests/legacy/test_phase1_port.py:77-87) ----
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_grid_reproduces_2010_velocity_grid(legacy_towers, legacy_grid, precision):
