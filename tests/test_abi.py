@@ -38,3 +38,31 @@ def test_invalid_arguments_rejected_on_host(lib):
     assert b"kind" in L.flg_last_error()
     st = L.flg_evaluate(2, -1.0, 0.0, None, 1, None, None, 1, None, 0, 1.0, 0.0, None, 0, None, 0, None)
     assert st == lib.FLG_ERR_INVALID
+
+
+def header_constants():
+    text = (ROOT / "include" / "fluidlets_gb300.h").read_text()
+    return {k: int(v, 0) for k, v in re.findall(r"#define\s+(FLG_[A-Z0-9_]+)\s+(0x[0-9A-Fa-f]+|\d+)\b", text)}
+
+
+def test_lu_mode_names_match_the_header(lib):
+    """The Python LU mode names (precision, and the tile width of the tensor-core updates) encode
+    the header's mode constants; every name the serving autotuner tries is a valid mode."""
+    c = header_constants()
+    assert lib.LU_MODE["tf32"] == c["FLG_LU_TF32"] and lib.LU_MODE["bf16"] == c["FLG_LU_BF16"]
+    assert lib.LU_MODE["fp32"] == c["FLG_LU_FP32"]
+    for prec in ("tf32", "bf16"):
+        assert lib.LU_MODE[f"{prec}:128"] == c[f"FLG_LU_{prec.upper()}"] | c["FLG_LU_TILE_N128"]
+        assert lib.LU_MODE[f"{prec}:256"] == c[f"FLG_LU_{prec.upper()}"] | c["FLG_LU_TILE_N256"]
+    from fluidlets_gb300.serve import TUNE_CANDIDATES
+    assert set(TUNE_CANDIDATES) <= set(lib.LU_MODE) and len(set(TUNE_CANDIDATES)) == 6
+
+
+def test_lu_workspace_does_not_depend_on_the_tile_width(lib):
+    L = lib.load()
+    for n in (128, 1000, 4608):
+        for prec in ("tf32", "bf16"):
+            base = L.flg_lu_factor_lowp_workspace(n, lib.LU_MODE[prec])
+            assert base > 0
+            assert L.flg_lu_factor_lowp_workspace(n, lib.LU_MODE[prec + ":128"]) == base
+            assert L.flg_lu_factor_lowp_workspace(n, lib.LU_MODE[prec + ":256"]) == base
