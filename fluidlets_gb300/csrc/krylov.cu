@@ -460,7 +460,7 @@ struct Gmres {
 // ---- matrix-free operator of flg_gmres --------------------------------------------
 struct SumOperator {
     SumLayout L;
-    SumPlan P;
+    SumPlan P{};
     SumRun R;
     int precision;
     cudaStream_t st;

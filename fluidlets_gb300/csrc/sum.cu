@@ -752,6 +752,7 @@ static void carve_plan(A &ar, int64_t M, int64_t N, const SumLayout &L, int prec
         p->offsets = ar.template take<int>(kMaxCells + 1);
         p->block_sums = ar.template take<int>(kMaxCells / kScanBlock + 1);
         p->sorted = ar.template take<int>(N);
+        p->tcell = p->toffsets = p->tperm = nullptr;
         if (M >= kSortTargetsMin) {
             p->tcell = ar.template take<int>(M);
             p->toffsets = ar.template take<int>(kMaxCells + 1);
