@@ -816,7 +816,7 @@ __global__ void transpose_f32_kernel(const float *src, int64_t lds, float *dst, 
 size_t tc_update_bytes(int64_t m, int64_t nc, int64_t K, int mode);
 int tc_update(float *C, int64_t ldc, const float *Lp, int64_t ldl, const float *Ut, int64_t ldu, int64_t m,
               int64_t nc, int64_t K, int mode, void *work, size_t work_bytes, cudaStream_t st, int *err_dev,
-              bool store = false, int tile = 0);
+              bool store = false, int tile = 0, int max_ctas = 0);
 
 static int sgemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, float alpha, const float *A, int64_t lda,
                  const float *B, int64_t ldb, float beta, float *C, int64_t ldc) {
@@ -1282,6 +1282,30 @@ extern "C" int flg_lu_solve_f64(int64_t n, int64_t nrhs, const double *LU, int64
 }
 
 // ---- low-precision LU entry points ----------------------------------------------------
+// Per host thread and device: the stream that runs the next diagonal block while the
+// trailing update finishes (highest priority), and the events of that fork and join.
+// Created on first use; an LU captured in a graph makes one eager pass first.
+struct SideStream {
+    int dev = -1;
+    cudaStream_t s = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+};
+static int side_stream(SideStream **out) {
+    thread_local SideStream ss;
+    int dev = 0;
+    FLG_CUDA(cudaGetDevice(&dev));
+    if (ss.dev != dev) {
+        int lo = 0, hi = 0;
+        FLG_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+        FLG_CUDA(cudaStreamCreateWithPriority(&ss.s, cudaStreamNonBlocking, hi));
+        FLG_CUDA(cudaEventCreateWithFlags(&ss.fork, cudaEventDisableTiming));
+        FLG_CUDA(cudaEventCreateWithFlags(&ss.join, cudaEventDisableTiming));
+        ss.dev = dev;
+    }
+    *out = &ss;
+    return FLG_OK;
+}
+
 extern "C" int64_t flg_lu_lowp_dinv_elems(int64_t n) { return 2 * ceil_div(std::max<int64_t>(n, 1), kNB) * kNB * kNB; }
 
 // Tensor-core modes defer most of the trailing update: blocks are grouped into
@@ -1350,17 +1374,46 @@ extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mod
     const bool tc = mode != FLG_LU_FP32;
     const int64_t nblk = ceil_div(n, kNB);
     float *Linv = dinv, *Uinv = dinv + nblk * kNB * kNB;
+    SideStream *side = nullptr;
+    if (tc) FLG_TRY(side_stream(&side));
+    // the persistent updates that run beside a look-ahead diagonal block leave it an SM
+    const int cap = std::max(1, sm_count() - 1);
+    auto diag = [&](int64_t d0, cudaStream_t s) {
+        const int64_t kd = d0 / kNB;
+        const int nbd = (int)std::min<int64_t>(kNB, n - d0);
+        const bool tcp = tc && nbd == kNB && n - (d0 + nbd) > 0;  // tensor-core panels follow
+        prof_begin(FLG_SLOT_LU_DIAG, s);
+        diag_lowp_kernel<<<1, 512, dsmem, s>>>(A, ld, d0, nbd, Linv + kd * kNB * kNB, Uinv + kd * kNB * kNB,
+                                               tcp ? UinvT : nullptr, dinfo);
+        prof_end(FLG_SLOT_LU_DIAG, s);
+    };
+    // Look-ahead: once the 128 x 128 block at d0 has its last update (launched on st), the
+    // diagonal kernel of that block runs on the side stream while st goes on with the rest of
+    // the trailing update; the next panels wait for it.  Only for a full block with a
+    // trailing part (the block's own panels then run on the tensor cores).
+    bool pending = false;
+    auto look_ahead = [&](int64_t d0) -> int {
+        FLG_CUDA(cudaEventRecord(side->fork, st));
+        FLG_CUDA(cudaStreamWaitEvent(side->s, side->fork, 0));
+        diag(d0, side->s);
+        FLG_LAUNCH_CHECK();
+        FLG_CUDA(cudaEventRecord(side->join, side->s));
+        pending = true;
+        return FLG_OK;
+    };
     for (int64_t K0 = 0; K0 < n; K0 += kOuterW) {
         const int64_t E = std::min<int64_t>(n, K0 + kOuterW);
         for (int64_t k0 = K0; k0 < E; k0 += kNB) {
             const int64_t k = k0 / kNB;
             const int nb = (int)std::min<int64_t>(kNB, n - k0);
-            prof_begin(FLG_SLOT_LU_DIAG, st);
             const bool tcp = tc && nb == kNB && n - (k0 + nb) > 0;  // tensor-core panels
-            diag_lowp_kernel<<<1, 512, dsmem, st>>>(A, ld, k0, nb, Linv + k * kNB * kNB, Uinv + k * kNB * kNB,
-                                                    tcp ? UinvT : nullptr, dinfo);
-            FLG_LAUNCH_CHECK();
-            prof_end(FLG_SLOT_LU_DIAG, st);
+            if (pending) {  // this block's diagonal kernel ran ahead on the side stream
+                FLG_CUDA(cudaStreamWaitEvent(st, side->join, 0));
+                pending = false;
+            } else {
+                diag(k0, st);
+                FLG_LAUNCH_CHECK();
+            }
             const int64_t c0 = k0 + nb, nr = n - c0;
             if (nr <= 0) continue;
             prof_begin(FLG_SLOT_LU_PANEL, st);
@@ -1399,23 +1452,49 @@ extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mod
             if (!tc || nb < kNB) {
                 FLG_TRY(sgemm(st, nr, nr, nb, -1.0f, A21, ld, A12, ld, 1.0f, A22, ld));
             } else if (E > c0) {
-                // rows > k0 x columns (k0, E)
-                FLG_TRY(tc_update(A22, ld, A21, ld, Ut, kOuterW, nr, E - c0, kNB, mode, tcw, tcb, st, dinfo + 1,
-                                  false, tile));
+                if (n - c0 > kNB) {
+                    // the next diagonal block first, then it factors beside the rest:
+                    // rows > c0 + 128 x its columns, rows > k0 x columns (c0 + 128, E)
+                    FLG_TRY(tc_update(A22, ld, A21, ld, Ut, kOuterW, kNB, kNB, kNB, mode, tcw, tcb, st, dinfo + 1,
+                                      false, tile));
+                    FLG_TRY(look_ahead(c0));
+                    FLG_TRY(tc_update(A22 + kNB * ld, ld, A21 + kNB * ld, ld, Ut, kOuterW, nr - kNB, kNB, kNB, mode,
+                                      tcw, tcb, st, dinfo + 1, false, tile, cap));
+                    if (E > c0 + kNB)
+                        FLG_TRY(tc_update(A22 + kNB, ld, A21, ld, Ut + kNB * kOuterW, kOuterW, nr, E - c0 - kNB, kNB,
+                                          mode, tcw, tcb, st, dinfo + 1, false, tile, cap));
+                } else {
+                    // rows > k0 x columns (k0, E)
+                    FLG_TRY(tc_update(A22, ld, A21, ld, Ut, kOuterW, nr, E - c0, kNB, mode, tcw, tcb, st, dinfo + 1,
+                                      false, tile));
+                }
                 // rows (k0, E) x columns >= E
                 if (n > E)
                     FLG_TRY(tc_update(A + c0 * ld + E, ld, A21, ld, Ut + (E - c0) * kOuterW, kOuterW, E - c0, n - E,
-                                      kNB, mode, tcw, tcb, st, dinfo + 1, false, tile));
+                                      kNB, mode, tcw, tcb, st, dinfo + 1, false, tile, pending ? cap : 0));
             }
             prof_end(FLG_SLOT_LU_UPDATE, st);
         }
         if (tc && n > E) {  // the deferred rank-(E - K0) update of rows and columns >= E (E - K0 = kOuterW here)
             prof_begin(FLG_SLOT_LU_UPDATE, st);
-            FLG_TRY(tc_update(A + E * ld + E, ld, A + E * ld + K0, ld, UtB + (E - K0) * kOuterW, kOuterW, n - E, n - E,
-                              E - K0, mode, tcw, tcb, st, dinfo + 1, false, tile));
+            float *C = A + E * ld + E, *Lp = A + E * ld + K0, *Up = UtB + (E - K0) * kOuterW;
+            if (n - E > kNB) {
+                // the next outer panel's first diagonal block first, then it factors beside the rest
+                FLG_TRY(tc_update(C, ld, Lp, ld, Up, kOuterW, kNB, kNB, E - K0, mode, tcw, tcb, st, dinfo + 1, false,
+                                  tile));
+                FLG_TRY(look_ahead(E));
+                FLG_TRY(tc_update(C + kNB * ld, ld, Lp + kNB * ld, ld, Up, kOuterW, n - E - kNB, kNB, E - K0, mode,
+                                  tcw, tcb, st, dinfo + 1, false, tile, cap));
+                FLG_TRY(tc_update(C + kNB, ld, Lp, ld, Up + kNB * kOuterW, kOuterW, n - E, n - E - kNB, E - K0, mode,
+                                  tcw, tcb, st, dinfo + 1, false, tile, cap));
+            } else {
+                FLG_TRY(tc_update(C, ld, Lp, ld, Up, kOuterW, n - E, n - E, E - K0, mode, tcw, tcb, st, dinfo + 1,
+                                  false, tile));
+            }
             prof_end(FLG_SLOT_LU_UPDATE, st);
         }
     }
+    if (pending) FLG_CUDA(cudaStreamWaitEvent(st, side->join, 0));  // (every look-ahead is joined above)
     return FLG_OK;
 }
 

@@ -417,16 +417,17 @@ static int tc_launch(const CUtensorMap &ma, const CUtensorMap &mb, const CUtenso
 // err_dev: device flag raised on a timed-out wait.  When null, the flag lives in
 // the workspace and the call synchronizes to check it; the LU passes its own
 // flag and checks it once at the end of the factorization.  tile: 0 picks the
-// tile width (tc_pick_tile), 128 or 256 forces it.
+// tile width (tc_pick_tile), 128 or 256 forces it.  max_ctas > 0 caps the
+// persistent grid (leaving SMs to work on another stream).
 int tc_update(float *C, int64_t ldc, const float *Lp, int64_t ldl, const float *Ut, int64_t ldu, int64_t m,
               int64_t nc, int64_t K, int mode, void *work, size_t work_bytes, cudaStream_t st, int *err_dev,
-              bool store, int tile) {
+              bool store, int tile, int max_ctas) {
     FLG_REQUIRE(mode == FLG_LU_TF32 || mode == FLG_LU_BF16, "tensor-core mode must be TF32 or BF16");
     FLG_REQUIRE(m >= 0 && nc >= 0 && m < (1LL << 31) && nc < (1LL << 31), "bad tensor-core update shape");
     FLG_REQUIRE(K > 0 && K % 128 == 0 && K <= (1 << 20), "tensor-core update depth must be a multiple of 128");
     FLG_REQUIRE(tile == 0 || tile == 128 || tile == 256, "tile width must be 128 or 256 (or 0 to choose)");
     if (m == 0 || nc == 0) return FLG_OK;
-    const int sms = sm_count_of_current_device();
+    const int sms = max_ctas > 0 ? std::min(max_ctas, sm_count_of_current_device()) : sm_count_of_current_device();
     const int bn = tile ? tile : tc_pick_tile(m, nc, sms);
     Arena ar(work, work_bytes);
     int *own = ar.take<int>(1);
@@ -477,5 +478,5 @@ extern "C" int flg_tc_rank_update(float *C, int64_t ldc, const float *A, int64_t
     FLG_REQUIRE(ldb == 128, "Bt must be compact (ldb == 128)");
     FLG_REQUIRE(lda >= 128 && ldc >= nc, "bad leading dimensions");
     return flg::tc_update(C, ldc, A, lda, Bt, 128, m, nc, 128, mode, work, work_bytes, flg::as_stream(stream), nullptr,
-                          false, 0);
+                          false, 0, 0);
 }
