@@ -335,7 +335,11 @@ __global__ void __launch_bounds__(256) gemv_f64_kernel(int64_t nr, int64_t nc, c
 // Oishi, "Accurate sum and dot product", SIAM J. Sci. Comput. 26, 2005).  The
 // _rn intrinsics keep the compiler from contracting the error-free steps.  A
 // warp per two rows, 32 rows per block; x goes through shared memory in chunks.
-constexpr int kGvWarps = 16, kGvRpw = 2, kGvRows = kGvWarps * kGvRpw, kGvChunk = 2048;
+// columns of x staged in shared memory per pass (48 KB for the split x: the static limit)
+#ifndef FLG_GV_CHUNK
+#define FLG_GV_CHUNK 6144
+#endif
+constexpr int kGvWarps = 16, kGvRpw = 2, kGvRows = kGvWarps * kGvRpw, kGvChunk = FLG_GV_CHUNK;
 
 __device__ __forceinline__ void dot2_step(float &s, float &c, float a, float xh, float xl) {
     const float p = __fmul_rn(a, xh);
