@@ -21,6 +21,14 @@ LU_MODE = {"tf32": 0, "bf16": 1, "fp32": 2}
 LU_TILE = {128: 0x100, 256: 0x200}
 LU_MODE.update({f"{p}:{t}": LU_MODE[p] | b for p in ("tf32", "bf16") for t, b in LU_TILE.items()})
 
+
+def lu_mode(name: str) -> int:
+    """Mode constant of a low-precision LU name ("tf32", "bf16", "fp32", "tf32:128", ...)."""
+    try:
+        return LU_MODE[name]
+    except (KeyError, TypeError):
+        raise ValueError(f"unknown lu {name!r}: expected one of {', '.join(LU_MODE)}") from None
+
 # name -> (restype, argtypes); mirrors include/fluidlets_gb300.h
 _P = c_void_p
 SIGNATURES = {

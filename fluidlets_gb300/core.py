@@ -21,7 +21,7 @@ import numpy as np
 import torch
 
 from . import _device as dv
-from ._lib import BF16, C128, F32, F64, FLG_ERR_NOT_CONVERGED, LU_MODE, PREC, check, load
+from ._lib import BF16, C128, F32, F64, FLG_ERR_NOT_CONVERGED, PREC, check, load, lu_mode
 from .kernels import kernel_params
 
 #: above this many unknowns, method="auto" switches from dense LU to GMRES (core/solve.py:20)
@@ -274,7 +274,7 @@ def _lu_solve_dev(K: torch.Tensor, U: torch.Tensor) -> torch.Tensor:
     return B.reshape(-1) if nrhs == 1 else B
 
 
-def _lowp_factor_dev(K: torch.Tensor, lu_mode: str):
+def _lowp_factor_dev(K: torch.Tensor, lu_name: str):
     """FP32 copy of K (leading dimension padded to 32) factored without pivoting
     on the tensor cores; returns (K32, ld32, dinv, A32) with A32 an unfactored FP32
     copy of K for the inner matvecs of GMRES-IR."""
@@ -285,7 +285,7 @@ def _lowp_factor_dev(K: torch.Tensor, lu_mode: str):
     check(L.flg_convert_f64_f32(n, n, dv.ptr(K), K.stride(0), dv.ptr(K32), ld32, dv.stream()), "convert")
     A32 = K32.clone()
     dinv = torch.empty(L.flg_lu_lowp_dinv_elems(n), dtype=torch.float32, device=K.device)
-    mode = LU_MODE[lu_mode]
+    mode = lu_mode(lu_name)
     nbytes = L.flg_lu_factor_lowp_workspace(n, mode)
     ws = dv.workspace(nbytes)
     info = ctypes.c_int(0)
@@ -319,9 +319,9 @@ def _gmres_ir_dense_dev(K, K32, ld32, dinv, b, rtol, restart, maxiter, required=
     return x, iters.value, outer.value, resid.value
 
 
-def _mixed_lu_solve_dev(K: torch.Tensor, U: torch.Tensor, rtol, restart, maxiter, lu_mode, required=None):
+def _mixed_lu_solve_dev(K: torch.Tensor, U: torch.Tensor, rtol, restart, maxiter, lu_name, required=None):
     """TF32/BF16 tensor-core LU of K (no pivoting) + FP64 GMRES iterative refinement."""
-    K32, ld32, dinv, A32 = _lowp_factor_dev(K, lu_mode)
+    K32, ld32, dinv, A32 = _lowp_factor_dev(K, lu_name)
     b = U.reshape(-1).to(torch.float64).contiguous()
     return _gmres_ir_dense_dev(K, K32, ld32, dinv, b, rtol, restart, maxiter, required, A32=A32)
 

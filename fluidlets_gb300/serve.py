@@ -36,7 +36,7 @@ import numpy as np
 import torch
 
 from . import _device as dv
-from ._lib import F64, LU_MODE, check, load
+from ._lib import F64, LU_MODE, check, load, lu_mode
 from .kernels import Stokeslet3D, kernel_params
 
 BUCKET_BASE = 128
@@ -114,7 +114,7 @@ class BucketPlan:
         self.A32 = torch.empty((n, self.ld32), dtype=torch.float32, device=dev)  # inner GMRES matvecs
         self.dinv = torch.empty(L.flg_lu_lowp_dinv_elems(n), dtype=torch.float32, device=dev)
         self.flags = torch.zeros(2, dtype=torch.int32, device=dev)
-        mode = LU_MODE[lu]
+        mode = lu_mode(lu)
         # sized for either tensor-core precision, so the autotuner can switch modes on one plan
         self.lu_bytes = max(L.flg_lu_factor_lowp_workspace(n, LU_MODE[m]) for m in ("tf32", "bf16"))
         self.lu_ws = dv.workspace(self.lu_bytes)
@@ -139,7 +139,7 @@ class BucketPlan:
         """Switch the LU mode of an uncaptured plan (the autotuner's candidates)."""
         if self.graph is not None:
             raise RuntimeError("the LU mode of a captured plan is fixed")
-        self.lu, self.mode = lu, LU_MODE[lu]
+        self.lu, self.mode = lu, lu_mode(lu)
 
     def capture(self):
         """Capture assembly -> FP32 copy -> tensor-core LU as a CUDA graph (in the library,

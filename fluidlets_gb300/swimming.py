@@ -22,7 +22,7 @@ import numpy as np
 import torch
 
 from . import _device as dv
-from ._lib import F64, LU_MODE, check, load
+from ._lib import F64, check, load, lu_mode
 from .core import _assemble_nearest_dev, _gmres_ir_dense_dev, _lowp_factor_dev, _lu_solve_dev, _prec, nearest_neighbors
 from .kernels import Stokeslet3D, kernel_params
 
@@ -119,7 +119,7 @@ class SwimmerPlan:
         self.A32 = torch.empty((n, self.ld32), dtype=torch.float32, device=dev)
         self.dinv = torch.empty(L.flg_lu_lowp_dinv_elems(n), dtype=torch.float32, device=dev)
         self.flags = torch.zeros(3, dtype=torch.int32, device=dev)
-        mode = LU_MODE[lu]
+        mode = lu_mode(lu)
         wb = L.flg_swimmer_graph_workspace(N, Q, mode)
         self.ws = dv.workspace(wb)
         kind, are, aim = kernel_params(kernel)

@@ -66,3 +66,10 @@ def test_lu_workspace_does_not_depend_on_the_tile_width(lib):
             assert base > 0
             assert L.flg_lu_factor_lowp_workspace(n, lib.LU_MODE[prec + ":128"]) == base
             assert L.flg_lu_factor_lowp_workspace(n, lib.LU_MODE[prec + ":256"]) == base
+
+
+def test_unknown_lu_name_is_a_value_error(lib):
+    assert lib.lu_mode("bf16:128") == lib.LU_MODE["bf16:128"]
+    for bad in ("tf16", "fp32:128", "tf32:64", None):
+        with pytest.raises(ValueError):
+            lib.lu_mode(bad)
