@@ -91,3 +91,45 @@ def test_plan_pool_limits_replanning():
     n_res = sum(isinstance(r, ResistanceRequest) for r in reqs)
     assert switches <= 2 * 4 + 2  # at most one plan per bucket and slot, not one per request
     assert n_res > 100
+
+
+class _Stream:
+    def synchronize(self):
+        pass
+
+
+def test_autotuner_keeps_the_fastest_candidate_that_converges(monkeypatch):
+    """The per-bucket autotuner times every precision x tile-width candidate on one plan and
+    keeps the fastest whose residual meets rtol; with none converging it falls back to TF32."""
+    import fluidlets_gb300.serve as sv
+
+    cost = {"tf32": 0.012, "tf32:128": 0.018, "tf32:256": 0.009, "bf16": 0.006, "bf16:128": 0.003,
+            "bf16:256": 0.015}
+    resid = dict.fromkeys(cost, 1e-12)
+    resid["bf16:128"] = 1e-6  # fastest, but does not converge
+    tried = []
+
+    class Plan:
+        def __init__(self, kernel, nbp, mu, lu, stream):
+            self.lu = lu
+
+        def set_lu(self, lu):
+            self.lu = lu
+            tried.append(lu)
+
+        def factor(self, X, e):
+            time.sleep(cost[self.lu])
+
+        def solve(self, U, rtol):
+            return None, 4, 2, resid[self.lu]
+
+    monkeypatch.setattr(sv, "BucketPlan", Plan)
+    assert set(cost) == set(sv.TUNE_CANDIDATES)
+    req = ResistanceRequest(fl.Stokeslet3D(), np.zeros((300, 3)), np.zeros((300, 3)), 0.1)
+    with FakeServer(slots=1) as srv:
+        assert srv._autotune(req, 384, _Stream(), None, None, None) == "bf16"
+        assert srv.stats["tuned"] == {"0:384": "bf16"}
+        assert sorted(tried) == sorted(sv.TUNE_CANDIDATES)
+        for k in resid:
+            resid[k] = 1e-3
+        assert srv._autotune(req, 512, _Stream(), None, None, None) == "tf32"
