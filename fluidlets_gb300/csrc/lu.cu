@@ -1288,7 +1288,7 @@ extern "C" int flg_lu_solve_f64(int64_t n, int64_t nrhs, const double *LU, int64
 struct SideStream {
     int dev = -1;
     cudaStream_t s = nullptr;
-    cudaEvent_t fork = nullptr, join = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr, tail = nullptr;
 };
 static int side_stream(SideStream **out) {
     thread_local SideStream ss;
@@ -1300,6 +1300,7 @@ static int side_stream(SideStream **out) {
         FLG_CUDA(cudaStreamCreateWithPriority(&ss.s, cudaStreamNonBlocking, hi));
         FLG_CUDA(cudaEventCreateWithFlags(&ss.fork, cudaEventDisableTiming));
         FLG_CUDA(cudaEventCreateWithFlags(&ss.join, cudaEventDisableTiming));
+        FLG_CUDA(cudaEventCreateWithFlags(&ss.tail, cudaEventDisableTiming));
         ss.dev = dev;
     }
     *out = &ss;
@@ -1391,13 +1392,30 @@ extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mod
     // diagonal kernel of that block runs on the side stream while st goes on with the rest of
     // the trailing update; the next panels wait for it.  Only for a full block with a
     // trailing part (the block's own panels then run on the tensor cores).
-    bool pending = false;
-    auto look_ahead = [&](int64_t d0) -> int {
+    bool pending = false, side_busy = false;
+    const dim3 tb(32, 8);
+    // Ut of an inner step back into the row block A12 (U12 row-major, read only by the solves):
+    // off the critical path, after the join on the side stream.  The next panels write other
+    // K slots of UtB and another row block; the next outer panel rewrites UtB only after a
+    // later diagonal kernel on the side stream, so every deferred transpose has run by then.
+    struct Deferred {
+        const float *Ut = nullptr;
+        float *A12 = nullptr;
+        int64_t nr = 0;
+    };
+    auto look_ahead = [&](int64_t d0, Deferred t) -> int {
         FLG_CUDA(cudaEventRecord(side->fork, st));
         FLG_CUDA(cudaStreamWaitEvent(side->s, side->fork, 0));
         diag(d0, side->s);
         FLG_LAUNCH_CHECK();
         FLG_CUDA(cudaEventRecord(side->join, side->s));
+        if (t.Ut) {
+            transpose_f32_kernel<<<dim3(kNB / 32, (unsigned)ceil_div(t.nr, 32)), tb, 0, side->s>>>(t.Ut, kOuterW,
+                                                                                                   t.A12, ld, t.nr,
+                                                                                                   kNB);
+            FLG_LAUNCH_CHECK();
+            side_busy = true;
+        }
         pending = true;
         return FLG_OK;
     };
@@ -1420,19 +1438,22 @@ extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mod
             // (nb < kNB only for the last block, which has no trailing part)
             float *A12 = A + k0 * ld + c0, *A21 = A + c0 * ld + k0, *A22 = A + c0 * ld + c0;
             float *Ut = UtB + (c0 - K0) * kOuterW + (k0 - K0);  // row: column - K0; K offset: k0 - K0
+            // an inner step whose next diagonal block runs ahead defers its transpose-back
+            const bool defer_t = tcp && E > c0 && n - c0 > kNB;
             if (tcp) {
                 // panels on the tensor cores (TF32 in both tensor-core modes):
                 //   Ut = A12^T Linv^T (the K-major copy the updates read), then A12 = Ut^T;
                 //   L21 = A21 Uinv, in place (each tile's rows are read in full before they are stored)
-                const dim3 tb(32, 8);
                 transpose_f32_kernel<<<dim3((unsigned)ceil_div(nr, 32), kNB / 32), tb, 0, st>>>(A12, ld, T12, kNB,
                                                                                                  kNB, nr);
                 FLG_LAUNCH_CHECK();
                 FLG_TRY(tc_update(Ut, kOuterW, T12, kNB, Linv + k * kNB * kNB, kNB, nr, kNB, kNB, FLG_LU_TF32, tcw,
                                   tcb, st, dinfo + 1, true));
-                transpose_f32_kernel<<<dim3(kNB / 32, (unsigned)ceil_div(nr, 32)), tb, 0, st>>>(Ut, kOuterW, A12, ld,
-                                                                                                 nr, kNB);
-                FLG_LAUNCH_CHECK();
+                if (!defer_t) {
+                    transpose_f32_kernel<<<dim3(kNB / 32, (unsigned)ceil_div(nr, 32)), tb, 0, st>>>(Ut, kOuterW, A12,
+                                                                                                     ld, nr, kNB);
+                    FLG_LAUNCH_CHECK();
+                }
                 FLG_TRY(tc_update(A21, ld, A21, ld, UinvT, kNB, nr, kNB, kNB, FLG_LU_TF32, tcw, tcb, st, dinfo + 1,
                                   true));
             } else if (nb == kNB) {
@@ -1457,7 +1478,7 @@ extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mod
                     // rows > c0 + 128 x its columns, rows > k0 x columns (c0 + 128, E)
                     FLG_TRY(tc_update(A22, ld, A21, ld, Ut, kOuterW, kNB, kNB, kNB, mode, tcw, tcb, st, dinfo + 1,
                                       false, tile));
-                    FLG_TRY(look_ahead(c0));
+                    FLG_TRY(look_ahead(c0, Deferred{Ut, A12, nr}));
                     FLG_TRY(tc_update(A22 + kNB * ld, ld, A21 + kNB * ld, ld, Ut, kOuterW, nr - kNB, kNB, kNB, mode,
                                       tcw, tcb, st, dinfo + 1, false, tile, cap));
                     if (E > c0 + kNB)
@@ -1482,7 +1503,7 @@ extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mod
                 // the next outer panel's first diagonal block first, then it factors beside the rest
                 FLG_TRY(tc_update(C, ld, Lp, ld, Up, kOuterW, kNB, kNB, E - K0, mode, tcw, tcb, st, dinfo + 1, false,
                                   tile));
-                FLG_TRY(look_ahead(E));
+                FLG_TRY(look_ahead(E, Deferred{}));
                 FLG_TRY(tc_update(C + kNB * ld, ld, Lp + kNB * ld, ld, Up, kOuterW, n - E - kNB, kNB, E - K0, mode,
                                   tcw, tcb, st, dinfo + 1, false, tile, cap));
                 FLG_TRY(tc_update(C + kNB, ld, Lp, ld, Up + kNB * kOuterW, kOuterW, n - E, n - E - kNB, E - K0, mode,
@@ -1495,6 +1516,10 @@ extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mod
         }
     }
     if (pending) FLG_CUDA(cudaStreamWaitEvent(st, side->join, 0));  // (every look-ahead is joined above)
+    if (side_busy) {  // the deferred transposes
+        FLG_CUDA(cudaEventRecord(side->tail, side->s));
+        FLG_CUDA(cudaStreamWaitEvent(st, side->tail, 0));
+    }
     return FLG_OK;
 }
 
