@@ -15,11 +15,14 @@
 // pivoting in FP32 storage, block FLG_LU_LOWP_BLOCK = 128; the diagonal block
 // is factored by one CTA, which also writes the inverses of its L and U
 // factors (kept in `dinv` for the solves); the panels are GEMMs with those
-// inverses; the trailing update runs on the tensor cores (tc_gemm.cu) or on
-// CUDA cores (FLG_LU_FP32).
+// inverses; the trailing update runs on the tensor cores (tc_gemm.cu, deferred
+// to one rank-512 update per outer panel of four blocks) or on CUDA cores
+// (FLG_LU_FP32).  With the tensor cores the next diagonal block runs ahead on
+// a side stream while the rest of each update finishes.
 //
-// Every spin-wait (the grid barrier) is bounded by a clock64 limit and
-// reports FLG_ERR_CUDA-style failure through a device flag instead of hanging.
+// Every spin-wait (the grid barrier, the diagonal block's warp handshake, the
+// solves' dataflow) is bounded by a clock64 limit and reports failure through
+// a device flag instead of hanging.
 #include <cooperative_groups.h>
 
 #include <algorithm>

@@ -4,8 +4,9 @@
 //   (or, in store mode, C = A * B^T)
 //
 // Both operands are K-major (K contiguous per row, K a multiple of 128).  A
-// persistent kernel, one CTA per SM, walks the 128 x BN tiles of C (BN = 256,
-// or 128 for narrow or small updates, chosen per call):
+// persistent kernel, one CTA per SM (the caller may cap the grid below the SM
+// count), walks the 128 x BN tiles of C (BN = 256, or 128 for narrow or small
+// updates, chosen per call):
 //   * warp 0 (one lane) streams K-blocks of A and B (128 B = 32 TF32 or 64 BF16
 //     per row) with TMA (cp.async.bulk.tensor, 128-byte swizzle) into a
 //     shared-memory ring guarded by mbarriers (4 stages at BN = 256, 6 at 128);
