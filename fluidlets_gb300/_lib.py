@@ -42,6 +42,8 @@ SIGNATURES = {
                                      c_double, _P, _P]),
     "flg_assemble": (c_int, [c_int, c_double, c_double, _P, c_int64, _P, _P, c_int64, c_double, c_double, _P,
                              c_int, c_int64, _P]),
+    "flg_assemble_self_uniform": (c_int, [c_int, c_double, c_double, _P, c_int64, c_double, c_double, c_double, _P,
+                                          c_int, c_int64, _P]),
     "flg_assemble_bucket": (c_int, [c_int, c_double, c_double, _P, _P, _P, c_int64, c_double, _P, c_int, c_int64,
                                     _P]),
     "flg_assemble_nearest_workspace": (c_size_t, [c_int64, c_int64]),

@@ -21,7 +21,7 @@ import numpy as np
 import torch
 
 from . import _device as dv
-from ._lib import BF16, C128, F32, F64, FLG_ERR_NOT_CONVERGED, PREC, check, load, lu_mode
+from ._lib import BF16, C128, F32, F64, FLG_ERR_NOT_CONVERGED, KIND, PREC, check, load, lu_mode
 from .kernels import kernel_params
 
 #: above this many unknowns, method="auto" switches from dense LU to GMRES (core/solve.py:20)
@@ -141,7 +141,20 @@ def evaluate_grid(kernel, axes, sources, strengths, eps, mu=1.0, *, precision="f
 
 
 # ---- core/assemble.py:27-101 ------------------------------------------------
-def _assemble_dev(kernel, X, Y, e, mu, out_dtype=torch.float64, out=None, ld=None):
+def _uniform_eps(eps):
+    """The blob width when it is one number (a scalar, or an array of equal entries on the
+    host), else None."""
+    if isinstance(eps, torch.Tensor):
+        return float(eps) if eps.numel() == 1 else None
+    a = np.asarray(eps, dtype=np.float64)
+    if a.size == 1:
+        return float(a.reshape(-1)[0])
+    return float(a.reshape(-1)[0]) if a.size and np.all(a == a.reshape(-1)[0]) else None
+
+
+def _assemble_dev(kernel, X, Y, e, mu, out_dtype=torch.float64, out=None, ld=None, sym_eps=None, reciprocal=False):
+    """sym_eps: the one blob width, when Y is X -- half the pair evaluations (bit-identical for
+    the free kernels; for the wall kernel only with reciprocal=True, equal to rounding)."""
     kind, are, aim = kernel_params(kernel)
     m, mu_c = _mu(mu)
     M, N = X.shape[0], Y.shape[0]
@@ -152,8 +165,12 @@ def _assemble_dev(kernel, X, Y, e, mu, out_dtype=torch.float64, out=None, ld=Non
     if out is None:
         out = torch.empty((3 * M, 3 * N), dtype=out_dtype, device=X.device)
         ld = 3 * N
-    st = load().flg_assemble(kind, are, aim, dv.ptr(X), M, dv.ptr(Y), dv.ptr(e), N, m.real, m.imag, dv.ptr(out),
-                             code, ld, dv.stream())
+    if sym_eps is not None and Y is X and (kind != KIND["wall"] or reciprocal):
+        st = load().flg_assemble_self_uniform(kind, are, aim, dv.ptr(X), N, sym_eps, m.real, m.imag, dv.ptr(out),
+                                              code, ld, dv.stream())
+    else:
+        st = load().flg_assemble(kind, are, aim, dv.ptr(X), M, dv.ptr(Y), dv.ptr(e), N, m.real, m.imag,
+                                 dv.ptr(out), code, ld, dv.stream())
     check(st, "assemble")
     if mu_c and not out.is_complex():
         out = out.to(torch.complex128)
@@ -380,7 +397,7 @@ def resistance(kernel, points, velocities, eps, mu=1.0, method="auto", rtol=1e-1
     rtol_ir = rtol * 1e-2 if prec == PREC["mixed"] else rtol
     resid = None
     if method == "lu":
-        K = _assemble_dev(kernel, X, X, e, mu)
+        K = _assemble_dev(kernel, X, X, e, mu, sym_eps=_uniform_eps(eps), reciprocal=prec == PREC["mixed"])
         if prec == PREC["mixed"] and not K.is_complex() and not Uc:
             # the refinement's last residual is ||U - K f|| / ||U|| with the FP64 K: reported as is
             f, iterations, ir_steps, resid = _mixed_lu_solve_dev(K, U, rtol_ir, restart, maxiter, lu, required=rtol)

@@ -1,6 +1,8 @@
 // assemble.cu -- dense mobility matrices and dense helpers.
 //
 //  flg_assemble            fluidlets.assemble (core/assemble.py:27-46, _fill 15-24)
+//  flg_assemble_self_uniform  the same for targets = sources and one blob width (half
+//                          the pair evaluations: the matrix is symmetric)
 //  flg_assemble_nearest    fluidlets.assemble_nearest (core/assemble.py:68-101,
 //                          _fill_nearest 49-58), deterministic segmented sum
 //  flg_swimmer_constraints the rows/columns of swimming.py:90-99
@@ -111,6 +113,44 @@ __global__ void __launch_bounds__(128) assemble_kernel(AsmArgs a) {
         double G[9], Gi[9];
         block_f64<KIND, CK>(a.tg[3 * i], a.tg[3 * i + 1], a.tg[3 * i + 2], sx, sy, sz, e2, a.are, a.aim, G, Gi);
         store_block(a, i, 3 * j, G, Gi, cplx);
+    }
+}
+
+// Self-assembly (targets = sources) with one blob width: the matrix is symmetric.  For the
+// free kernels block (j, i) equals block (i, j) bit for bit (d -> -d is exact and the block
+// depends on d only through products d_a d_b and |d|^2), so the mirror is written as is; for
+// the wall kernel it is the transpose (Lorentz reciprocity of the image system, equal to
+// rounding).  Thread j takes targets i <= j in tiles of kSymTile rows: it writes block (i, j)
+// (a warp covers contiguous row segments) and its mirror at (j, i) (per thread, three row
+// segments of 3 kSymTile entries per tile); half the pair evaluations of assemble_kernel.
+constexpr int kSymTile = 8;
+template <int KIND, bool CK, bool TRANSPOSE>
+__global__ void __launch_bounds__(128) assemble_sym_kernel(AsmArgs a, double e2) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= a.N) return;
+    const double sx = a.src[3 * j], sy = a.src[3 * j + 1], sz = a.src[3 * j + 2];
+    const bool cplx = CK || a.imu_im != 0.0;
+    for (int64_t i0 = (int64_t)blockIdx.y * kSymTile; i0 <= j; i0 += (int64_t)gridDim.y * kSymTile) {
+        for (int t = 0; t < kSymTile; t++) {
+            const int64_t i = i0 + t;
+            if (i > j) break;
+            double G[9], Gi[9];
+            block_f64<KIND, CK>(a.src[3 * i], a.src[3 * i + 1], a.src[3 * i + 2], sx, sy, sz, e2, a.are, a.aim, G,
+                                Gi);
+            store_block(a, i, 3 * j, G, Gi, cplx);
+            if (i == j) continue;
+            if (TRANSPOSE) {
+#pragma unroll
+                for (int r = 0; r < 3; r++)
+#pragma unroll
+                    for (int c = r + 1; c < 3; c++) {
+                        const double u = G[3 * r + c], v = Gi[3 * r + c];
+                        G[3 * r + c] = G[3 * c + r], Gi[3 * r + c] = Gi[3 * c + r];
+                        G[3 * c + r] = u, Gi[3 * c + r] = v;
+                    }
+            }
+            store_block(a, j, 3 * i, G, Gi, cplx);
+        }
     }
 }
 
@@ -512,6 +552,35 @@ extern "C" int flg_assemble(int kind, double alpha_re, double alpha_im, const do
     cudaStream_t st = as_stream(stream);
     prof_begin(FLG_SLOT_ASSEMBLE, st);
     dispatch<LaunchAsm>(kind, kind == FLG_BRINKMANLET && alpha_im != 0.0, asm_grid(M, N), 128, st, a);
+    FLG_LAUNCH_CHECK();
+    prof_end(FLG_SLOT_ASSEMBLE, st);
+    return FLG_OK;
+}
+
+extern "C" int flg_assemble_self_uniform(int kind, double alpha_re, double alpha_im, const double *points, int64_t N,
+                                         double eps, double mu_re, double mu_im, void *out, int out_type, int64_t ld,
+                                         void *stream) {
+    AsmArgs a{};
+    FLG_TRY(prepare(kind, alpha_re, alpha_im, mu_re, mu_im, out_type, a));
+    FLG_REQUIRE(N >= 0, "negative size");
+    FLG_REQUIRE(ld >= 3 * N, "ld (%lld) < 3N (%lld)", (long long)ld, (long long)(3 * N));
+    if (N == 0) return FLG_OK;
+    FLG_REQUIRE(points && out, "null pointer");
+    a.tg = points;
+    a.M = N;
+    a.src = points;
+    a.eps = nullptr;
+    a.N = N;
+    a.out = out;
+    a.ld = ld;
+    cudaStream_t st = as_stream(stream);
+    const dim3 grid((unsigned)ceil_div(N, 128), (unsigned)std::min<int64_t>(ceil_div(N, kSymTile), 65535));
+    const double e2 = eps * eps;
+    prof_begin(FLG_SLOT_ASSEMBLE, st);
+    if (kind == FLG_STOKESLET) assemble_sym_kernel<FLG_STOKESLET, false, false><<<grid, 128, 0, st>>>(a, e2);
+    else if (kind == FLG_WALL) assemble_sym_kernel<FLG_WALL, false, true><<<grid, 128, 0, st>>>(a, e2);
+    else if (alpha_im != 0.0) assemble_sym_kernel<FLG_BRINKMANLET, true, false><<<grid, 128, 0, st>>>(a, e2);
+    else assemble_sym_kernel<FLG_BRINKMANLET, false, false><<<grid, 128, 0, st>>>(a, e2);
     FLG_LAUNCH_CHECK();
     prof_end(FLG_SLOT_ASSEMBLE, st);
     return FLG_OK;

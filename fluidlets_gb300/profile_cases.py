@@ -121,7 +121,7 @@ def breakdown(a, kern):
 
     for rep in range(a.reps):
         L.flg_profile_enable(1)
-        K, t_asm = t(lambda: core._assemble_dev(kern, Xd, Xd, e, 1.0))
+        K, t_asm = t(lambda: core._assemble_dev(kern, Xd, Xd, e, 1.0, sym_eps=eps, reciprocal=True))
         (K32, ld32, dinv, A32), t_lu = t(lambda: core._lowp_factor_dev(K, a.lu))
         (x, it, outer, res), t_ir = t(lambda: core._gmres_ir_dense_dev(K, K32, ld32, dinv, b, 1e-12, 60, 200,
                                                                         required=1e-10, A32=A32))

@@ -19,7 +19,8 @@ import numpy as np
 import torch
 
 from . import _device as dv
-from .core import _assemble_dev, _blob_widths, _gmres_ir_dense_dev, _lowp_factor_dev, _lu_solve_dev, _points, _prec
+from .core import (_assemble_dev, _blob_widths, _gmres_ir_dense_dev, _lowp_factor_dev, _lu_solve_dev, _points, _prec,
+                   _uniform_eps)
 from .kernels import Stokeslet3D
 from .swimming import _system_dev
 
@@ -69,7 +70,7 @@ def resistance_matrix(kernel, points, eps, mu=1.0, center=None, *, precision="fp
         U[:, j, j] = 1.0
         U[:, :, 3 + j] = np.cross(np.eye(3)[j], r)
     Ud = torch.from_numpy(U.reshape(3 * N, 6)).to(Xd.device)
-    K = _assemble_dev(kernel, Xd, Xd, e, mu)
+    K = _assemble_dev(kernel, Xd, Xd, e, mu, sym_eps=_uniform_eps(eps), reciprocal=_prec(precision) == 1)
     if K.is_complex():
         raise ValueError("the resistance matrix needs a real kernel and viscosity")
     if _prec(precision) == 1:

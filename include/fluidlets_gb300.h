@@ -131,6 +131,16 @@ int flg_assemble(int kind, double alpha_re, double alpha_im,
                  double mu_re, double mu_im,
                  void *out, int out_type, int64_t ld, void *stream);
 
+/* The same matrix for targets = sources (points, N) and one blob width eps,
+ * from half the pair evaluations (the matrix is symmetric): for
+ * FLG_STOKESLET and FLG_BRINKMANLET bit-identical to flg_assemble with
+ * eps broadcast; for FLG_WALL the lower blocks are the transposes of the
+ * upper ones (Lorentz reciprocity), equal to flg_assemble's to rounding. */
+int flg_assemble_self_uniform(int kind, double alpha_re, double alpha_im,
+                              const double *points, int64_t N, double eps,
+                              double mu_re, double mu_im,
+                              void *out, int out_type, int64_t ld, void *stream);
+
 /* Assembly into a fixed-size bucket (used by the solve server's captured CUDA
  * graphs): points/eps hold n_cap entries of which the first *n_real (a DEVICE
  * int64) are real; the matrix (3 n_cap x 3 n_cap, ld) gets the kernel block

@@ -61,6 +61,28 @@ def test_assemble_low_precision_outputs():
     assert rel_err(Kbf.double().cpu().numpy(), K64.cpu().numpy()) < 1e-2
 
 
+@pytest.mark.parametrize("n", [1, 7, 130, 1037])
+def test_symmetric_self_assembly(n):
+    """Targets = sources with one blob width: half the pair evaluations, the mirror blocks
+    bit-identical to the direct ones for the free kernels (every output type, complex alpha and
+    mu) and equal to rounding for the wall kernel (reciprocity)."""
+    from fluidlets_gb300.core import _assemble_dev
+    rng = np.random.default_rng(n)
+    X = torch.tensor(np.c_[rng.uniform(-1, 1, (n, 2)), rng.uniform(0.05, 1.5, n)], device="cuda")
+    e = torch.full((n,), 0.07, dtype=torch.float64, device="cuda")
+    for k, mu in ((S3, 1.0), (fl.Brinkmanlet3D(2.5), 1.0), (fl.Brinkmanlet3D(1 + 2j), 1.0), (S3, 2 - 0.5j)):
+        for dt in (torch.float64, torch.float32, torch.bfloat16):
+            if dt != torch.float64 and (mu != 1.0 or complex(k.alpha).imag != 0.0):
+                continue  # complex outputs are complex128 whatever the requested type
+            a = _assemble_dev(k, X, X, e, mu, out_dtype=dt)
+            b = _assemble_dev(k, X, X, e, mu, out_dtype=dt, sym_eps=0.07)
+            assert torch.equal(a, b), (k, mu, dt)
+    a = _assemble_dev(W, X, X, e, 1.0)
+    b = _assemble_dev(W, X, X, e, 1.0, sym_eps=0.07, reciprocal=True)
+    assert rel_err(b.cpu().numpy(), a.cpu().numpy()) < 1e-14
+    assert torch.equal(_assemble_dev(W, X, X, e, 1.0, sym_eps=0.07), a)  # no reciprocity asked: the direct kernel
+
+
 def test_assemble_nearest_matches_reference(golden):
     g = golden
     xc, Xq, nn = g["an_coarse"], g["an_quad"], g["an_nearest"]
