@@ -73,3 +73,17 @@ def test_unknown_lu_name_is_a_value_error(lib):
     for bad in ("tf16", "fp32:128", "tf32:64", None):
         with pytest.raises(ValueError):
             lib.lu_mode(bad)
+
+
+def test_uniform_blob_width_detection():
+    """The symmetric self-assembly is chosen only for one blob width: a scalar, a one-element
+    tensor, or a host array of equal entries (device arrays are not inspected)."""
+    import numpy as np
+    import torch
+
+    from fluidlets_gb300.core import _uniform_eps
+    assert _uniform_eps(0.25) == 0.25 and _uniform_eps(np.float64(0.5)) == 0.5
+    assert _uniform_eps(np.full(7, 0.1)) == 0.1 and _uniform_eps([0.2, 0.2]) == 0.2
+    assert _uniform_eps(np.array([0.1, 0.2])) is None
+    assert _uniform_eps(torch.tensor(0.3, dtype=torch.float64)) == 0.3
+    assert _uniform_eps(torch.full((5,), 0.3, dtype=torch.float64)) is None
