@@ -1291,7 +1291,7 @@ extern "C" int flg_lu_solve_f64(int64_t n, int64_t nrhs, const double *LU, int64
 struct SideStream {
     int dev = -1;
     cudaStream_t s = nullptr;
-    cudaEvent_t fork = nullptr, join = nullptr, tail = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr, tail = nullptr, lfork = nullptr, ljoin = nullptr;
 };
 static int side_stream(SideStream **out) {
     thread_local SideStream ss;
@@ -1304,6 +1304,8 @@ static int side_stream(SideStream **out) {
         FLG_CUDA(cudaEventCreateWithFlags(&ss.fork, cudaEventDisableTiming));
         FLG_CUDA(cudaEventCreateWithFlags(&ss.join, cudaEventDisableTiming));
         FLG_CUDA(cudaEventCreateWithFlags(&ss.tail, cudaEventDisableTiming));
+        FLG_CUDA(cudaEventCreateWithFlags(&ss.lfork, cudaEventDisableTiming));
+        FLG_CUDA(cudaEventCreateWithFlags(&ss.ljoin, cudaEventDisableTiming));
         ss.dev = dev;
     }
     *out = &ss;
@@ -1446,7 +1448,15 @@ extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mod
             if (tcp) {
                 // panels on the tensor cores (TF32 in both tensor-core modes):
                 //   Ut = A12^T Linv^T (the K-major copy the updates read), then A12 = Ut^T;
-                //   L21 = A21 Uinv, in place (each tile's rows are read in full before they are stored)
+                //   L21 = A21 Uinv, in place (each tile's rows are read in full before they are stored),
+                //   on the side stream beside the U panel (TF32 store mode touches no shared
+                //   workspace); the updates below join it, and the next diagonal kernel, which
+                //   rewrites Uinv^T, follows it on the side stream
+                FLG_CUDA(cudaEventRecord(side->lfork, st));
+                FLG_CUDA(cudaStreamWaitEvent(side->s, side->lfork, 0));
+                FLG_TRY(tc_update(A21, ld, A21, ld, UinvT, kNB, nr, kNB, kNB, FLG_LU_TF32, tcw, tcb, side->s,
+                                  dinfo + 1, true));
+                FLG_CUDA(cudaEventRecord(side->ljoin, side->s));
                 transpose_f32_kernel<<<dim3((unsigned)ceil_div(nr, 32), kNB / 32), tb, 0, st>>>(A12, ld, T12, kNB,
                                                                                                  kNB, nr);
                 FLG_LAUNCH_CHECK();
@@ -1457,8 +1467,7 @@ extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mod
                                                                                                      ld, nr, kNB);
                     FLG_LAUNCH_CHECK();
                 }
-                FLG_TRY(tc_update(A21, ld, A21, ld, UinvT, kNB, nr, kNB, kNB, FLG_LU_TF32, tcw, tcb, st, dinfo + 1,
-                                  true));
+                FLG_CUDA(cudaStreamWaitEvent(st, side->ljoin, 0));
             } else if (nb == kNB) {
                 // U12 = Linv A12 (+ its K-major copy), L21 = A21 Uinv: one launch, in place
                 const int ntu = (int)ceil_div(nr, 32), ntl = (int)ceil_div(nr, 32);
