@@ -46,7 +46,9 @@ def parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--cpu-sample", type=int, default=2048, help="targets in the CPU sample (x all sources)")
+    p.add_argument("--cpu-sample", type=int, default=16384, help="targets in the CPU slice (x all sources)")
+    p.add_argument("--cpu-chunk", type=int, default=2048,
+                   help="targets of the CPU slice timed per step of --impl reference (the slice in turn)")
     p.add_argument("--no-extras", action="store_true", help="skip the accuracy / FP64 / solve sections")
     p.add_argument("--workload", default="wall_sum", choices=["wall_sum", "brinkman_gmres", "wall_lu", "serve"],
                    help="wall_sum (default, the headline) or one of the other benchmark configurations")
@@ -54,6 +56,17 @@ def parse():
     p.add_argument("--fp64", action="store_true", help="also run the plain FP64 GPU solve (slow at full size)")
     p.add_argument("--slots", type=int, default=6, help="solve-server slots (serve workload)")
     p.add_argument("--rates", default="50,200,800", help="Poisson arrival rates (serve workload)")
+    # one hot-path operation at a chosen size, for profiler captures (no JSON line)
+    p.add_argument("--case", default=None, choices=["sum", "assemble", "lu", "resistance", "breakdown", "swim"],
+                   help="run one operation at a chosen size for a profiler capture instead of the benchmark")
+    p.add_argument("--kind", default="wall", choices=["stokeslet", "wall", "brinkman"])
+    p.add_argument("--alpha", type=complex, default=0.0)
+    p.add_argument("--targets", type=int, default=65536)
+    p.add_argument("--sources", type=int, default=262144)
+    p.add_argument("--precision", default="mixed")
+    p.add_argument("--n", type=int, default=1536, help="points for the assemble / lu / resistance cases")
+    p.add_argument("--lu", default="tf32")
+    p.add_argument("--reps", type=int, default=2)
     return p.parse_args()
 
 
@@ -144,16 +157,20 @@ def make_workload(seed):
     return wall_sum_workload(N_SRC, N_TGT, N_WALL, EPS, seed=seed)
 
 
-def cpu_sample_rate(T, S, F, eps, n_targets):
-    """The oracle (C/OpenMP restatement of the reference loop) on all host cores."""
+def cpu_slice(T, n_targets):
+    """The CPU baseline's slice of the targets: n_targets of them, evenly strided over the set."""
+    return T[:: max(1, len(T) // n_targets)][:n_targets]
+
+
+def cpu_sample_rate(sub, S, F, eps):
+    """The oracle (C/OpenMP restatement of the reference loop, -O3) on all host cores."""
     import oracle
 
     threads = oracle.max_threads()
-    sub = T[:: max(1, len(T) // n_targets)][:n_targets]
     t0 = time.perf_counter()
     oracle.evaluate("wall", sub, S, F, eps)
     dt = time.perf_counter() - t0
-    return len(sub) * len(S) / dt, threads, f"{len(sub)} targets x {len(S)} sources (WallStokeslet3D, FP64)"
+    return len(sub) * len(S) / dt, threads
 
 
 def run_reference(args):
@@ -165,12 +182,21 @@ def run_reference(args):
     import oracle
 
     oracle.build()
+    sl = cpu_slice(T, args.cpu_sample)
+    nchunk = max(1, len(sl) // args.cpu_chunk)
+    pairs = []
     for i in range(args.warmup + args.steps):
-        r, threads, sample = cpu_sample_rate(T[i % 7:], S, F, eps, args.cpu_sample)
+        c = i % nchunk
+        sub = sl[c * args.cpu_chunk:(c + 1) * args.cpu_chunk]
+        r, threads = cpu_sample_rate(sub, S, F, eps)
         if i >= args.warmup:
             rates.append(r)
-    total_pairs = args.cpu_sample * N_SRC * args.steps
-    total_time = sum(args.cpu_sample * N_SRC / r for r in rates)
+            pairs.append(len(sub) * N_SRC)
+    sample = (f"{len(sl)}-target slice (every {max(1, len(T) // args.cpu_sample)}th target) x {N_SRC} sources, "
+              f"{args.cpu_chunk} targets of it per step in turn (WallStokeslet3D, FP64); pairs/s scale linearly "
+              "to the full 278,528 x 262,144 sum")
+    total_pairs = sum(pairs)
+    total_time = sum(p / r for p, r in zip(pairs, rates))
     value = total_pairs / total_time
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_time / args.steps,
@@ -238,6 +264,56 @@ def solve_section(dev, n_points=1536, reps=5):
     for lu in ("tf32", "bf16"):
         res[f"mixed_{lu}"]["speedup_vs_faster_fp64"] = base / res[f"mixed_{lu}"]["ms_mean"]
     return res
+
+
+def wall_lu_section(dev, n_points=8192, h=1.05, reps=3):
+    """Mixed-precision dense resistance near a wall: sphere radius 1, N Fibonacci points centred at
+    h/a over z = 0, eps = 0.25 x mean NN spacing, WallStokeslet3D, translation parallel to the wall
+    (3N unknowns); TF32 and BF16 tensor-core LU + FP64 GMRES-IR against one FP64 GPU LU."""
+    import torch
+
+    import fluidlets_gb300 as fl
+    from fluidlets_gb300.geometry import fibonacci_sphere, mean_nn_spacing
+
+    S = fibonacci_sphere(n_points)
+    eps = 0.25 * mean_nn_spacing(S)
+    X = torch.from_numpy(S + [0.0, 0.0, h]).to(dev)
+    e = torch.full((n_points,), eps, dtype=torch.float64, device=dev)
+    U = torch.zeros_like(X)
+    U[:, 0] = 1.0
+    k = fl.WallStokeslet3D()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    F64, i64 = fl.resistance(k, X, U, e, method="lu")
+    torch.cuda.synchronize()
+    res = {"workload": f"WallStokeslet3D resistance, sphere N={n_points} ({3 * n_points} unknowns) at h/a={h}, "
+                       f"eps={eps:.7f}, translation parallel to the wall, dense LU",
+           "fp64_gpu": {"ms": 1e3 * (time.perf_counter() - t0), "residual": i64.residual},
+           "drag_x": float(F64[:, 0].sum())}
+    for lu in ("tf32", "bf16"):
+        fl.resistance(k, X, U, e, method="lu", precision="mixed", lu=lu)  # warm-up
+        ms = []
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            Fm, im = fl.resistance(k, X, U, e, method="lu", precision="mixed", lu=lu)
+            torch.cuda.synchronize()
+            ms.append(1e3 * (time.perf_counter() - t0))
+        err = float(torch.linalg.vector_norm(Fm - F64) / torch.linalg.vector_norm(F64))
+        res[f"mixed_{lu}"] = {"ms_mean": float(np.mean(ms)), "solves_per_s": float(1e3 / np.mean(ms)),
+                              "rel_force_err_vs_fp64": err, "residual": im.residual, "ir_steps": im.ir_steps,
+                              "gmres_iterations": im.iterations,
+                              "speedup_vs_fp64": res["fp64_gpu"]["ms"] / float(np.mean(ms))}
+    return res
+
+
+def serve_section(n_requests=512, rate=200.0, slots=6):
+    """A short served run of the mixed workload (the serve workload's generator): n_requests
+    Poisson arrivals at `rate`/s through the continuous-batching server; p50 / p99 latency and
+    solves/s (warm-up and per-bucket autotuning before the timed run)."""
+    from fluidlets_gb300.serve import serve_run
+
+    return serve_run(n_requests=n_requests, rate=rate, slots=slots)
 
 
 def run_ours(args):
@@ -318,13 +394,30 @@ def run_ours(args):
 
     far_avg_ms = far_ms.value / max(far_n.value, 1)
     achieved = FLOPS_PER_PAIR * pairs / (far_avg_ms * 1e-3) / 1e12
-    traffic = None
+    traffic, prof_data = None, {}
     prof = ROOT / "profiles" / "far_f32_wall_traffic.json"
     if prof.exists():
         try:
-            traffic = json.loads(prof.read_text()).get("bytes_per_launch_full_size")
+            prof_data = json.loads(prof.read_text())
+            traffic = prof_data.get("bytes_per_launch_full_size")
         except (ValueError, OSError):
             traffic = None
+    # executed-instruction view beside the canonical-flop fraction: the live pair rate times the
+    # instructions per pair that ncu counted, against the issue peak (one warp instruction per
+    # SM sub-partition per clock) at the SM clock seen during the timed region
+    clocks = clk.summary()
+    executed = None
+    ipp = prof_data.get("thread_instructions_per_pair")
+    if ipp and clocks.get("sm_mhz"):
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        issue_peak = sms * 4 * clocks["sm_mhz"] * 1e6          # warp instructions / s
+        achieved_issue = pairs / (far_avg_ms * 1e-3) * ipp / 32  # warp instructions / s
+        executed = {"thread_instructions_per_pair": ipp, "issue_frac": achieved_issue / issue_peak,
+                    "fma_pipe_pct_ncu": prof_data.get("fma_pipe_pct"),
+                    "issue_active_pct_ncu": prof_data.get("issue_active_pct"),
+                    "note": "frac above counts canonical flops (106 per pair); the kernel issues fewer "
+                            "instructions than that count implies, so its frac can exceed 1 while the "
+                            "issue slots are not all used"}
     line = {
         "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -333,14 +426,15 @@ def run_ours(args):
         "config": {"workload": WORKLOAD, "targets": len(T), "sources": len(S), "eps": eps,
                    "precision": "mixed", "l2": "flushed (256 MB write) between timed steps",
                    "parallelism": f"replicas x{world}"},
-        "clocks": clk.summary(),
+        "clocks": clocks,
         "e2e": {"value": e2e_value, "unit": "pairs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak.value, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak.value, "traffic": traffic,
                      "kernel": "far_f32_kernel", "flops_per_pair": FLOPS_PER_PAIR,
                      "peak_source": "FFMA microbenchmark measured in this run (of measured)",
-                     "far_ms_per_launch": far_avg_ms, "near_ms_per_launch": near_ms.value / max(near_n.value, 1)},
+                     "far_ms_per_launch": far_avg_ms, "near_ms_per_launch": near_ms.value / max(near_n.value, 1),
+                     "executed": executed},
         "fp64_peak_tflops": fp64_peak.value,
     }
     if rank == 0 and not args.no_extras:
@@ -362,9 +456,14 @@ def run_ours(args):
                                  "sample": f"{len(idx)} targets x {N_SRC} sources",
                                  "mixed_speedup": value / world / fp64_rate}
         line["solves"] = solve_section(dev)
-        rate, threads, sample = cpu_sample_rate(T, S, F, eps, args.cpu_sample)
+        line["wall_lu"] = wall_lu_section(dev)
+        line["served"] = serve_section()
+        sub = cpu_slice(T, args.cpu_sample)
+        rate, threads = cpu_sample_rate(sub, S, F, eps)
         line["cpu_baseline"] = {"value": rate, "unit": "pairs/s", "cores": threads, "kind": "port",
-                                "sample": sample}
+                                "sample": f"{len(sub)}-target slice (every {max(1, len(T) // args.cpu_sample)}th "
+                                          f"target) x {N_SRC} sources (WallStokeslet3D, FP64); pairs/s scale "
+                                          "linearly to the full sum"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
@@ -477,8 +576,146 @@ def run_wall_lu(args):
     print(json.dumps(out), flush=True)
 
 
+def run_case(a):
+    """One hot-path operation at a chosen size (for profiler captures); inputs are the seeded
+    synthetic workloads of this file at reduced size."""
+    import torch
+
+    import fluidlets_gb300 as fl
+    from fluidlets_gb300 import core
+    from fluidlets_gb300.geometry import fibonacci_sphere, mean_nn_spacing, wall_sum_workload
+
+    dev = torch.device("cuda")
+    kern = {"stokeslet": fl.Stokeslet3D(), "wall": fl.WallStokeslet3D()}.get(a.kind) or fl.Brinkmanlet3D(a.alpha)
+    if a.case == "sum":
+        T, S, F, eps = wall_sum_workload(a.sources, a.targets, 0, 0.01, seed=0)
+        Td, Sd, Fd = (torch.from_numpy(x).to(dev) for x in (T, S, F))
+        for _ in range(a.reps):
+            fl.evaluate(kern, Td, Sd, Fd, eps, precision=a.precision)
+        torch.cuda.synchronize()
+    elif a.case == "breakdown":
+        case_breakdown(a, kern)
+    elif a.case == "swim":
+        case_swim(a)
+    else:
+        X = fibonacci_sphere(a.n) + (np.array([0, 0, 1.5]) if a.kind == "wall" else 0)
+        eps = 0.25 * mean_nn_spacing(X)
+        Xd = torch.from_numpy(X).to(dev)
+        U = torch.zeros_like(Xd)
+        U[:, 0] = 1.0
+        for _ in range(a.reps):
+            t0 = time.perf_counter()
+            if a.case == "assemble":
+                fl.assemble(kern, Xd, Xd, eps)
+            elif a.case == "lu":
+                core.resistance(kern, Xd, U, eps, method="lu", precision=a.precision, lu=a.lu)
+            else:
+                core.resistance(kern, Xd, U, eps, precision=a.precision, lu=a.lu)
+            torch.cuda.synchronize()
+            print(f"{a.case} n={a.n}: {1e3 * (time.perf_counter() - t0):.2f} ms")
+
+
+def case_swim(a):
+    """swim() of the biflagellate swimmer over one beat period (RK45, rtol 1e-6): FP64 solves per
+    stage vs the captured mixed-precision stage graph; time per right-hand side.  Flagellum
+    amplitude 0.08, so the two mirror-image flagella (attached at z = +-0.1) never touch (with 0.2
+    they cross and the system is near-singular there); nearest map fixed at t = 0 (the flagellum
+    quadrature points sit midway between force points, so a recomputed map would flip and make
+    the right-hand side discontinuous)."""
+    import torch
+
+    import fluidlets_gb300 as fl
+    from fluidlets_gb300.geometry import biflagellate_shape
+
+    calls = {"n": 0}
+
+    def shape_at(t):
+        calls["n"] += 1
+        return biflagellate_shape(t, amplitude=0.08)
+
+    s0 = biflagellate_shape(0.0, amplitude=0.08)
+    out = {}
+    for prec in ("fp64", "mixed", "mixed"):  # the second mixed run is timed warm
+        calls["n"] = 0
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        tr = fl.swim(shape_at, (0.0, 1.0), 0.02, rtol=1e-6, atol=1e-9, fixed_nearest=True, precision=prec)
+        torch.cuda.synchronize()
+        out[prec] = (time.perf_counter() - t0, calls["n"], tr)
+    t64, n64, tr64 = out["fp64"]
+    tmx, nmx, trmx = out["mixed"]
+    dx = np.abs(tr64.x0[-1] - trmx.x0[-1]).max()
+    print(f"swim: N={len(s0.x)} force / {len(s0.X)} quadrature points, n={3 * len(s0.x) + 6}; "
+          f"fp64 {t64 * 1e3:.0f} ms for {n64} right-hand sides ({t64 / n64 * 1e3:.2f} ms each); "
+          f"mixed {tmx * 1e3:.0f} ms for {nmx} ({tmx / nmx * 1e3:.2f} ms each); final position difference {dx:.1e}")
+
+
+def case_breakdown(a, kern):
+    """Phase times of one mixed-precision dense resistance solve (assembly, FP32 copy,
+    tensor-core LU, FP64 GMRES-IR, final FP64 residual) and of the FP64 LU."""
+    import ctypes
+
+    import torch
+
+    from fluidlets_gb300 import _lib, core
+    from fluidlets_gb300.geometry import fibonacci_sphere, mean_nn_spacing
+
+    L = _lib.load()
+    dev = torch.device("cuda")
+    X = fibonacci_sphere(a.n) + (np.array([0, 0, 1.5]) if a.kind == "wall" else 0)
+    eps = 0.25 * mean_nn_spacing(X)
+    Xd = torch.from_numpy(X).to(dev)
+    e = torch.full((a.n,), eps, dtype=torch.float64, device=dev)
+    U = torch.zeros_like(Xd)
+    U[:, 0] = 1.0
+    b = U.reshape(-1).contiguous()
+
+    def t(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = fn()
+        torch.cuda.synchronize()
+        return out, 1e3 * (time.perf_counter() - t0)
+
+    for rep in range(a.reps):
+        L.flg_profile_enable(1)
+        K, t_asm = t(lambda: core._assemble_dev(kern, Xd, Xd, e, 1.0, sym_eps=eps, reciprocal=True))
+        (K32, ld32, dinv, A32), t_lu = t(lambda: core._lowp_factor_dev(K, a.lu))
+        (x, it, outer, res), t_ir = t(lambda: core._gmres_ir_dense_dev(K, K32, ld32, dinv, b, 1e-12, 60, 200,
+                                                                        required=1e-10, A32=A32))
+        _, t_res = t(lambda: core._evaluate_dev(kern, Xd, Xd, x.reshape(-1, 3), e, 1.0, "fp64"))
+        slots = {}
+        for name, k in _lib.SLOT.items():
+            ms, n = ctypes.c_double(0), ctypes.c_int64(0)
+            L.flg_profile_read(k, ctypes.byref(ms), ctypes.byref(n))
+            if n.value:
+                slots[name] = (round(ms.value, 3), n.value)
+        L.flg_profile_enable(0)
+        print(f"[mixed {a.lu}] n={3 * a.n}: assemble {t_asm:.2f} ms, convert+LU {t_lu:.2f} ms, GMRES-IR {t_ir:.2f} ms "
+              f"({it} it, {outer} IR, resid {res:.2e}), residual {t_res:.2f} ms; kernel slots (ms, launches): {slots}")
+    if a.n > 4096:  # the FP64 factorizations take seconds at this size
+        return
+    K = core._assemble_dev(kern, Xd, Xd, e, 1.0)
+    L.flg_profile_enable(1)
+    _, t64 = t(lambda: core._lu_solve_dev(K.clone(), b))
+    slots = {}
+    for name, k in _lib.SLOT.items():
+        ms, n = ctypes.c_double(0), ctypes.c_int64(0)
+        L.flg_profile_read(k, ctypes.byref(ms), ctypes.byref(n))
+        if n.value:
+            slots[name] = (round(ms.value, 3), n.value)
+    L.flg_profile_enable(0)
+    print(f"[fp64] kernel slots (ms, launches): {slots}")
+    torch.linalg.solve(K, b)  # library initialization outside the timing
+    _, tcs = t(lambda: torch.linalg.solve(K, b))
+    print(f"[fp64] LU factor+solve {t64:.2f} ms; cuSOLVER (torch.linalg.solve) {tcs:.2f} ms")
+
+
+
 def main():
     args = parse()
+    if args.case:
+        return run_case(args)
     if args.impl != "reference" and args.workload == "brinkman_gmres":
         return run_brinkman_gmres(args)
     if args.impl != "reference" and args.workload == "wall_lu":

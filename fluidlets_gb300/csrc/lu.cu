@@ -1288,15 +1288,20 @@ extern "C" int flg_lu_solve_f64(int64_t n, int64_t nrhs, const double *LU, int64
 // Per host thread and device: the stream that runs the next diagonal block while the
 // trailing update finishes (highest priority), and the events of that fork and join.
 // Created on first use; an LU captured in a graph makes one eager pass first.
+// One set per device ordinal, so a thread that moves between GPUs keeps (and reuses) each
+// device's stream and events instead of creating new ones on every switch.
 struct SideStream {
     int dev = -1;
     cudaStream_t s = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr, tail = nullptr, lfork = nullptr, ljoin = nullptr;
 };
+constexpr int kSideStreamDevices = 64;
 static int side_stream(SideStream **out) {
-    thread_local SideStream ss;
+    thread_local SideStream per_dev[kSideStreamDevices];
     int dev = 0;
     FLG_CUDA(cudaGetDevice(&dev));
+    FLG_REQUIRE(dev >= 0 && dev < kSideStreamDevices, "device ordinal %d out of range", dev);
+    SideStream &ss = per_dev[dev];
     if (ss.dev != dev) {
         int lo = 0, hi = 0;
         FLG_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));

@@ -1,10 +1,12 @@
 """Point sets used to build the benchmark and test workloads.
 
-``fibonacci_sphere`` is the golden-angle spiral of the reference's
-``geometry/spheres.py:7-13``; ``cube_sphere`` its six-patch sphere (33-52).
-``spheroid`` and ``workload_*`` generate the synthetic, seeded inputs of the
-benchmark configurations.  The ``*_device`` functions build the same point sets
-(and the mean nearest-neighbour spacing) on the GPU, as CUDA tensors.
+The sphere discretizations of the reference (``geometry/spheres.py``: the
+golden-angle spiral and the six-patch cube sphere) and the mean
+nearest-neighbour spacing that sets blob widths are generated on the GPU by
+``csrc/geometry.cu``; the ``*_device`` functions return CUDA tensors, the plain
+names NumPy arrays.  ``spheroid`` and the ``*_workload`` / ``*_shape``
+functions build the synthetic, seeded inputs of the benchmark configurations
+from them.
 """
 from __future__ import annotations
 
@@ -12,36 +14,19 @@ import numpy as np
 
 
 def fibonacci_sphere(n: int, radius: float = 1.0, center=(0.0, 0.0, 0.0)) -> np.ndarray:
-    """n nearly uniform points on a sphere (golden-angle spiral), shape (n, 3)."""
-    k = np.arange(n) + 0.5
-    phi = np.arccos(1 - 2 * k / n)
-    theta = np.pi * (1 + np.sqrt(5)) * k
-    unit = np.c_[np.cos(theta) * np.sin(phi), np.sin(theta) * np.sin(phi), np.cos(phi)]
-    return radius * unit + np.asarray(center, float)
+    """n nearly uniform points on a sphere (golden-angle spiral), shape (n, 3), generated on the GPU."""
+    return fibonacci_sphere_device(n, radius, center).cpu().numpy()
 
 
 def cube_sphere(n: int, radius: float = 1.0, center=(0.0, 0.0, 0.0)) -> np.ndarray:
-    """Six n x n cell-centred patches of the cube projected onto the sphere: 6 n^2 points."""
-    s = np.linspace(-1.0 + 1.0 / n, 1.0 - 1.0 / n, n)
-    A, B = np.meshgrid(s, s, indexing="ij")
-    A, B, one = A.ravel(), B.ravel(), np.ones(n * n)
-    faces = []
-    for axis in range(3):
-        for sign in (-1.0, 1.0):
-            cols = [A, B]
-            cols.insert(axis, sign * one)
-            faces.append(np.c_[cols[0], cols[1], cols[2]])
-    cube = np.vstack(faces)
-    unit = cube / np.linalg.norm(cube, axis=1)[:, None]
-    return radius * unit + np.asarray(center, float)
+    """Six n x n cell-centred patches of the cube projected onto the sphere: 6 n^2 points,
+    generated on the GPU."""
+    return cube_sphere_device(n, radius, center).cpu().numpy()
 
 
-def mean_nn_spacing(points: np.ndarray) -> float:
-    """Mean nearest-neighbour distance (k-d tree)."""
-    from scipy.spatial import cKDTree
-
-    d, _ = cKDTree(points).query(points, k=2)
-    return float(d[:, 1].mean())
+def mean_nn_spacing(points) -> float:
+    """Mean nearest-neighbour distance (exhaustive search on the GPU)."""
+    return mean_nn_spacing_device(points)
 
 
 def spheroid(n: int, aspect: float, rotation: np.ndarray | None = None, center=(0.0, 0.0, 0.0)) -> np.ndarray:

@@ -461,6 +461,52 @@ def make_requests(n_requests=4096, seed=0):
     return reqs
 
 
+def _warm(srv, reqs):
+    """One request per (type, bucket, kernel) in use: builds and autotunes their plans."""
+    warm = {}
+    for r in reqs:
+        key = (type(r).__name__, bucket_of(len(r.points)) if isinstance(r, ResistanceRequest) else 0,
+               type(getattr(r, "kernel", None)).__name__)
+        warm.setdefault(key, r)
+    for f in [srv.submit(r) for r in warm.values()]:
+        f.result()
+
+
+def _poisson_run(srv, reqs, rate, seed):
+    """Submit reqs at Poisson arrival times (rate per second); latency percentiles and throughput."""
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, size=len(reqs))
+    t0 = time.perf_counter()
+    arrivals = t0 + np.cumsum(gaps)
+    futs = []
+    for r, ta in zip(reqs, arrivals):
+        now = time.perf_counter()
+        if ta > now:
+            time.sleep(ta - now)
+        futs.append(srv.submit(r, t_arrival=ta))
+    res = [f.result() for f in futs]
+    t_end = max(x.t_done for x in res)
+    lat = np.array([x.latency for x in res]) * 1e3
+    resid = np.array([x.residual for x in res if np.isfinite(x.residual)])
+    return {"rate_per_s": rate, "requests": len(res), "solves_per_s": len(res) / (t_end - t0),
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "max_residual": float(resid.max()) if len(resid) else None}
+
+
+def serve_run(n_requests=512, rate=200.0, slots=6, seed=0):
+    """A served run of the mixed workload at one arrival rate: p50 / p99 latency, solves/s and the
+    server's counters (warm-up and per-bucket autotuning of the buckets in use happen first)."""
+    reqs = make_requests(n_requests, seed=seed)
+    with SolveServer(slots=slots) as srv:
+        _warm(srv, reqs)
+        line = _poisson_run(srv, reqs, rate, int(rate))
+        stats = dict(srv.stats)
+    line["workload"] = (f"served mixed workload: {n_requests} requests (75% rigid bodies N log-uniform [256, 6144], "
+                        f"25% biflagellate swimmers), Poisson arrivals at {rate:g}/s, {slots} slots, HBM budget 150 GB")
+    line["server_stats"] = {k: (v if not isinstance(v, list) else len(v)) for k, v in stats.items()}
+    return line
+
+
 def bench_serving(args):
     """Poisson arrivals at rates {50, 200, 800}/s over the mixed workload, served with continuous
     batching; p50 / p99 latency and solves/s, and the one-solve-at-a-time FP64 GPU service time on a
@@ -479,31 +525,9 @@ def bench_serving(args):
     with SolveServer(slots=slots) as srv:
         srv_stats = srv.stats
         # warm-up and autotuning of the buckets in use, outside the timed runs
-        warm = {}
-        for r in reqs:
-            key = (type(r).__name__, bucket_of(len(r.points)) if isinstance(r, ResistanceRequest) else 0,
-                   type(getattr(r, "kernel", None)).__name__)
-            warm.setdefault(key, r)
-        for f in [srv.submit(r) for r in warm.values()]:
-            f.result()
+        _warm(srv, reqs)
         for rate in rates:
-            rng = np.random.default_rng(int(rate))
-            gaps = rng.exponential(1.0 / rate, size=len(reqs))
-            t0 = time.perf_counter()
-            arrivals = t0 + np.cumsum(gaps)
-            futs = []
-            for r, ta in zip(reqs, arrivals):
-                now = time.perf_counter()
-                if ta > now:
-                    time.sleep(ta - now)
-                futs.append(srv.submit(r, t_arrival=ta))
-            res = [f.result() for f in futs]
-            t_end = max(x.t_done for x in res)
-            lat = np.array([x.latency for x in res]) * 1e3
-            resid = np.array([x.residual for x in res if np.isfinite(x.residual)])
-            line = {"rate_per_s": rate, "requests": len(res), "solves_per_s": len(res) / (t_end - t0),
-                    "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-                    "max_residual": float(resid.max()) if len(resid) else None}
+            line = _poisson_run(srv, reqs, rate, int(rate))
             out["rates"].append(line)
             print(json.dumps(line), flush=True)
     out["server_stats"] = {k: (v if not isinstance(v, list) else len(v)) for k, v in srv_stats.items()}

@@ -104,13 +104,23 @@ int flg_evaluate(int kind, double alpha_re, double alpha_im,
  * flg_evaluate either.  It calls no cudaMalloc, cudaFree or other allocating
  * routine: its scratch (the per-split partial sums) is a fixed array of
  * flg_evaluate_noalloc_max_bytes() = 16 MiB of device memory that every GPU
- * loading the library holds until the process exits.  Limit: the targets
- * must satisfy M * 24 bytes (real output) or M * 48 bytes (complex) <= 16 MiB,
- * i.e. M <= 699,050 real / 349,525 complex; larger M returns FLG_ERR_INVALID.
- * The first call on each device looks up the array's device address (with
- * that device current); make that first call before any stream capture.
- * All calls share the one array, so calls whose work overlaps on the GPU
- * (different streams, or different host threads) race: serialize them. */
+ * loading the library holds until the process exits.  Limit: 48 bytes of
+ * scratch per target with complex strengths or a complex Brinkman alpha, 24
+ * bytes otherwise (a complex mu alone keeps 24), so M <= 349,525 or 699,050
+ * targets; larger M returns FLG_ERR_INVALID.  The scratch is split between
+ * source splits; with many targets the call runs fewer, longer splits.
+ * The array is module data: under CUDA's default lazy module loading it is
+ * allocated, with this file's kernels, on the first use of any of them on a
+ * device.  A caller that reserves the device memory for its own pool must
+ * therefore make its first call of this function (or of flg_evaluate) on each
+ * device before that reservation, or run with CUDA_MODULE_LOADING=EAGER.
+ * The first call on each device also looks up the array's device address
+ * (with that device current) and caches it; make that first call before any
+ * stream capture.  cudaDeviceReset recreates the module and invalidates the
+ * cached address: do not call this function after a reset in the same process.
+ * All calls share the one array and it keeps the last call's contents; calls
+ * whose work overlaps on the GPU (different streams, or different host
+ * threads) race: serialize them. */
 size_t flg_evaluate_noalloc_max_bytes(void);
 int flg_evaluate_noalloc(int kind, double alpha_re, double alpha_im,
                          const double *targets, int64_t M,

@@ -45,7 +45,7 @@ def build(force: bool = False) -> Path:
         return LIB_PATH
     LIB_PATH.parent.mkdir(exist_ok=True)
     tmp = LIB_PATH.with_suffix(f".so.{os.getpid()}")
-    cmd = ["gcc", "-O2", "-fopenmp", "-fPIC", "-shared", "-std=c11", str(src), "-o", str(tmp), "-lm"]
+    cmd = ["gcc", "-O3", "-fopenmp", "-fPIC", "-shared", "-std=c11", str(src), "-o", str(tmp), "-lm"]
     subprocess.run(cmd, check=True)
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
@@ -248,13 +248,42 @@ def block(kernel, x, x0, eps, alpha=0.0):
     return G.view(np.complex128).reshape(3, 3)
 
 
-# ---- geometry (geometry/spheres.py:7-13), used to build the workloads -----
+# ---- geometry (geometry/spheres.py), the checker of the device generators --
 def fibonacci_sphere(n, radius=1.0, center=(0.0, 0.0, 0.0)):
+    """geometry/spheres.py:7-13: golden-angle spiral, NumPy's operation order."""
     k = np.arange(n) + 0.5
     phi = np.arccos(1 - 2 * k / n)
     theta = np.pi * (1 + np.sqrt(5)) * k
     unit = np.c_[np.cos(theta) * np.sin(phi), np.sin(theta) * np.sin(phi), np.cos(phi)]
     return radius * unit + np.asarray(center, float)
+
+
+def cube_sphere(n, radius=1.0, center=(0.0, 0.0, 0.0)):
+    """geometry/spheres.py:33-52: n x n cell-centred points on each cube face (faces ordered
+    x = -1, x = +1, y = -1, y = +1, z = -1, z = +1; the two free coordinates in ascending axis
+    order, the first one slowest), normalized onto the sphere."""
+    s = np.linspace(-1.0 + 1.0 / n, 1.0 - 1.0 / n, n)
+    u = np.repeat(s, n)          # slow free coordinate
+    v = np.tile(s, n)            # fast free coordinate
+    blocks = []
+    for axis in range(3):
+        for side in (-1.0, 1.0):
+            P = np.empty((n * n, 3))
+            free = [a for a in range(3) if a != axis]
+            P[:, axis] = side
+            P[:, free[0]] = u
+            P[:, free[1]] = v
+            blocks.append(P)
+    P = np.concatenate(blocks)
+    return radius * (P / np.linalg.norm(P, axis=1)[:, None]) + np.asarray(center, float)
+
+
+def mean_nn_spacing(points):
+    """Mean distance to the nearest other point (SciPy k-d tree)."""
+    from scipy.spatial import cKDTree
+
+    d, _ = cKDTree(points).query(points, k=2)
+    return float(d[:, 1].mean())
 
 
 def max_threads():

@@ -2,7 +2,7 @@
 
 Run once, in a container where the reference source tree is available:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <path of the reference source tree>
 
 Two kinds of fixture are written:
 
@@ -168,7 +168,9 @@ def reference_cases(ref: Path):
 
 
 if __name__ == "__main__":
-    ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of the reference source tree>")
+    ref = Path(sys.argv[1])
     convert_legacy(ref)
     convert_legacy_grid(ref)
     reference_cases(ref)

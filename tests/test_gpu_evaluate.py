@@ -93,7 +93,6 @@ def test_ragged_sizes_fp64_and_mixed(kind, alpha, M, N):
 def test_self_interaction_and_near_pairs_mixed():
     """Targets == sources (the resistance matvec): every target has its own source at r = 0."""
     rng = np.random.default_rng(11)
-    X = fl.geometry.fibonacci_sphere(3000) if hasattr(fl, "geometry") else None
     from fluidlets_gb300.geometry import fibonacci_sphere
     X = fibonacci_sphere(3000) + [0, 0, 1.2]
     F = rng.normal(size=X.shape)
@@ -252,11 +251,12 @@ def test_device_spheres_match_reference_formulas():
 
     for n in (1, 3, 12, 40):
         d = G.cube_sphere_device(n, 0.7, (0.1, -2.0, 3.0)).cpu().numpy()
-        assert np.array_equal(d, G.cube_sphere(n, 0.7, (0.1, -2.0, 3.0)))  # sqrt and division: exact
+        assert np.array_equal(d, O.cube_sphere(n, 0.7, (0.1, -2.0, 3.0)))  # sqrt and division: exact
+        assert np.array_equal(G.cube_sphere(n, 0.7, (0.1, -2.0, 3.0)), d)
     for n in (1, 2, 1536, 65536):
         d = G.fibonacci_sphere_device(n, 2.0, (1.0, 0.0, -1.0)).cpu().numpy()
-        h = G.fibonacci_sphere(n, 2.0, (1.0, 0.0, -1.0))
+        h = O.fibonacci_sphere(n, 2.0, (1.0, 0.0, -1.0))
         assert np.abs(d - h).max() <= 8 * np.finfo(float).eps  # CUDA's acos/sin/cos vs the C library's
     rng = np.random.default_rng(5)
-    for P in (G.fibonacci_sphere(2000), rng.uniform(-1, 1, (3001, 3)), G.cube_sphere(12)):
-        assert abs(G.mean_nn_spacing_device(P) - G.mean_nn_spacing(P)) <= 1e-13 * G.mean_nn_spacing(P)
+    for P in (O.fibonacci_sphere(2000), rng.uniform(-1, 1, (3001, 3)), O.cube_sphere(12)):
+        assert abs(G.mean_nn_spacing(P) - O.mean_nn_spacing(P)) <= 1e-13 * O.mean_nn_spacing(P)

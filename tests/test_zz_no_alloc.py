@@ -39,7 +39,14 @@ def _evaluate(L, kind, alpha, X, Y, F, e, mu, noalloc):
     return out.cpu().numpy()
 
 
-@pytest.mark.parametrize("case", [(1, 0j, False, 1 + 0j, 2000, 3001), (2, 1.5 + 1.5j, True, 0.8 - 0.2j, 777, 1234)])
+# (kind, alpha, complex strengths, mu, M, N).  The last two cases hold enough targets that the
+# default number of source splits would overflow the fixed array (6 splits x 2.88 MB > 16 MiB), so
+# the call runs fewer, longer splits: real output (24 B per target) and complex (48 B).
+CASES = [(1, 0j, False, 1 + 0j, 2000, 3001), (2, 1.5 + 1.5j, True, 0.8 - 0.2j, 777, 1234),
+         (1, 0j, False, 1 + 0j, 120000, 4000), (0, 0j, True, 1 + 0j, 60000, 3000)]
+
+
+@pytest.mark.parametrize("case", CASES)
 def test_noalloc_matches_evaluate_on_two_calls_in_a_row(case):
     kind, alpha, fcomplex, mu, M, N = case
     L = _lib.load()
