@@ -12,7 +12,7 @@ import numpy as np
 
 from .build import lib_path
 
-FLG_OK, FLG_ERR_INVALID, FLG_ERR_CUDA, FLG_ERR_NOT_CONVERGED, FLG_ERR_SINGULAR, FLG_ERR_NOMEM = range(6)
+FLG_OK, FLG_ERR_INVALID, FLG_ERR_CUDA, FLG_ERR_NOT_CONVERGED, FLG_ERR_SINGULAR, FLG_ERR_NOMEM, FLG_ERR_TIMEOUT = range(7)
 KIND = {"stokeslet": 0, "wall": 1, "brinkman": 2}
 PREC = {"fp64": 0, "mixed": 1}
 F64, C128, F32, BF16 = 0, 1, 2, 3
@@ -94,6 +94,8 @@ SIGNATURES = {
     "flg_profile_enable": (c_int, [c_int]),
     "flg_profile_read": (c_int, [c_int, POINTER(c_double), POINTER(c_int64)]),
     "flg_launch_count": (c_int64, []),
+    "flg_wait_selftest_workspace": (c_size_t, []),
+    "flg_wait_selftest": (c_int, [c_int, c_double, _P, c_size_t, _P]),
 }
 SLOT = {"far_f32": 0, "near_f64": 1, "sum_f64": 2, "assemble": 3, "lu_update": 4, "lu_panel": 5, "gemv": 6, "lu_solve": 7, "lu_diag": 8}
 
@@ -145,4 +147,6 @@ def check(status: int, what: str = "") -> None:
         raise LinAlgError(text)
     if status == FLG_ERR_NOMEM:
         raise MemoryError(text)
+    if status == FLG_ERR_TIMEOUT:
+        raise RuntimeError(text)
     raise RuntimeError(f"CUDA error in {text}")

@@ -20,56 +20,20 @@
 // (FLG_LU_FP32).  With the tensor cores the next diagonal block runs ahead on
 // a side stream while the rest of each update finishes.
 //
-// Every spin-wait (the grid barrier, the diagonal block's warp handshake, the
-// solves' dataflow) is bounded by a clock64 limit and reports failure through
-// a device flag instead of hanging.
+// Every spin-wait (the grid barrier, the solves' dataflow, waits.cuh; the
+// diagonal block's warp handshake, an iteration count) is bounded and reports
+// failure through a device flag instead of hanging.
 #include <cooperative_groups.h>
 
 #include <algorithm>
 
 #include "flg_common.cuh"
+#include "waits.cuh"
 
 namespace flg {
 
 constexpr int kPanel = 64;                    // FP64 LU block width
 constexpr int kNB = FLG_LU_LOWP_BLOCK;        // low-precision LU block
-constexpr long long kSpinLimit = 4000000000LL;  // ~2 s of SM clock
-
-// ---- bounded grid barrier ------------------------------------------------------
-// One atomic per CTA: CTA 0 adds 2^31 - (nblocks - 1), every other CTA adds 1,
-// so once all have arrived the counter has grown by exactly 2^31 and its top
-// bit has flipped (no reset needed between barriers); waiters spin on an
-// acquire load until the bit flips, for at most kSpinLimit cycles.
-struct GridBar {
-    unsigned int count;
-    unsigned int pad;
-    int err;   // a wait ran out
-    int info;  // 1 + first zero pivot
-};
-
-__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
-    unsigned v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
-__device__ bool grid_sync(GridBar *b, unsigned nblocks) {
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        const unsigned inc = (blockIdx.x == 0) ? (0x80000000u - (nblocks - 1)) : 1u;
-        unsigned old;
-        asm volatile("atom.add.release.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(&b->count), "r"(inc) : "memory");
-        const long long t0 = clock64();
-        while (((old ^ ld_acquire_u32(&b->count)) & 0x80000000u) == 0) {
-            if (clock64() - t0 > kSpinLimit) {
-                atomicExch(&b->err, 1);
-                break;
-            }
-        }
-    }
-    __syncthreads();
-    return *(volatile int *)&b->err == 0;
-}
 
 // ---- FP64 panel ------------------------------------------------------------------
 struct PanelArgs {
@@ -144,7 +108,7 @@ __global__ void __launch_bounds__(256) panel_f64_kernel(PanelArgs a) {
         if (g >= r0 && g < r0 + nr)
             for (int q = threadIdx.x; q < kb; q += blockDim.x) a.diagbuf[buf * kb + q] = P[(g - r0) * kb + q];
         __threadfence();
-        if (!grid_sync(a.bar, nblk)) return;
+        if (!grid_sync(a.bar, nblk, kWaitLimitNs)) return;
         // global argmax over the CTAs' candidates: warp 0, lane-strided, then a shuffle
         // reduction (largest |value|, first row on ties)
         if (threadIdx.x < 32) {
@@ -877,11 +841,6 @@ struct ApplyArgs {
     int *err;        // a wait ran out
 };
 
-__device__ __forceinline__ unsigned ld_relaxed_u32(const float *p) {
-    unsigned v;
-    asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
 __device__ __forceinline__ void st_relaxed_f32(float *p, float v) {
     unsigned u = __float_as_uint(v);
     if (u == kUnset) u = 0x7fffffffu;  // keep the sentinel unique
@@ -905,17 +864,8 @@ __device__ bool fetch_block(float *vec, const float *src, int64_t j, int64_t n, 
         const int64_t e = j * kNB + t;
         float v = 0.0f;
         if (e < n) {
-            unsigned u = first;
-            if (u == kUnset) {
-                const long long t0 = clock64();
-                while ((u = ld_relaxed_u32(src + e)) == kUnset) {
-                    if (*(volatile int *)err || clock64() - t0 > kSpinLimit) {
-                        atomicExch(err, 1);
-                        *abort_s = 1;
-                        break;
-                    }
-                }
-            }
+            unsigned u;
+            if (!wait_published(src + e, kUnset, first, &u, kWaitLimitNs, err)) *abort_s = 1;
             v = __uint_as_float(u);
         }
         vec[qpos(t)] = v;
@@ -1065,13 +1015,9 @@ __global__ void __launch_bounds__(kApplyThreads) lowp_apply_kernel(ApplyArgs a) 
                 for (int m = 1; m < T; m++) {
                     if (count(m) == 0) continue;
                     unsigned uv;
-                    const long long t0 = clock64();
-                    while ((uv = ld_relaxed_u32(pslot + m * kNB + r)) == kUnset) {
-                        if (*(volatile int *)a.err || clock64() - t0 > kSpinLimit) {
-                            atomicExch(a.err, 1);
-                            abort_s = 1;
-                            break;
-                        }
+                    if (!wait_published(pslot + m * kNB + r, kUnset, kUnset, &uv, kWaitLimitNs, a.err)) {
+                        abort_s = 1;
+                        break;
                     }
                     tot += __uint_as_float(uv);
                 }
@@ -1230,8 +1176,8 @@ extern "C" int flg_lu_factor_f64(int64_t n, double *A, int64_t ld, int32_t *ipiv
     FLG_CUDA(cudaMemcpyAsync(&hb, bar, sizeof(GridBar), cudaMemcpyDeviceToHost, st));
     FLG_CUDA(cudaStreamSynchronize(st));
     if (hb.err) {
-        set_error("LU panel barrier timed out");
-        return FLG_ERR_CUDA;
+        set_error("a bounded device wait timed out (LU panel grid barrier)");
+        return FLG_ERR_TIMEOUT;
     }
     *info = hb.info;
     if (hb.info) {
@@ -1557,7 +1503,7 @@ extern "C" int flg_lu_factor_lowp(int64_t n, float *A, int64_t ld, int mode, flo
     FLG_CUDA(cudaStreamSynchronize(st));
     if (hflags[1]) {
         set_error("a bounded device wait timed out (tensor-core update or diagonal block)");
-        return FLG_ERR_CUDA;
+        return FLG_ERR_TIMEOUT;
     }
     *info = hflags[0];
     if (hflags[0]) {

@@ -28,13 +28,13 @@
 #include <mutex>
 
 #include "flg_common.cuh"
+#include "waits.cuh"
 
 namespace flg {
 
 constexpr int TC_BM = 128, TC_THREADS = 192, TC_EPI_WARPS = 4;
 constexpr int TC_A_BYTES = TC_BM * 128;   // A tile of a K-block: 128 rows x 128 B
 constexpr int TC_STG_BYTES = 32 * 128;    // one 32 x 32 FP32 staging box
-constexpr long long TC_WAIT_LIMIT = 2000000000LL;  // ~1 s of SM clock per wait
 
 // tile width BN: ring depth, B tile bytes (BN rows x 128 B), TMEM columns (two accumulators)
 template <int BN>
@@ -47,48 +47,12 @@ struct TcTile {
     static_assert(SMEM <= 232448 - 256, "shared memory per CTA");
 };
 
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
 __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
                  : "memory");
 }
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// bounded wait: false if the limit ran out (the error flag is raised) or another role raised it
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err) {
-    const long long t0 = clock64();
-    while (!mbar_try_wait(bar, parity)) {
-        if (*(volatile int *)err) return false;
-        if (clock64() - t0 > TC_WAIT_LIMIT) {
-            atomicExch(err, 1);
-            return false;
-        }
-    }
-    return true;
-}
-// bounded wait that ignores the error flag (draining own operations on the way out)
-__device__ __forceinline__ void mbar_drain(uint64_t *bar, uint32_t parity, int *err) {
-    const long long t0 = clock64();
-    while (!mbar_try_wait(bar, parity)) {
-        if (clock64() - t0 > TC_WAIT_LIMIT) {
-            atomicExch(err, 1);
-            return;
-        }
-    }
 }
 
 __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar, int x, int y) {
@@ -178,7 +142,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_update_kernel(const __grid_c
                 for (int kb = 0; kb < nkb; kb++, g++) {
                     const int s = g % TC_STAGES;
                     const uint32_t use = g / TC_STAGES;
-                    if (use > 0 && !mbar_wait(&empty[s], (use & 1) ^ 1, err)) {
+                    if (use > 0 && !mbar_wait(&empty[s], (use & 1) ^ 1, err, kWaitLimitNs)) {
                         ok = false;
                         break;
                     }
@@ -189,7 +153,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_update_kernel(const __grid_c
             }
             // the last (up to S) loads issued must have landed before the CTA exits
             for (uint32_t q = (g > TC_STAGES ? g - TC_STAGES : 0); q < g; q++)
-                mbar_drain(&full[q % TC_STAGES], (q / TC_STAGES) & 1, err);
+                mbar_drain(&full[q % TC_STAGES], (q / TC_STAGES) & 1, err, kWaitLimitNs);
         }
     } else if (warp == 1) {
         if (lane == 0) {  // MMA issuer
@@ -197,7 +161,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_update_kernel(const __grid_c
             bool ok = true;
             for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, i++) {
                 const uint32_t buf = i & 1, ause = i >> 1;
-                if (ause > 0 && !mbar_wait(&acce[buf], (ause & 1) ^ 1, err)) {
+                if (ause > 0 && !mbar_wait(&acce[buf], (ause & 1) ^ 1, err, kWaitLimitNs)) {
                     ok = false;
                     break;
                 }
@@ -206,7 +170,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_update_kernel(const __grid_c
                 for (int kb = 0; kb < nkb; kb++, g++) {
                     const int s = g % TC_STAGES;
                     const uint32_t use = g / TC_STAGES;
-                    if (!mbar_wait(&full[s], use & 1, err)) {
+                    if (!mbar_wait(&full[s], use & 1, err, kWaitLimitNs)) {
                         ok = false;
                         break;
                     }
@@ -243,7 +207,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_update_kernel(const __grid_c
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                              smem_u32(&mma_done))
                          : "memory");
-            mbar_drain(&mma_done, 0, err);
+            mbar_drain(&mma_done, 0, err, kWaitLimitNs);
         }
     } else {
         // epilogue: warp w reads TMEM lanes 32 (w % 4) .. +32, i.e. tile rows 32 (w % 4) + lane
@@ -253,7 +217,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_update_kernel(const __grid_c
         for (int t = blockIdx.x; t < ntiles; t += gridDim.x, i++) {
             const uint32_t buf = i & 1, ause = i >> 1;
             // warp-uniform: tcgen05.ld.sync.aligned must be executed by the whole warp
-            if (!__all_sync(0xffffffffu, mbar_wait(&accf[buf], ause & 1, err))) break;
+            if (!__all_sync(0xffffffffu, mbar_wait(&accf[buf], ause & 1, err, kWaitLimitNs))) break;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const int m0 = (t / ntx) * TC_BM, n0 = (t % ntx) * TC_BN;
 #pragma unroll 1
@@ -464,7 +428,10 @@ int tc_update(float *C, int64_t ldc, const float *Lp, int64_t ldl, const float *
     int herr = 0;
     FLG_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
     FLG_CUDA(cudaStreamSynchronize(st));
-    FLG_REQUIRE(herr == 0, "tensor-core update: an mbarrier wait timed out");
+    if (herr != 0) {
+        set_error("a bounded device wait timed out (tensor-core update, mbarrier)");
+        return FLG_ERR_TIMEOUT;
+    }
     return FLG_OK;
 }
 

@@ -47,6 +47,7 @@ extern "C" {
 #define FLG_ERR_NOT_CONVERGED 3  /* iterative solver hit maxiter: RuntimeError */
 #define FLG_ERR_SINGULAR 4       /* zero / non-finite pivot: LinAlgError     */
 #define FLG_ERR_NOMEM 5          /* request exceeds the caller's budget      */
+#define FLG_ERR_TIMEOUT 6        /* a bounded device wait ran out: RuntimeError */
 
 /* ---- kernel kinds, precisions, element types ---------------------------- */
 #define FLG_STOKESLET 0
@@ -388,6 +389,21 @@ int flg_measure_peaks(double *fp32_tflops, double *fp64_tflops, void *stream);
 int flg_profile_enable(int enable);
 int flg_profile_read(int slot, double *total_ms, int64_t *launches);
 int64_t flg_launch_count(void);
+
+/* ---- failure detection ----------------------------------------------------
+ * Every spin-wait in the library's kernels is bounded (2 s in production) and
+ * reports a wait that ran out as FLG_ERR_TIMEOUT instead of hanging the GPU.
+ * No counterpart in the reference (its solvers run on the host; their only
+ * failure report is RuntimeError on GMRES non-convergence, core/solve.py:77-78).
+ * flg_wait_selftest drives one kind of wait to expiry on a condition nothing
+ * satisfies, with a limit of `limit_ms`: which = 0 the grid barrier of the FP64
+ * LU panel (one arrival never comes), 1 the low-precision solve's poll of a
+ * published value (nothing publishes it), 2 the tensor-core update's mbarrier
+ * wait (no arrival completes the phase).  It returns FLG_ERR_TIMEOUT, as the
+ * production entry points do for such a wait, after about limit_ms, with the
+ * context still usable.  Synchronizes. */
+size_t flg_wait_selftest_workspace(void);
+int flg_wait_selftest(int which, double limit_ms, void *work, size_t work_bytes, void *stream);
 
 #ifdef __cplusplus
 }
