@@ -4,9 +4,10 @@
 // np.linalg.solve, swimming.py:101): right-looking blocked LU with partial
 // pivoting, row-major storage, block width kPanel = 64.
 //   panel_f64_kernel  cooperative launch over up to one CTA per SM; each CTA
-//                     keeps a slab of panel rows in shared memory; one grid
-//                     barrier per column (pivot search is a grid-wide argmax,
-//                     first index on ties as LAPACK's idamax).
+//                     keeps a slab of panel rows in shared memory; one round of
+//                     published candidates per column (pivot search is a
+//                     grid-wide argmax, first index on ties as LAPACK's idamax),
+//                     with the next column's look-ahead overlapping it.
 //   laswp_kernel      the panel's row swaps on the other columns.
 //   trsm_f64_kernel   U12 = L11^-1 A12.
 //   dgemm_update      A22 -= L21 U12 (FP64 CUDA cores).
@@ -36,146 +37,347 @@ constexpr int kPanel = 64;                    // FP64 LU block width
 constexpr int kNB = FLG_LU_LOWP_BLOCK;        // low-precision LU block
 
 // ---- FP64 panel ------------------------------------------------------------------
+// Partial-pivoting LU of the m x kb panel A[k0:n, k0:k0+kb] (LAPACK getf2's pivot
+// choice: the largest |a| in the column, the first row on ties), one cooperative
+// launch of up to one CTA per SM, each CTA holding `rpc` consecutive panel rows in
+// shared memory (CTA c owns rows k0 + c rpc ...).  GB300 runs FP64 at ~2 FMA per
+// SM and clock, so the panel's arithmetic must be spread over every SM; what
+// limits it is the exchange between CTAs per column, which is kept to one
+// round of published values:
+//   * every CTA publishes, for column j, its candidate (the largest |a| among its
+//     rows >= g, encoded with the column's parity bit in one 64-bit word released
+//     after the candidate's full row and, by the owner of row g, row g itself);
+//   * every CTA polls the words (acquire), picks the winner (largest value; on ties
+//     the smaller CTA index, which owns the smaller rows), and reads the winning
+//     row; the winner writes ipiv[g] and row g's old content into the pivot row,
+//     the owner of g writes the pivot row into row g;
+//   * look-ahead inside the panel: after scaling column j each CTA updates column
+//     j + 1 first, finds its next candidate, completes the update of that row and
+//     of row g + 1 and publishes them, and only then updates its other rows, so
+//     the bulk of the rank-1 update overlaps the exchange.
+// Every element receives the same fma, in the same column order, as in the
+// textbook right-looking loop, so the factors do not depend on the CTA count.
+// A word holds (bits(|a|) + 1) | parity << 63 (0 for "no rows >= g" or only
+// NaN); the
+// parity ((j >> 1) & 1) tells column j from column j - 2, which used the same
+// one of the two buffers; the host presets both buffers to parity 1 before
+// every panel.
 struct PanelArgs {
     double *A;
     int64_t ld, n, k0;
     int kb, rpc;
     int32_t *ipiv;
-    GridBar *bar;
-    double *slot_val;  // [2][nblk]
-    long long *slot_row;
-    double *rowbuf;   // [2][nblk][kb]
-    double *diagbuf;  // [2][kb]
+    GridBar *bar;                 // err: a wait ran out; info: 1 + first zero pivot
+    unsigned long long *word;     // [2][nblk]
+    double *rowbuf;               // [2][nblk][kRowBufLd]: each CTA's candidate row and 1 / its pivot
+    double *diagbuf;              // [2][kb]: row g
 };
+
+__device__ __forceinline__ void st_release_u64(unsigned long long *p, unsigned long long v) {
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+constexpr int kRowBufLd = kPanel + 8;  // a published row: kb values, then the reciprocal of its pivot
 
 __global__ void __launch_bounds__(256) panel_f64_kernel(PanelArgs a) {
     extern __shared__ double P[];  // [rpc][kb]
-    __shared__ double s_piv[kPanel];
-    __shared__ double red_v[8];
-    __shared__ long long red_r[8];
-    __shared__ long long s_p;
-    __shared__ int s_wc, s_lb;
-    const int nblk = gridDim.x, c = blockIdx.x, kb = a.kb;
-    const int64_t r0 = a.k0 + (int64_t)c * a.rpc;
-    const int nr = (int)max((int64_t)0, min((int64_t)a.rpc, a.n - r0));
-    for (int e = threadIdx.x; e < nr * kb; e += blockDim.x) {
+    __shared__ double s_piv[kRowBufLd], s_old[kPanel];
+    __shared__ unsigned long long red_w[8];
+    __shared__ int red_c[8];
+    __shared__ double s_rcp;  // 1 / this CTA's candidate value, published with its row
+    __shared__ int s_win;     // winning CTA
+    __shared__ int s_abort;
+    const int nblk = gridDim.x, c = blockIdx.x, kb = a.kb, rpc = a.rpc;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const int64_t r0 = a.k0 + (int64_t)c * rpc;
+    const int nr = (int)max((int64_t)0, min((int64_t)rpc, a.n - r0));
+    for (int e = t; e < nr * kb; e += blockDim.x) {
         const int lr = e / kb, j = e - lr * kb;
         P[e] = a.A[(r0 + lr) * a.ld + a.k0 + j];
     }
+    if (t == 0) s_abort = 0;
     __syncthreads();
-    for (int j = 0; j < kb; j++) {
-        const int64_t g = a.k0 + j;
-        const int buf = j & 1;
-        // local argmax of |P[., j]| over rows >= g (first index on ties)
-        double best = -1.0;
-        long long brow = LLONG_MAX;
-        for (int lr = threadIdx.x; lr < nr; lr += blockDim.x) {
-            const int64_t gr = r0 + lr;
-            if (gr < g) continue;
-            const double v = fabs(P[lr * kb + j]);
-            if (v > best) {
-                best = v;
-                brow = gr;
+
+    // Local argmax of |P[., col]| over local rows >= lo (first row on ties), compared as
+    // integers (the bits of a non-negative double order like its value; NaN never wins, as
+    // in an FP comparison): the key bits(|a|) + 1 (0 if there is no candidate) and the local
+    // row (-1), the same in every thread.  With `upd`, each row's column col first receives
+    // its update from column col - 1 (multiplier P[., col - 1], pivot-row entry u).
+    auto argmax = [&](int col, int lo, bool upd, double u, int &row) -> unsigned long long {
+        unsigned long long best = 0;
+        int brow = INT_MAX;
+        for (int lr = lo + t; lr < nr; lr += blockDim.x) {
+            double x = P[lr * kb + col];
+            if (upd) {
+                x = fma(-P[lr * kb + col - 1], u, x);
+                P[lr * kb + col] = x;
+            }
+            const unsigned long long b = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+            const unsigned long long k = b > 0x7ff0000000000000ull ? 0ull : b + 1ull;
+            if (k > best) {
+                best = k;
+                brow = lr;
             }
         }
         for (int o = 16; o > 0; o >>= 1) {
-            const double ov = __shfl_xor_sync(0xffffffffu, best, o);
-            const long long orow = __shfl_xor_sync(0xffffffffu, brow, o);
+            const unsigned long long ov = __shfl_xor_sync(0xffffffffu, best, o);
+            const int orow = __shfl_xor_sync(0xffffffffu, brow, o);
             if (ov > best || (ov == best && orow < brow)) {
                 best = ov;
                 brow = orow;
             }
         }
-        if ((threadIdx.x & 31) == 0) {
-            red_v[threadIdx.x >> 5] = best;
-            red_r[threadIdx.x >> 5] = brow;
+        if (lane == 0) {
+            red_w[warp] = best;
+            red_c[warp] = brow;
         }
         __syncthreads();
-        if (threadIdx.x == 0) {
-            for (int w = 1; w < (int)(blockDim.x >> 5); w++)
-                if (red_v[w] > red_v[0] || (red_v[w] == red_v[0] && red_r[w] < red_r[0])) {
-                    red_v[0] = red_v[w];
-                    red_r[0] = red_r[w];
-                }
-            a.slot_val[buf * nblk + c] = red_v[0];
-            a.slot_row[buf * nblk + c] = red_r[0];
-            s_lb = red_r[0] == LLONG_MAX ? -1 : (int)(red_r[0] - r0);
-        }
+        unsigned long long bk = red_w[0];
+        int br = red_c[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++)
+            if (red_w[w] > bk || (red_w[w] == bk && red_c[w] < br)) {
+                bk = red_w[w];
+                br = red_c[w];
+            }
         __syncthreads();
-        if (s_lb >= 0)
-            for (int q = threadIdx.x; q < kb; q += blockDim.x)
-                a.rowbuf[((int64_t)buf * nblk + c) * kb + q] = P[s_lb * kb + q];
-        if (g >= r0 && g < r0 + nr)
-            for (int q = threadIdx.x; q < kb; q += blockDim.x) a.diagbuf[buf * kb + q] = P[(g - r0) * kb + q];
-        __threadfence();
-        if (!grid_sync(a.bar, nblk, kWaitLimitNs)) return;
-        // global argmax over the CTAs' candidates: warp 0, lane-strided, then a shuffle
-        // reduction (largest |value|, first row on ties)
-        if (threadIdx.x < 32) {
-            double bv = -1.0;
-            long long br = LLONG_MAX;
-            int wc = -1;
-            for (int q = threadIdx.x; q < nblk; q += 32) {
-                const double v = __ldcg(a.slot_val + buf * nblk + q);
-                const long long r = __ldcg(a.slot_row + buf * nblk + q);
-                if (r == LLONG_MAX) continue;
-                if (v > bv || (v == bv && r < br)) {
-                    bv = v;
-                    br = r;
-                    wc = q;
+        row = bk == 0 ? -1 : br;
+        return bk;
+    };
+    // the reciprocal of the candidate's value, computed while other threads work (one thread)
+    auto candidate_rcp = [&](int col, int cand) {
+        if (t == blockDim.x - 1) {
+            const double v = cand >= 0 ? P[cand * kb + col] : 0.0;
+            s_rcp = (v != 0.0 && isfinite(v)) ? 1.0 / v : 0.0;
+        }
+    };
+    // publish column col's candidate (key k, local row cand, its reciprocal s_rcp) and, from
+    // the owner, row g
+    auto publish = [&](int col, unsigned long long k, int cand) {
+        const int buf = col & 1;
+        const unsigned long long par = (unsigned long long)((col >> 1) & 1) << 63;
+        const int64_t g = a.k0 + col;
+        double *rb = a.rowbuf + ((int64_t)buf * nblk + c) * kRowBufLd;
+        if (cand >= 0 && t < kb) rb[t] = P[cand * kb + t];
+        if (cand >= 0 && t == kb) rb[kPanel] = s_rcp;
+        if (g >= r0 && g < r0 + nr && t < kb) a.diagbuf[buf * kb + t] = P[(g - r0) * kb + t];
+        __syncthreads();  // the CTA's writes precede thread 0's release (cumulative through bar.sync)
+        if (t == 0) st_release_u64(a.word + (int64_t)buf * nblk + c, par | k);
+    };
+
+    const int lo0 = (int)max((int64_t)0, min((int64_t)nr, a.k0 - r0));
+    int mycand = -1;
+    {
+        const unsigned long long k0key = argmax(0, lo0, false, 0.0, mycand);
+        candidate_rcp(0, mycand);
+        __syncthreads();
+        publish(0, k0key, mycand);
+    }
+    for (int j = 0; j < kb; j++) {
+        const int64_t g = a.k0 + j;
+        const int buf = j & 1;
+        const unsigned long long par = (unsigned long long)((j >> 1) & 1);
+        // (1) the winner of column j: every thread polls at most one CTA's word per pass
+        //     (relaxed loads issued together, one acquire fence once all have arrived)
+        {
+            unsigned long long bv = 0;
+            int bc = INT_MAX;
+            for (int q0 = 0; q0 < nblk; q0 += blockDim.x) {
+                const int q = q0 + t;
+                if (q < nblk) {
+                    const unsigned long long *w = a.word + (int64_t)buf * nblk + q;
+                    unsigned long long u = ld_relaxed_u64(w);
+                    if ((u >> 63) != par) {
+                        const unsigned long long t0 = global_ns();
+                        while (((u = ld_relaxed_u64(w)) >> 63) != par) {
+                            if (*(volatile int *)&a.bar->err || global_ns() - t0 > kWaitLimitNs) {
+                                atomicExch(&a.bar->err, 1);
+                                s_abort = 1;
+                                break;
+                            }
+                        }
+                    }
+                    const unsigned long long val = u & 0x7fffffffffffffffull;
+                    if (val > bv) {
+                        bv = val;
+                        bc = q;
+                    }
                 }
             }
+            asm volatile("fence.acq_rel.gpu;" ::: "memory");
             for (int o = 16; o > 0; o >>= 1) {
-                const double ov = __shfl_xor_sync(0xffffffffu, bv, o);
-                const long long orow = __shfl_xor_sync(0xffffffffu, br, o);
-                const int owc = __shfl_xor_sync(0xffffffffu, wc, o);
-                if (owc >= 0 && (wc < 0 || ov > bv || (ov == bv && orow < br))) {
+                const unsigned long long ov = __shfl_xor_sync(0xffffffffu, bv, o);
+                const int oc = __shfl_xor_sync(0xffffffffu, bc, o);
+                if (ov > bv || (ov == bv && oc < bc)) {
                     bv = ov;
-                    br = orow;
-                    wc = owc;
+                    bc = oc;
                 }
             }
-            if (threadIdx.x == 0) {
-                if (wc < 0) br = g;  // no finite candidate: keep row g
-                s_p = br;
-                s_wc = wc;
-                if (c == 0) a.ipiv[g] = (int32_t)br;
+            if (lane == 0) {
+                red_w[warp] = bv;
+                red_c[warp] = bc;
             }
-        }
-        __syncthreads();
-        const long long p = s_p;
-        for (int q = threadIdx.x; q < kb; q += blockDim.x)
-            s_piv[q] = s_wc >= 0 ? ((volatile double *)a.rowbuf)[((int64_t)buf * nblk + s_wc) * kb + q]
-                                 : ((volatile double *)a.diagbuf)[buf * kb + q];
-        __syncthreads();
-        if (p != g) {
-            if (p >= r0 && p < r0 + nr)
-                for (int q = threadIdx.x; q < kb; q += blockDim.x)
-                    P[(p - r0) * kb + q] = ((volatile double *)a.diagbuf)[buf * kb + q];
-            if (g >= r0 && g < r0 + nr)
-                for (int q = threadIdx.x; q < kb; q += blockDim.x) P[(g - r0) * kb + q] = s_piv[q];
-        }
-        __syncthreads();
-        const double piv = s_piv[j];
-        if (piv == 0.0 || !isfinite(piv)) {
-            if (threadIdx.x == 0) atomicCAS(&a.bar->info, 0, (int)(g + 1));
-        } else {
-            const double rp = 1.0 / piv;
-            for (int lr = threadIdx.x; lr < nr; lr += blockDim.x)
-                if (r0 + lr > g) P[lr * kb + j] *= rp;
             __syncthreads();
-            const int w = kb - j - 1;
-            for (int e = threadIdx.x; e < nr * w; e += blockDim.x) {
-                const int lr = e / w, q = j + 1 + (e - lr * w);
-                if (r0 + lr > g) P[lr * kb + q] = fma(-P[lr * kb + j], s_piv[q], P[lr * kb + q]);
+            if (t == 0) {
+                for (int w = 1; w < (int)(blockDim.x >> 5); w++)
+                    if (red_w[w] > red_w[0] || (red_w[w] == red_w[0] && red_c[w] < red_c[0])) {
+                        red_w[0] = red_w[w];
+                        red_c[0] = red_c[w];
+                    }
+                s_win = red_c[0];
             }
         }
+        __syncthreads();
+        if (s_abort) return;
+        // no candidate anywhere (every |a| of the column NaN): row g stays, as the pivot
+        const bool none = s_win == INT_MAX;
+        const int own_g = (int)((g - a.k0) / rpc);
+        const int win = none ? own_g : s_win;
+        // (2) the pivot row with its reciprocal, and for the winner the old row g
+        if (t <= kb) {
+            if (none) s_piv[t] = t < kb ? __ldcg(a.diagbuf + buf * kb + t) : 0.0;
+            else s_piv[t == kb ? kPanel : t] = __ldcg(a.rowbuf + ((int64_t)buf * nblk + win) * kRowBufLd +
+                                                      (t == kb ? kPanel : t));
+            if (win == c && t < kb) s_old[t] = __ldcg(a.diagbuf + buf * kb + t);
+        }
+        __syncthreads();
+        // (3) the swap
+        const int64_t p = (win == c) ? (none ? g : r0 + mycand) : -1;
+        if (win == c && t == 0) a.ipiv[g] = (int32_t)p;
+        if (t < kb) {
+            if (win == c && p != g) P[(p - r0) * kb + t] = s_old[t];
+            if (g >= r0 && g < r0 + nr) P[(g - r0) * kb + t] = s_piv[t];
+        }
+        const int lr1 = (int)max((int64_t)0, min((int64_t)nr, g + 1 - r0));  // first local row > g
+        const double piv = s_piv[j];
+        const bool ok = piv != 0.0 && isfinite(piv);
+        if (!ok && t == 0) atomicCAS(&a.bar->info, 0, (int)(g + 1));
+        // (3b) scale column j below g (rows > g are not touched by the swap's writes to row g;
+        //      the winner's write to row p is by the same threads, t < kb, before their scaling)
+        __syncthreads();
+        if (ok) {
+            const double rp = s_piv[kPanel];  // = 1 / piv, computed by the publisher
+            for (int lr = lr1 + t; lr < nr; lr += blockDim.x) P[lr * kb + j] *= rp;
+        }
+        __syncthreads();
+        if (j + 1 == kb) break;
+        // (4) look-ahead: column j + 1 (updated on the way), the next candidate, its row and
+        //     row g + 1, published
+        int cand;
+        const unsigned long long v = argmax(j + 1, lr1, ok, s_piv[j + 1], cand);
+        candidate_rcp(j + 1, cand);
+        const int lg1 = (g + 1 >= r0 && g + 1 < r0 + nr) ? (int)(g + 1 - r0) : -1;
+        if (ok) {
+            const int q = j + 2 + (t & 63);
+            const int which = t >> 6;  // 0: the candidate row, 1: row g + 1
+            const int lr = which == 0 ? cand : (lg1 != cand ? lg1 : -1);
+            if (which < 2 && lr >= 0 && q < kb) P[lr * kb + q] = fma(-P[lr * kb + j], s_piv[q], P[lr * kb + q]);
+        }
+        __syncthreads();
+        publish(j + 1, v, cand);
+        // (5) the rest of the rank-1 update (columns > j + 1), beside the exchange
+        if (ok) {
+            const int q = t % kPanel, rg = t / kPanel;
+            constexpr int kRowStep = 256 / kPanel;
+            if (q > j + 1 && q < kb) {
+                const double u = s_piv[q];
+                for (int lr = lr1 + rg; lr < nr; lr += kRowStep)
+                    if (lr != cand && lr != lg1) P[lr * kb + q] = fma(-P[lr * kb + j], u, P[lr * kb + q]);
+            }
+        }
+        mycand = cand;
         __syncthreads();
     }
-    for (int e = threadIdx.x; e < nr * kb; e += blockDim.x) {
+    for (int e = t; e < nr * kb; e += blockDim.x) {
         const int lr = e / kb, j = e - lr * kb;
         a.A[(r0 + lr) * a.ld + a.k0 + j] = P[e];
     }
+}
+
+// The panel's kb row interchanges (LAPACK laswp: for q = 0..kb-1 swap rows k0 + q and
+// ipiv[k0 + q]) applied to the columns [c0, c1), and with TRSM also U12 = L11^-1 A12 (the
+// unit lower L11 = A[k0:k0+kb, k0:k0+kb]) for the columns right of the panel.  Instead of
+// kb dependent read-modify-write swaps per column, each CTA first works out in shared
+// memory where every touched row's final content comes from (at most 2 kb rows: the panel
+// rows and the pivot rows below them); then each thread gathers its column's touched rows
+// with independent loads, solves, and writes them back.
+constexpr int kSwapThreads = 128;
+template <bool TRSM>
+__global__ void __launch_bounds__(kSwapThreads) swap_trsm_kernel(double *A, int64_t ld, const int32_t *ipiv,
+                                                                  int64_t k0, int kb, int64_t c0, int64_t c1) {
+    __shared__ double L[TRSM ? kPanel : 1][kPanel + 1];
+    __shared__ int64_t srow[2 * kPanel];   // slot -> row whose old content the slot's row receives
+    __shared__ int64_t xrow[kPanel];       // extra slot kb + e -> its row (a pivot row below the panel)
+    __shared__ int src[2 * kPanel];        // slot -> source slot, built by warp 0
+    __shared__ int s_ne;
+    extern __shared__ double E[];          // [extras][kSwapThreads]: old contents for the extra rows
+    const int t = threadIdx.x;
+    if (TRSM)
+        for (int e = t; e < kb * kb; e += blockDim.x) {
+            const int r = e / kb, q = e - r * kb;
+            L[r][q] = A[(k0 + r) * ld + k0 + q];
+        }
+    if (t < 32) {
+        // slots 0..kb-1: rows k0..k0+kb-1; kb.. : pivot rows below the panel, in order of appearance
+        for (int q = t; q < 2 * kPanel; q += 32) src[q] = q;
+        int ne = 0;
+        __syncwarp();
+        for (int q = 0; q < kb; q++) {
+            const int64_t p = ipiv[k0 + q];
+            int b;
+            if (p < k0 + kb) {
+                b = (int)(p - k0);
+            } else {
+                const bool hit0 = t < ne && xrow[t] == p, hit1 = t + 32 < ne && xrow[t + 32] == p;
+                const unsigned m0 = __ballot_sync(0xffffffffu, hit0), m1 = __ballot_sync(0xffffffffu, hit1);
+                if (m0) b = kb + __ffs(m0) - 1;
+                else if (m1) b = kb + 32 + __ffs(m1) - 1;
+                else {
+                    if (t == 0) xrow[ne] = p;
+                    b = kb + ne;
+                    ne++;
+                }
+            }
+            if (t == 0 && b != q) {
+                const int tmp = src[q];
+                src[q] = src[b];
+                src[b] = tmp;
+            }
+            __syncwarp();
+        }
+        if (t == 0) s_ne = ne;
+        __syncwarp();
+        for (int sl = t; sl < kb + ne; sl += 32) {
+            const int so = src[sl];
+            srow[sl] = so < kb ? k0 + so : xrow[so - kb];
+        }
+    }
+    __syncthreads();
+    const int ne = s_ne;
+    const int64_t c = c0 + (int64_t)blockIdx.x * blockDim.x + t;
+    if (c >= c1) return;
+    double x[kPanel];
+#pragma unroll
+    for (int q = 0; q < kPanel; q++)
+        if (q < kb) x[q] = A[srow[q] * ld + c];
+    for (int e = 0; e < ne; e++) E[e * kSwapThreads + t] = A[srow[kb + e] * ld + c];
+    if (TRSM) {
+#pragma unroll
+        for (int r = 0; r < kPanel; r++) {
+            double v = x[r];
+#pragma unroll
+            for (int q = 0; q < r; q++) v = fma(-L[r][q], x[q], v);
+            x[r] = v;
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < kPanel; q++)
+        if (q < kb) A[(k0 + q) * ld + c] = x[q];
+    for (int e = 0; e < ne; e++) A[xrow[e] * ld + c] = E[e * kSwapThreads + t];
 }
 
 // row swaps of rows k0 .. k0+kb-1 on columns [c0, c1)
@@ -1109,12 +1311,39 @@ extern "C" size_t flg_lu_factor_f64_workspace(int64_t n) {
     CountingArena c;
     const int nblk = sm_count();
     c.take<GridBar>(1);
-    c.take<double>(2 * nblk);
-    c.take<long long>(2 * nblk);
-    c.take<double>((size_t)2 * nblk * kPanel);
+    c.take<unsigned long long>(2 * nblk);
+    c.take<double>((size_t)2 * nblk * kRowBufLd);
     c.take<double>(2 * kPanel);
     (void)n;
     return c.bytes();
+}
+
+// Per host thread and device: the streams of the FP64 LU's look-ahead -- the next panel
+// (highest priority) beside the trailing update, and the interchanges of the columns left of
+// each panel (lowest priority), which nothing reads until the factorization ends.
+struct F64Streams {
+    int dev = -1;
+    cudaStream_t panel = nullptr, left = nullptr;
+    cudaEvent_t next_ready = nullptr, panel_done = nullptr, factored = nullptr, left_done = nullptr;
+};
+constexpr int kF64StreamDevices = 64;
+static int f64_streams(F64Streams **out) {
+    thread_local F64Streams per_dev[kF64StreamDevices];
+    int dev = 0;
+    FLG_CUDA(cudaGetDevice(&dev));
+    FLG_REQUIRE(dev >= 0 && dev < kF64StreamDevices, "device ordinal %d out of range", dev);
+    F64Streams &fs = per_dev[dev];
+    if (fs.dev != dev) {
+        int lo = 0, hi = 0;
+        FLG_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+        FLG_CUDA(cudaStreamCreateWithPriority(&fs.panel, cudaStreamNonBlocking, hi));
+        FLG_CUDA(cudaStreamCreateWithPriority(&fs.left, cudaStreamNonBlocking, lo));
+        for (cudaEvent_t *e : {&fs.next_ready, &fs.panel_done, &fs.factored, &fs.left_done})
+            FLG_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+        fs.dev = dev;
+    }
+    *out = &fs;
+    return FLG_OK;
 }
 
 extern "C" int flg_lu_factor_f64(int64_t n, double *A, int64_t ld, int32_t *ipiv, int *info, void *work,
@@ -1130,15 +1359,25 @@ extern "C" int flg_lu_factor_f64(int64_t n, double *A, int64_t ld, int32_t *ipiv
     Arena ar(work, work_bytes);
     const int maxblk = sm_count();
     GridBar *bar = ar.take<GridBar>(1);
-    double *slot_val = ar.take<double>(2 * maxblk);
-    long long *slot_row = ar.take<long long>(2 * maxblk);
-    double *rowbuf = ar.take<double>((size_t)2 * maxblk * kPanel);
+    unsigned long long *word = ar.take<unsigned long long>(2 * maxblk);
+    double *rowbuf = ar.take<double>((size_t)2 * maxblk * kRowBufLd);
     double *diagbuf = ar.take<double>(2 * kPanel);
     FLG_REQUIRE(diagbuf != nullptr, "workspace too small for LU (%zu bytes)", work_bytes);
+    F64Streams *fs = nullptr;
+    FLG_TRY(f64_streams(&fs));
+    static bool attr_set = false;
+    if (!attr_set) {
+        FLG_CUDA(cudaFuncSetAttribute(panel_f64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      384 * kPanel * (int)sizeof(double)));
+        for (const void *k : {(const void *)swap_trsm_kernel<true>, (const void *)swap_trsm_kernel<false>})
+            FLG_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          kPanel * kSwapThreads * (int)sizeof(double)));
+        attr_set = true;
+    }
+    const size_t swap_smem = (size_t)kPanel * kSwapThreads * sizeof(double);
     FLG_CUDA(cudaMemsetAsync(bar, 0, sizeof(GridBar), st));
-    FLG_CUDA(cudaFuncSetAttribute(panel_f64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  384 * kPanel * (int)sizeof(double)));
-    for (int64_t k0 = 0; k0 < n; k0 += kPanel) {
+    // the panel of columns [k0, k0 + kb), rows k0.. on stream s
+    auto panel = [&](int64_t k0, cudaStream_t s) -> int {
         const int kb = (int)std::min<int64_t>(kPanel, n - k0);
         const int64_t m = n - k0;
         int nblk, rpc;
@@ -1147,36 +1386,65 @@ extern "C" int flg_lu_factor_f64(int64_t n, double *A, int64_t ld, int32_t *ipiv
         const size_t smem = (size_t)rpc * kb * sizeof(double);
         FLG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, panel_f64_kernel, 256, smem));
         FLG_REQUIRE(per_sm * sm_count() >= nblk, "panel grid (%d CTAs) cannot be co-resident", nblk);
-        PanelArgs pa{A, ld, n, k0, kb, rpc, ipiv, bar, slot_val, slot_row, rowbuf, diagbuf};
+        // both buffers of the published words to parity 1 (columns 0 and 1 expect parity 0)
+        FLG_CUDA(cudaMemsetAsync(word, 0x80, 2 * (size_t)maxblk * sizeof(unsigned long long), s));
+        PanelArgs pa{A, ld, n, k0, kb, rpc, ipiv, bar, word, rowbuf, diagbuf};
         void *args[] = {&pa};
-        prof_begin(FLG_SLOT_LU_PANEL, st);
-        FLG_CUDA(cudaLaunchCooperativeKernel((void *)panel_f64_kernel, dim3(nblk), dim3(256), args, smem, st));
+        prof_begin(FLG_SLOT_LU_PANEL, s);
+        FLG_CUDA(cudaLaunchCooperativeKernel((void *)panel_f64_kernel, dim3(nblk), dim3(256), args, smem, s));
         count_launch();
-        prof_end(FLG_SLOT_LU_PANEL, st);
+        prof_end(FLG_SLOT_LU_PANEL, s);
+        return FLG_OK;
+    };
+    // Look-ahead: after each panel's trailing update has reached the next panel's 64 columns,
+    // the next panel factors on the panel stream while the main stream updates the rest.
+    // The interchanges of the columns left of each panel go to the left stream, in order.
+    FLG_CUDA(cudaEventRecord(fs->factored, st));
+    FLG_CUDA(cudaStreamWaitEvent(fs->left, fs->factored, 0));  // the left stream starts after prior work
+    FLG_TRY(panel(0, st));
+    bool ahead = false;  // the current panel ran ahead on the panel stream
+    for (int64_t k0 = 0; k0 < n; k0 += kPanel) {
+        const int kb = (int)std::min<int64_t>(kPanel, n - k0);
+        if (ahead) FLG_CUDA(cudaStreamWaitEvent(st, fs->panel_done, 0));
         if (k0 > 0) {
-            laswp_kernel<<<(unsigned)ceil_div(k0, 256), 256, 0, st>>>(A, ld, ipiv, k0, kb, 0, k0);
+            FLG_CUDA(cudaEventRecord(fs->factored, st));
+            FLG_CUDA(cudaStreamWaitEvent(fs->left, fs->factored, 0));
+            swap_trsm_kernel<false><<<(unsigned)ceil_div(k0, kSwapThreads), kSwapThreads, swap_smem, fs->left>>>(
+                A, ld, ipiv, k0, kb, 0, k0);
             FLG_LAUNCH_CHECK();
         }
         const int64_t c0 = k0 + kb;
-        if (c0 < n) {
-            const int64_t nc = n - c0;
-            laswp_kernel<<<(unsigned)ceil_div(nc, 256), 256, 0, st>>>(A, ld, ipiv, k0, kb, c0, n);
+        ahead = false;
+        if (c0 >= n) break;
+        const int64_t nc = n - c0;
+        swap_trsm_kernel<true><<<(unsigned)ceil_div(nc, kSwapThreads), kSwapThreads, swap_smem, st>>>(A, ld, ipiv, k0,
+                                                                                                     kb, c0, n);
+        FLG_LAUNCH_CHECK();
+        prof_begin(FLG_SLOT_LU_UPDATE, st);
+        const int64_t nn = std::min<int64_t>(kPanel, nc);  // the next panel's columns first
+        dgemm_update_kernel<<<dim3((unsigned)ceil_div(nn, 64), (unsigned)ceil_div(nc, 64)), 256, 0, st>>>(
+            A + c0 * ld + c0, A + c0 * ld + k0, A + k0 * ld + c0, ld, nc, nn, kb);
+        FLG_LAUNCH_CHECK();
+        if (nc > nn) {
+            FLG_CUDA(cudaEventRecord(fs->next_ready, st));
+            FLG_CUDA(cudaStreamWaitEvent(fs->panel, fs->next_ready, 0));
+            FLG_TRY(panel(c0, fs->panel));
+            FLG_CUDA(cudaEventRecord(fs->panel_done, fs->panel));
+            ahead = true;
+            dgemm_update_kernel<<<dim3((unsigned)ceil_div(nc - nn, 64), (unsigned)ceil_div(nc, 64)), 256, 0, st>>>(
+                A + c0 * ld + c0 + nn, A + c0 * ld + k0, A + k0 * ld + c0 + nn, ld, nc, nc - nn, kb);
             FLG_LAUNCH_CHECK();
-            trsm_f64_kernel<<<(unsigned)ceil_div(nc, 128), 128, 0, st>>>(A, ld, k0, c0, n);
-            FLG_LAUNCH_CHECK();
-            dim3 grid((unsigned)ceil_div(nc, 64), (unsigned)ceil_div(nc, 64));
-            prof_begin(FLG_SLOT_LU_UPDATE, st);
-            dgemm_update_kernel<<<grid, 256, 0, st>>>(A + c0 * ld + c0, A + c0 * ld + k0, A + k0 * ld + c0, ld, nc, nc,
-                                                      kb);
-            FLG_LAUNCH_CHECK();
-            prof_end(FLG_SLOT_LU_UPDATE, st);
         }
+        prof_end(FLG_SLOT_LU_UPDATE, st);
+        if (!ahead) FLG_TRY(panel(c0, st));  // the last panel: nothing to overlap it with
     }
+    FLG_CUDA(cudaEventRecord(fs->left_done, fs->left));
+    FLG_CUDA(cudaStreamWaitEvent(st, fs->left_done, 0));
     GridBar hb;
     FLG_CUDA(cudaMemcpyAsync(&hb, bar, sizeof(GridBar), cudaMemcpyDeviceToHost, st));
     FLG_CUDA(cudaStreamSynchronize(st));
     if (hb.err) {
-        set_error("a bounded device wait timed out (LU panel grid barrier)");
+        set_error("a bounded device wait timed out (LU panel exchange)");
         return FLG_ERR_TIMEOUT;
     }
     *info = hb.info;
