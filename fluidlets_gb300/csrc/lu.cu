@@ -25,6 +25,7 @@
 // diagonal block's warp handshake, an iteration count) is bounded and reports
 // failure through a device flag instead of hanging.
 #include <cooperative_groups.h>
+#include <cuda.h>
 
 #include <algorithm>
 
@@ -1005,41 +1006,46 @@ static int copy2d(cudaStream_t st, const float *src, int64_t lds, float *dst, in
 }
 
 // ---- low precision triangular solve with the diagonal-block inverses ------------------
-// x = U^-1 L^-1 b for one right-hand side, FP32 factors, as a dataflow over the
-// 128-row blocks in ONE cooperative launch.  CTA c owns blocks c, c + G, ...
-// (G CTAs).  Forward: y_i = Linv_i (b_i - sum_{j<i} L_ij y_j); the owner of
-// block i consumes y_0, y_1, ... as their owners publish them, accumulating
-// L_ij y_j for all of its blocks, and finalizes block i as soon as y_{i-1} has
-// arrived.  The two operands on that critical step -- L_{i,i-1} and Linv_i --
-// are prefetched into registers before the wait.  Backward: the same in
-// reverse with U and Uinv on x_i = Uinv_i (y_i - sum_{j>i} U_ij x_j).
-// Publication is the data itself: y and x start filled with an all-ones bit
-// pattern (a NaN that FP32 arithmetic never produces; results are stored
-// canonicalized), values are stored with st.relaxed.gpu and consumers poll
-// their element with ld.relaxed.gpu (bounded) -- no flag, no fence.  Every
-// wait is on a block earlier in the global order (forward by increasing, then
-// backward by decreasing index) and all CTAs are resident, so the order always
-// advances.  512 threads: thread t covers row t / 4 of a block, columns
-// 32 (t % 4) + 0..31.
-constexpr int kApplyThreads = 512;
+// x = U^-1 L^-1 b for one right-hand side, FP32 factors, as a dataflow over the 128-row
+// blocks in ONE cooperative launch of G CTAs.  CTA c owns the q consecutive blocks
+// [c q, c q + q) (q <= kApplyQ).  In "pass order" -- the forward pass by increasing block,
+// the backward pass by decreasing block -- block p needs every earlier block p' < p:
+//   forward   y_i = Linv_i (b_i - sum_{j<i} L_ij y_j)
+//   backward  x_i = Uinv_i (y_i - sum_{j>i} U_ij x_j).
+// A CTA accumulates the contributions of the blocks before its chunk as their owners
+// publish them, then runs through its own chunk locally: each finished block goes straight
+// from shared memory into the later blocks of the chunk, so only one result in q crosses
+// between SMs (through L2) on the critical chain.
+//   * One producer thread streams the 128 x 128 FP32 slices in the order they are used
+//     (for each earlier source block, its slice for every own block; for each own block,
+//     its inverse, then its slices for the later own blocks) by TMA (cp.async.bulk.tensor,
+//     64 KB each) into a 3-stage shared-memory ring guarded by mbarriers; rows and
+//     columns outside the matrix arrive as zeros.
+//   * Eight consumer warps own 16 rows of every block; lane l multiplies columns
+//     4l..4l+3 of its rows (one conflict-free 16-byte load per row) by its float4 of the
+//     source block and keeps 16 running partial sums per own block; finishing a block
+//     reduce-scatters them over the lanes (16 shuffles).
+//   * Publication is the data itself: y and x start filled with an all-ones bit pattern
+//     (a NaN that FP32 arithmetic never produces; results are stored canonicalized),
+//     values are stored with st.relaxed.gpu and consumers poll their four elements with
+//     ld.relaxed.gpu (bounded) -- no flag, no fence.  Every wait is on a block earlier in
+//     the global order (forward, then backward) and all CTAs are resident, so the order
+//     always advances.
+// Each block's sum runs in one CTA in a fixed order (by source block), so the result does
+// not depend on G.
+constexpr int kApplyConsumers = 8;                         // warps
+constexpr int kApplyThreads = (kApplyConsumers + 1) * 32;  // + the producer warp
+constexpr int kApplyStages = 3;
+constexpr int kApplyQ = 4;                  // at most this many blocks per CTA
+constexpr int kSliceBytes = kNB * kNB * 4;  // 64 KB
+constexpr size_t kApplySmem = (size_t)kApplyStages * kSliceBytes + 1024;
 constexpr unsigned kUnset = 0xffffffffu;
 
-// A 128-entry vector in shared memory is stored as four 32-float quarters kQP
-// floats apart: the four quarters that the threads of a warp read at once then
-// sit in different banks (with a plain 32-float stride, all four hit the same
-// bank, a 4-way conflict on every load).
-constexpr int kQP = 36;
-__device__ __forceinline__ int qpos(int e) { return (e >> 5) * kQP + (e & 31); }
-
-
 struct ApplyArgs {
-    const float *LU;
-    int64_t ld, n;
-    const float *Linv, *Uinv;
+    int64_t n;
+    int q;           // blocks per CTA
     const float *b;  // right-hand side (FP32, n)
     float *y, *x;    // forward / backward results (n), preset to kUnset
-    float *part;     // team partial sums [2 passes][blocks][T][128], preset to kUnset
-    int T;           // CTAs per owned block (team size)
     int *err;        // a wait ran out
 };
 
@@ -1048,190 +1054,221 @@ __device__ __forceinline__ void st_relaxed_f32(float *p, float v) {
     if (u == kUnset) u = 0x7fffffffu;  // keep the sentinel unique
     asm volatile("st.relaxed.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(u) : "memory");
 }
-
-// sum over the four threads of a row (consecutive lanes)
-__device__ __forceinline__ float row_sum4(float v) {
-    v += __shfl_xor_sync(0xffffffffu, v, 1);
-    v += __shfl_xor_sync(0xffffffffu, v, 2);
-    return v;
+__device__ __forceinline__ void tma_load_box(void *dst, const CUtensorMap *map, uint64_t *bar, int x, int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
+            smem_u32(dst)),
+        "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(x), "r"(y)
+        : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive1(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-// vec = block j of src, each of the first 128 threads waiting (bounded) for its
-// element to be published (`first` is an earlier probe of that element);
-// false (for the whole CTA) if a wait ran out here or elsewhere
-__device__ bool fetch_block(float *vec, const float *src, int64_t j, int64_t n, unsigned first, int *err,
-                            int *abort_s) {
-    const int t = threadIdx.x;
-    if (t < kNB) {
-        const int64_t e = j * kNB + t;
-        float v = 0.0f;
-        if (e < n) {
-            unsigned u;
-            if (!wait_published(src + e, kUnset, first, &u, kWaitLimitNs, err)) *abort_s = 1;
-            v = __uint_as_float(u);
-        }
-        vec[qpos(t)] = v;
-    }
-    __syncthreads();
-    return *(volatile int *)abort_s == 0;
-}
-
-// Per-thread prefetch ring: thread t's 32-float slice of each consumed block goes
-// to shared memory by cp.async (kRing blocks in flight, 64 KB each per CTA);
-// 16-byte chunk c of thread t sits at chunk position c ^ (t % 8), so the
-// LDS.128 reads of a warp are free of bank conflicts.
-constexpr int kRing = 3;
-constexpr size_t kApplySmem = (size_t)kRing * kApplyThreads * 32 * sizeof(float);
-
-__device__ __forceinline__ void ring_issue(float *slot, const float *src, int valid_floats) {
-    const int t = threadIdx.x;
-    float *dst = slot + t * 32;
+// the published float4 of a block (elements e .. e+3, those < n): the four loads are issued
+// together, then any still unset is polled until published
+__device__ __forceinline__ bool fetch4(const float *v, int64_t e, int64_t n, float4 &out, int *err) {
+    unsigned first[4];
 #pragma unroll
-    for (int c = 0; c < 8; c++) {
-        const int bytes = max(0, min(16, (valid_floats - 4 * c) * 4));
-        const float *g = bytes > 0 ? src + 4 * c : src;  // a valid address even when nothing is read
-        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(
-                         (unsigned)__cvta_generic_to_shared(dst + 4 * (c ^ (t & 7)))),
-                     "l"(g), "r"(bytes)
-                     : "memory");
-    }
-}
-// dot of a 32-float slice with quarter v (kQP layout), float4 reads
-__device__ __forceinline__ float dot32q(const float (&w)[32], const float *v) {
-    float a0 = 0.f, a1 = 0.f;
+    for (int k = 0; k < 4; k++) first[k] = e + k < n ? ld_relaxed_u32(v + e + k) : 0u;
+    float f[4];
 #pragma unroll
-    for (int c = 0; c < 32; c += 4) {
-        const float4 x = *reinterpret_cast<const float4 *>(v + c);
-        a0 = fmaf(w[c], x.x, a0);
-        a1 = fmaf(w[c + 1], x.y, a1);
-        a0 = fmaf(w[c + 2], x.z, a0);
-        a1 = fmaf(w[c + 3], x.w, a1);
+    for (int k = 0; k < 4; k++) {
+        unsigned u = first[k];
+        if (e + k < n && !wait_published(v + e + k, kUnset, first[k], &u, kWaitLimitNs, err)) return false;
+        f[k] = __uint_as_float(u);
     }
-    return a0 + a1;
-}
-__device__ __forceinline__ float ring_dot(const float *slot, const float *v) {
-    const int t = threadIdx.x;
-    const float *src = slot + t * 32;
-    float a0 = 0.f, a1 = 0.f;
-#pragma unroll
-    for (int c = 0; c < 8; c++) {
-        const float4 w = *reinterpret_cast<const float4 *>(src + 4 * (c ^ (t & 7)));
-        const float4 x = *reinterpret_cast<const float4 *>(v + 4 * c);
-        a0 = fmaf(w.x, x.x, a0);
-        a1 = fmaf(w.y, x.y, a1);
-        a0 = fmaf(w.z, x.z, a0);
-        a1 = fmaf(w.w, x.w, a1);
-    }
-    return a0 + a1;
+    out = make_float4(f[0], f[1], f[2], f[3]);
+    return true;
 }
 
-// loads that stay where they are written (volatile asm is not moved past the other
-// volatile asm of the loop), so operands needed after a wait are fetched before it
-__device__ __forceinline__ void load_row32_early(float (&v)[32], const float *p) {
+// sum of acc[0..15] over the 32 lanes, scattered: lanes 2r and 2r + 1 end with row r's total
+__device__ __forceinline__ float reduce_scatter16(float (&acc)[16], int lane) {
+    float a8[8], a4[4], a2[2];
+    const bool h4 = lane & 16, h3 = lane & 8, h2 = lane & 4, h1 = lane & 2;
 #pragma unroll
-    for (int c = 0; c < 32; c += 4)
-        asm volatile("ld.global.nc.v4.f32 {%0, %1, %2, %3}, [%4];"
-                     : "=f"(v[c]), "=f"(v[c + 1]), "=f"(v[c + 2]), "=f"(v[c + 3])
-                     : "l"(p + c));
-}
-__device__ __forceinline__ float load_f32_early(const float *p) {
-    float v;
-    asm volatile("ld.global.nc.f32 %0, [%1];" : "=f"(v) : "l"(p));
-    return v;
+    for (int k = 0; k < 8; k++) {
+        const float send = h4 ? acc[k] : acc[8 + k];
+        const float keep = h4 ? acc[8 + k] : acc[k];
+        a8[k] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const float send = h3 ? a8[k] : a8[4 + k];
+        const float keep = h3 ? a8[4 + k] : a8[k];
+        a4[k] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+    }
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        const float send = h2 ? a4[k] : a4[2 + k];
+        const float keep = h2 ? a4[2 + k] : a4[k];
+        a2[k] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+    }
+    const float send = h1 ? a2[0] : a2[1];
+    const float keep = h1 ? a2[1] : a2[0];
+    const float a1 = keep + __shfl_xor_sync(0xffffffffu, send, 2);
+    return a1 + __shfl_xor_sync(0xffffffffu, a1, 1);
 }
 
-__global__ void __launch_bounds__(kApplyThreads) lowp_apply_kernel(ApplyArgs a) {
-    extern __shared__ __align__(16) float ring[];  // [kRing][kApplyThreads * 32]
-    __shared__ __align__(16) float vec[4 * kQP];    // the block being consumed (kQP layout)
-    __shared__ __align__(16) float tvec[4 * kQP];   // t_i of the block being finalized (kQP layout)
-    __shared__ int abort_s;
-    const int t = threadIdx.x, r = t >> 2, q = t & 3;
-    const int T = a.T, tm = blockIdx.x % T;   // team member (0 = leader, which finalizes)
-    const int GO = gridDim.x / T, o = blockIdx.x / T;  // owner slots, this CTA's slot
-    const int nblk = (int)ceil_div(a.n, kNB);
-    const int nown = o < nblk ? (nblk - 1 - o) / GO + 1 : 0;
-    if (t == 0) abort_s = 0;
-    __syncthreads();
-    for (int pass = 0; pass < 2 && nown > 0; pass++) {
-        const bool fwd = pass == 0;
-        const int dir = fwd ? 1 : -1;
-        const float *D = fwd ? a.Linv : a.Uinv;
-        float *out_v = fwd ? a.y : a.x;  // this pass publishes into out_v and consumes from it
-        // owned blocks in order: ascending forward, descending backward
-        for (int mi = 0; mi < nown; mi++) {
-            const int i = o + (fwd ? mi : nown - 1 - mi) * GO;
-            const int64_t row = (int64_t)i * kNB + r;
-            const bool rok = row < a.n;
-            float Dr[32];
-            float rhs = 0.0f;
-            if (tm == 0) {
-                load_row32_early(Dr, D + (int64_t)i * kNB * kNB + r * kNB + 32 * q);
-                if (rok) rhs = fwd ? load_f32_early(a.b + row) : __uint_as_float(ld_relaxed_u32(a.y + row));
+// acc[sel] += S (16 rows of this warp) . v, for a run-time sel < kApplyQ
+__device__ __forceinline__ void slice_fma(float (&acc)[kApplyQ][16], int sel, const float *S, float4 v) {
+#pragma unroll
+    for (int q = 0; q < kApplyQ; q++)
+        if (q == sel) {
+#pragma unroll
+            for (int r = 0; r < 16; r++) {
+                const float4 w = *reinterpret_cast<const float4 *>(S + r * kNB);
+                acc[q][r] = fmaf(w.x, v.x, acc[q][r]);
+                acc[q][r] = fmaf(w.y, v.y, acc[q][r]);
+                acc[q][r] = fmaf(w.z, v.z, acc[q][r]);
+                acc[q][r] = fmaf(w.w, v.w, acc[q][r]);
             }
-            // blocks to consume: k = 0 .. nc - 1 (block jfirst + dir k); member tm takes
-            // k = tm, tm + T, ... below nc - 1, the leader also the critical k = nc - 1
-            const int jfirst = fwd ? 0 : nblk - 1;
-            const int nc = fwd ? i : nblk - 1 - i;
-            auto count = [&](int m) { return nc - 1 > m ? (nc - 1 - m + T - 1) / T : 0; };
-            const int cnt = count(tm) + ((tm == 0 && nc >= 1) ? 1 : 0);
-            auto kth = [&](int u) { return u < count(tm) ? tm + u * T : nc - 1; };
-            auto issue = [&](int u) {
-                const int j = jfirst + dir * kth(u);
-                const int64_t col0 = (int64_t)j * kNB + 32 * q;
-                const int valid = rok ? (int)max((int64_t)0, min((int64_t)32, a.n - col0)) : 0;
-                ring_issue(ring + (u % kRing) * (kApplyThreads * 32), rok ? a.LU + row * a.ld + col0 : a.LU, valid);
-                asm volatile("cp.async.commit_group;" ::: "memory");
-            };
-            auto probe = [&](int u) {
-                const int64_t e = (int64_t)(jfirst + dir * kth(u)) * kNB + t;
-                return (t < kNB && e < a.n) ? ld_relaxed_u32(out_v + e) : 0u;
-            };
-            float acc = 0.0f;
-            int issued = 0;
-            for (; issued < min(kRing, cnt); issued++) issue(issued);
-            unsigned pc = cnt > 0 ? probe(0) : 0u;
-            for (int u = 0; u < cnt; u++) {
-                // slice u has landed once at most (issued - u - 1) newer groups are pending
-                const int pend = issued - u - 1;
-                if (pend >= 2) asm volatile("cp.async.wait_group 2;" ::: "memory");
-                else if (pend == 1) asm volatile("cp.async.wait_group 1;" ::: "memory");
-                else asm volatile("cp.async.wait_group 0;" ::: "memory");
-                const unsigned pn = u + 1 < cnt ? probe(u + 1) : 0u;
-                if (!fetch_block(vec, out_v, jfirst + dir * kth(u), a.n, pc, a.err, &abort_s)) {
-                    asm volatile("cp.async.wait_all;" ::: "memory");
+        }
+}
+
+__global__ void __launch_bounds__(kApplyThreads, 1)
+    lowp_apply_kernel(const __grid_constant__ CUtensorMap mLU, const __grid_constant__ CUtensorMap mD, ApplyArgs a) {
+    extern __shared__ __align__(1024) unsigned char apply_smem[];
+    float *ring = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(apply_smem) + 1023) & ~uintptr_t(1023));
+    __shared__ __align__(8) uint64_t full[kApplyStages], empty[kApplyStages];
+    __shared__ __align__(16) float tvec[kNB], yvec[kNB];
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    const int nblk = (int)ceil_div(a.n, kNB);
+    const int c = blockIdx.x;
+    const int b0 = c * a.q, b1 = min(nblk, b0 + a.q);  // own physical blocks [b0, b1)
+    const int qc = max(0, b1 - b0);
+    if (t == 0) {
+        for (int q = 0; q < kApplyStages; q++) {
+            mbar_init(&full[q], 1);
+            mbar_init(&empty[q], kApplyConsumers);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (qc == 0) return;
+    // pass order: forward p = i, backward p = nblk - 1 - i; own pass-order blocks [p0, p0 + qc)
+    auto blk = [&](bool fwd, int p) { return fwd ? p : nblk - 1 - p; };
+    if (warp == kApplyConsumers) {
+        if (lane == 0) {
+            long long k = 0;  // slices issued
+            bool ok = true;
+            auto issue = [&](const CUtensorMap *m, int x, int y) {
+                const int stg = (int)(k % kApplyStages);
+                if (k >= kApplyStages &&
+                    !mbar_wait(&empty[stg], (uint32_t)((k / kApplyStages - 1) & 1), a.err, kWaitLimitNs)) {
+                    ok = false;
                     return;
                 }
-                acc += ring_dot(ring + (u % kRing) * (kApplyThreads * 32), vec + q * kQP);
-                __syncthreads();  // vec is rewritten next
-                if (issued < cnt) issue(issued++);  // reuses slot u % kRing, just read by this thread
-                pc = pn;
-            }
-            float tot = row_sum4(acc);
-            float *pslot = a.part + ((int64_t)(pass * nblk + i) * T) * kNB;
-            if (tm > 0) {  // a member hands its partial sums to the leader
-                if (count(tm) > 0 && q == 0 && rok) st_relaxed_f32(pslot + tm * kNB + r, tot);
-                continue;
-            }
-            // the leader adds the members' partial sums (each row polled by its q == 0 thread)
-            if (q == 0 && rok) {
-                for (int m = 1; m < T; m++) {
-                    if (count(m) == 0) continue;
-                    unsigned uv;
-                    if (!wait_published(pslot + m * kNB + r, kUnset, kUnset, &uv, kWaitLimitNs, a.err)) {
-                        abort_s = 1;
-                        break;
-                    }
-                    tot += __uint_as_float(uv);
+                mbar_arrive_expect(&full[stg], kSliceBytes);
+                tma_load_box(ring + (size_t)stg * (kNB * kNB), m, &full[stg], x, y);
+                k++;
+            };
+            for (int pass = 0; pass < 2 && ok; pass++) {
+                const bool fwd = pass == 0;
+                const int p0 = fwd ? b0 : nblk - b1;
+                for (int pj = 0; pj < p0 + qc && ok; pj++) {
+                    const int j = blk(fwd, pj);
+                    if (pj >= p0) issue(&mD, 0, (fwd ? j : nblk + j) * kNB);
+                    for (int p = max(p0, pj + 1); p < p0 + qc && ok; p++) issue(&mLU, j * kNB, blk(fwd, p) * kNB);
                 }
             }
-            __syncthreads();
-            if (*(volatile int *)&abort_s) return;
-            // finalize block i: t_i = rhs_i - sum, out_i = D_i t_i, published element by element
-            if (q == 0) tvec[qpos(r)] = rok ? rhs - tot : 0.0f;
-            __syncthreads();
-            const float out = row_sum4(dot32q(Dr, tvec + q * kQP));
-            if (q == 0 && rok) st_relaxed_f32(out_v + row, out);
-            __syncthreads();  // tvec is rewritten by the next block
+            // drain: every issued load has landed before the CTA may exit
+            for (long long q = k > kApplyStages ? k - kApplyStages : 0; q < k; q++)
+                mbar_drain(&full[q % kApplyStages], (uint32_t)((q / kApplyStages) & 1), a.err, kWaitLimitNs);
+        }
+        return;
+    }
+    // consumers.  After a wait has run out (a.err raised, possibly by another CTA) a warp
+    // keeps the loop's structure -- every stage is still waited for (each wait now returns at
+    // once) and released, and every named barrier is reached -- so the producer can stop and
+    // drain and no warp waits on one that has left; the results are then discarded.
+    long long k = 0;  // slices consumed
+    bool dead = false;
+    const int row0 = warp * 16;
+    auto take = [&]() -> const float * {  // the next ring stage, this warp's rows and lane's columns
+        const int stg = (int)(k % kApplyStages);
+        dead = !__all_sync(0xffffffffu, !dead);
+        if (!mbar_wait(&full[stg], (uint32_t)((k / kApplyStages) & 1), a.err, kWaitLimitNs)) dead = true;
+        return ring + (size_t)stg * (kNB * kNB) + (size_t)row0 * kNB + 4 * lane;
+    };
+    auto release = [&]() {
+        __syncwarp();
+        if (lane == 0) mbar_arrive1(&empty[k % kApplyStages]);
+        k++;
+    };
+    for (int pass = 0; pass < 2; pass++) {
+        const bool fwd = pass == 0;
+        float *out_v = fwd ? a.y : a.x;  // published into and consumed from
+        const int p0 = fwd ? b0 : nblk - b1;
+        float acc[kApplyQ][16];
+#pragma unroll
+        for (int q = 0; q < kApplyQ; q++)
+#pragma unroll
+            for (int r = 0; r < 16; r++) acc[q][r] = 0.0f;
+        // this lane's right-hand side entries of the own blocks (lanes 2r, 2r + 1 hold row r)
+        float rhs[kApplyQ];
+#pragma unroll
+        for (int q = 0; q < kApplyQ; q++) {
+            rhs[q] = 0.0f;
+            if (q < qc) {
+                const int64_t e = (int64_t)blk(fwd, p0 + q) * kNB + row0 + (lane >> 1);
+                if (e < a.n) rhs[q] = fwd ? a.b[e] : __uint_as_float(ld_relaxed_u32(a.y + e));
+            }
+        }
+        for (int pj = 0; pj < p0 + qc; pj++) {
+            const int j = blk(fwd, pj);
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (pj < p0) {
+                // an earlier block, published by its owner
+                if (!dead && !fetch4(out_v, (int64_t)j * kNB + 4 * lane, a.n, v, a.err)) dead = true;
+            } else {
+                // an own block: t = rhs - sums, then out_j = inverse . t, published and kept
+                const int sel = pj - p0;
+                float tmp[16];
+                float rh = 0.0f;
+#pragma unroll
+                for (int q = 0; q < kApplyQ; q++)
+                    if (q == sel) {
+#pragma unroll
+                        for (int r = 0; r < 16; r++) tmp[r] = acc[q][r];
+                        rh = rhs[q];
+                    }
+                const float tot = reduce_scatter16(tmp, lane);
+                if ((lane & 1) == 0) tvec[row0 + (lane >> 1)] = rh - tot;
+                asm volatile("bar.sync 1, %0;" ::"r"(kApplyConsumers * 32) : "memory");
+                const float4 tv = *reinterpret_cast<const float4 *>(tvec + 4 * lane);
+#pragma unroll
+                for (int r = 0; r < 16; r++) tmp[r] = 0.0f;
+                const float *S = take();
+#pragma unroll
+                for (int r = 0; r < 16; r++) {
+                    const float4 w = *reinterpret_cast<const float4 *>(S + r * kNB);
+                    tmp[r] = fmaf(w.x, tv.x, tmp[r]);
+                    tmp[r] = fmaf(w.y, tv.y, tmp[r]);
+                    tmp[r] = fmaf(w.z, tv.z, tmp[r]);
+                    tmp[r] = fmaf(w.w, tv.w, tmp[r]);
+                }
+                release();
+                const float res = reduce_scatter16(tmp, lane);
+                if ((lane & 1) == 0) {
+                    const int r = row0 + (lane >> 1);
+                    const int64_t e = (int64_t)j * kNB + r;
+                    yvec[r] = e < a.n ? res : 0.0f;
+                    if (e < a.n) st_relaxed_f32(out_v + e, res);
+                }
+                asm volatile("bar.sync 1, %0;" ::"r"(kApplyConsumers * 32) : "memory");
+                v = *reinterpret_cast<const float4 *>(yvec + 4 * lane);
+            }
+            // (tvec and yvec are rewritten only after the next own block's first barrier, which
+            // every warp reaches after its last read of them)
+            for (int p = max(p0, pj + 1); p < p0 + qc; p++) {
+                const float *S = take();
+                slice_fma(acc, p - p0, S, v);
+                release();
+            }
         }
     }
 }
@@ -1246,17 +1283,17 @@ __global__ void f2d_kernel(const float *a, double *b, int64_t n, const int *err)
     if (i < n) b[i] = *err ? __longlong_as_double(0x7ff8000000000000LL) : (double)a[i];
 }
 
-constexpr int kApplyMaxTeam = 8;
-// CTAs per owned block: spare SMs share the consumption of each block row
-static int apply_team(int64_t nblk) {
-    return (int)std::max<int64_t>(1, std::min<int64_t>(kApplyMaxTeam, sm_count() / std::max<int64_t>(nblk, 1)));
-}
+int make_box_map_f32(CUtensorMap *map, const float *base, int64_t rows, int64_t cols, int64_t ld, int box_rows,
+                     int box_cols);
+
+// blocks per CTA of the low-precision solve: 2 measured fastest on GB300 from n = 1,536 to
+// 24,576 (1 hands every block between SMs; 3 and 4 lengthen each CTA's slice stream)
+constexpr int kApplyQDefault = 2;
 
 size_t lu_solve_lowp_bytes(int64_t n) {
     CountingArena c;
-    const int64_t nblk = ceil_div(std::max<int64_t>(n, 1), kNB);
     c.take<float>(n);
-    c.take<float>(3 * n + 2 * nblk * kApplyMaxTeam * kNB);  // y, x, team partials: one sentinel fill
+    c.take<float>(2 * n);  // y, x: one sentinel fill
     c.take<int>(1);
     return c.bytes();
 }
@@ -1267,19 +1304,25 @@ int lu_solve_lowp_apply(int64_t n, const float *LU, int64_t ld, const float *din
     Arena ar(work, work_bytes);
     const int64_t nblk = ceil_div(n, kNB);
     float *bf = ar.take<float>(n);
-    float *yz = ar.take<float>(3 * n + 2 * nblk * kApplyMaxTeam * kNB);
+    float *yz = ar.take<float>(2 * n);
     int *err = ar.take<int>(1);
     FLG_REQUIRE(bf && yz && err, "workspace too small for the low-precision solve");
-    float *y = yz, *z = yz + n, *part = yz + 2 * n;
-    const int T = apply_team(nblk);
-    const int G = (int)std::min<int64_t>(nblk, sm_count() / T) * T;  // T CTAs per owner slot
+    float *y = yz, *z = yz + n;
+    // blocks per CTA: the chain crosses SMs once per q blocks; q grows only as far as the
+    // CTAs' shared streams allow (one CTA per SM)
+    int q = (int)std::max<int64_t>(kApplyQDefault, ceil_div(nblk, sm_count()));
+    q = (int)std::min<int64_t>(q, nblk);
+    FLG_REQUIRE(q <= kApplyQ, "low-precision solve: at most %lld unknowns", (long long)kApplyQ * sm_count() * kNB);
+    const int G = (int)ceil_div(nblk, q);
+    CUtensorMap mLU, mD;
+    FLG_TRY(make_box_map_f32(&mLU, LU, n, n, ld, kNB, kNB));
+    FLG_TRY(make_box_map_f32(&mD, dinv, 2 * nblk * kNB, kNB, kNB, kNB, kNB));
     d2f_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(b, bf, n);
     FLG_LAUNCH_CHECK();
-    // y, z and the partials: one fill with the unset pattern
-    FLG_CUDA(cudaMemsetAsync(yz, 0xff, sizeof(float) * (size_t)(2 * n + 2 * nblk * T * kNB), st));
+    FLG_CUDA(cudaMemsetAsync(yz, 0xff, sizeof(float) * (size_t)(2 * n), st));  // the unset pattern
     FLG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
-    ApplyArgs aa{LU, ld, n, dinv, dinv + nblk * kNB * kNB, bf, y, z, part, T, err};
-    void *args[] = {&aa};
+    ApplyArgs aa{n, q, bf, y, z, err};
+    void *args[] = {&mLU, &mD, &aa};
     static bool attr_set = false;
     if (!attr_set) {
         FLG_CUDA(cudaFuncSetAttribute(lowp_apply_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kApplySmem));

@@ -327,6 +327,25 @@ static int make_c_map(CUtensorMap *map, float *C, int64_t m, int64_t nc, int64_t
     return FLG_OK;
 }
 
+// plain FP32 box map (no swizzle): rows x cols, row stride ld elements, boxes of
+// box_rows x box_cols; reads outside the matrix return zeros
+int make_box_map_f32(CUtensorMap *map, const float *base, int64_t rows, int64_t cols, int64_t ld, int box_rows,
+                     int box_cols) {
+    auto fn = encode_fn();
+    FLG_REQUIRE(fn != nullptr, "cuTensorMapEncodeTiled unavailable");
+    FLG_REQUIRE(((uintptr_t)base & 15) == 0 && (ld * 4) % 16 == 0 && (box_cols * 4) % 16 == 0,
+                "TMA box map not 16-byte aligned");
+    cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)(ld * 4)};
+    cuuint32_t box[2] = {(cuuint32_t)box_cols, (cuuint32_t)box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(base), dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    FLG_REQUIRE(r == CUDA_SUCCESS, "cuTensorMapEncodeTiled failed for a box map (%d)", (int)r);
+    return FLG_OK;
+}
+
 static int sm_count_of_current_device() {
     static std::mutex mu;
     static int cached[64] = {0};
