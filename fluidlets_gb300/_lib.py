@@ -90,6 +90,7 @@ SIGNATURES = {
     "flg_gemv_f64": (c_int, [c_int64, c_int64, _P, c_int64, _P, _P, _P]),
     "flg_gemv_f32": (c_int, [c_int64, c_int64, _P, c_int64, _P, _P, _P]),
     "flg_convert_f64_f32": (c_int, [c_int64, c_int64, _P, c_int64, _P, c_int64, _P]),
+    "flg_convert_f64_f32x2": (c_int, [c_int64, c_int64, _P, c_int64, _P, _P, c_int64, _P]),
     "flg_measure_peaks": (c_int, [POINTER(c_double), POINTER(c_double), _P]),
     "flg_profile_enable": (c_int, [c_int]),
     "flg_profile_read": (c_int, [c_int, POINTER(c_double), POINTER(c_int64)]),

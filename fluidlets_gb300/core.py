@@ -299,8 +299,9 @@ def _lowp_factor_dev(K: torch.Tensor, lu_name: str):
     L = load()
     ld32 = (n + 31) // 32 * 32
     K32 = torch.empty((n, ld32), dtype=torch.float32, device=K.device)
-    check(L.flg_convert_f64_f32(n, n, dv.ptr(K), K.stride(0), dv.ptr(K32), ld32, dv.stream()), "convert")
-    A32 = K32.clone()
+    A32 = torch.empty_like(K32)
+    check(L.flg_convert_f64_f32x2(n, n, dv.ptr(K), K.stride(0), dv.ptr(K32), dv.ptr(A32), ld32, dv.stream()),
+          "convert")
     dinv = torch.empty(L.flg_lu_lowp_dinv_elems(n), dtype=torch.float32, device=K.device)
     mode = lu_mode(lu_name)
     nbytes = L.flg_lu_factor_lowp_workspace(n, mode)

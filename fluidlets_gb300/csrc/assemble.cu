@@ -489,6 +489,28 @@ __global__ void convert_f64_f32_kernel(int64_t nr, int64_t nc, const double *src
             dst[rr * ldd + c] = (float)src[rr * lds + c];
 }
 
+// dst1 = dst2 = (float) src, read once: the mixed solve's two FP32 copies of the FP64 matrix
+// (the one factored in place and the one of the inner matvecs).  Each thread converts four
+// consecutive elements of a row (independent loads in flight); dst2 may be null.
+__global__ void __launch_bounds__(256) convert2_f64_f32_kernel(int64_t nr, int64_t nc, const double *src,
+                                                              int64_t lds, float *dst1, float *dst2, int64_t ldd) {
+    const int64_t per_row = (nc + 3) / 4;
+    const int64_t total = nr * per_row;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = q / per_row, c0 = (q - r * per_row) * 4;
+        const double *s = src + r * lds + c0;
+        float v[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) v[k] = c0 + k < nc ? (float)s[k] : 0.0f;
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            if (c0 + k < nc) {
+                dst1[r * ldd + c0 + k] = v[k];
+                if (dst2) dst2[r * ldd + c0 + k] = v[k];
+            }
+    }
+}
+
 // ---- host side ----------------------------------------------------------------
 static int prepare(int kind, double are, double aim, double mu_re, double mu_im, int out_type, AsmArgs &a) {
     FLG_TRY(check_kernel_args(kind, are, aim));
@@ -835,6 +857,17 @@ extern "C" int flg_grid_points(const double *x_axis, int64_t nx, const double *y
     FLG_REQUIRE(x_axis && y_axis && z_axis && points, "null pointer");
     grid_points_kernel<<<(unsigned)ceil_div(np, 256), 256, 0, as_stream(stream)>>>(x_axis, nx, y_axis, ny, z_axis,
                                                                                     nz, points);
+    FLG_LAUNCH_CHECK();
+    return FLG_OK;
+}
+
+extern "C" int flg_convert_f64_f32x2(int64_t n_rows, int64_t n_cols, const double *src, int64_t lds, float *dst1,
+                                     float *dst2, int64_t ldd, void *stream) {
+    FLG_REQUIRE(n_rows >= 0 && n_cols >= 0 && lds >= n_cols && ldd >= n_cols && dst1, "bad conversion shape");
+    if (n_rows == 0 || n_cols == 0) return FLG_OK;
+    const int64_t work = n_rows * ((n_cols + 3) / 4);
+    const unsigned grid = (unsigned)std::min<int64_t>(ceil_div(work, 256), (int64_t)sm_count() * 16);
+    convert2_f64_f32_kernel<<<grid, 256, 0, as_stream(stream)>>>(n_rows, n_cols, src, lds, dst1, dst2, ldd);
     FLG_LAUNCH_CHECK();
     return FLG_OK;
 }

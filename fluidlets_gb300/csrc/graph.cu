@@ -2,8 +2,8 @@
 //
 // flg_bucket_graph_create captures, on the caller's stream and in thread-local
 // capture mode (other host threads keep launching and allocating freely),
-//   flg_assemble_bucket -> flg_convert_f64_f32 (x2: the factors' copy and the
-//   inner-matvec copy A32) -> flg_lu_factor_lowp_async
+//   flg_assemble_bucket -> flg_convert_f64_f32x2 (the factors' copy and the
+//   inner-matvec copy A32, in one pass) -> flg_lu_factor_lowp_async
 // over fixed buffers, and instantiates it (solve server).  Replaying it with
 // flg_graph_launch refactors whatever points are in the buffers; the real
 // point count is read from device memory by the assembly kernel, so one graph
@@ -57,8 +57,7 @@ extern "C" int flg_bucket_graph_create(int kind, double alpha_re, double alpha_i
     auto seq = [&]() -> int {
         FLG_TRY(flg_assemble_bucket(kind, alpha_re, alpha_im, points, eps, n_real, n_cap, mu_re, K, FLG_F64, n,
                                     stream));
-        FLG_TRY(flg_convert_f64_f32(n, n, K, n, K32, ld32, stream));
-        if (A32) FLG_TRY(flg_convert_f64_f32(n, n, K, n, A32, ld32, stream));
+        FLG_TRY(flg_convert_f64_f32x2(n, n, K, n, K32, A32, ld32, stream));
         return flg_lu_factor_lowp_async(n, K32, ld32, mode, dinv, flags, work, work_bytes, stream);
     };
     return capture_graph(stream, seq, graph_exec);
@@ -81,8 +80,7 @@ extern "C" int flg_swimmer_graph_create(int kind, double alpha_re, double alpha_
         FLG_TRY(flg_assemble_nearest_async(kind, alpha_re, alpha_im, x, N, X, nearest, eps, Q, N, mu_re, 0.0, A,
                                            FLG_F64, n, flags + 2, work, work_bytes, stream));
         FLG_TRY(flg_swimmer_constraints_dev(x, N, x0, X, nearest, Q, A, FLG_F64, n, stream));
-        FLG_TRY(flg_convert_f64_f32(n, n, A, n, K32, ld32, stream));
-        if (A32) FLG_TRY(flg_convert_f64_f32(n, n, A, n, A32, ld32, stream));
+        FLG_TRY(flg_convert_f64_f32x2(n, n, A, n, K32, A32, ld32, stream));
         // the workspace is reused by the LU: the assembly is done with it by then (stream order)
         return flg_lu_factor_lowp_async(n, K32, ld32, mode, dinv, flags, work, work_bytes, stream);
     };

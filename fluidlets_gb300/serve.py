@@ -18,9 +18,11 @@ zero, so the solution is exactly that of the unpadded system (the forces
 agree with a solve of the request alone to rounding).  The per-bucket choice
 of tensor-core precision (TF32 or BF16) and of the trailing updates' tile
 width (128 x 128, 128 x 256, or chosen per update from its shape) is made by a
-small autotuner that times the six combinations on the first request of the
-bucket and keeps the fastest one that converges.  Swimmer requests run the mixed-precision swimmer solve on the
-slot's stream without a graph.
+small autotuner that times the candidates on the first request of the bucket and
+keeps the fastest one that converges.  Swimmer requests run on pooled swimmer
+plans, one per shape size: a captured graph of the nearest map, the nearest-
+neighbour assembly, the constraint rows, the FP32 copies and the tensor-core LU,
+replayed with the request's points, then FP64 GMRES-IR.
 """
 from __future__ import annotations
 
@@ -41,8 +43,9 @@ from .kernels import Stokeslet3D, kernel_params
 
 BUCKET_BASE = 128
 # LU modes the autotuner times per bucket: precision, and the tile width of the trailing updates
-# (no suffix: chosen per update from its shape)
-TUNE_CANDIDATES = ("tf32", "tf32:128", "tf32:256", "bf16", "bf16:128", "bf16:256")
+# (no suffix: chosen per update from its shape); "fp32" factors on the CUDA cores, which can win
+# for the smallest buckets, where the tensor-core updates are too small to fill the GPU
+TUNE_CANDIDATES = ("tf32", "tf32:128", "tf32:256", "bf16", "bf16:128", "bf16:256", "fp32")
 
 
 def bucket_of(n_points: int) -> int:
@@ -130,8 +133,8 @@ class BucketPlan:
         check(L.flg_assemble_bucket(self.kind, self.are, self.aim, dv.ptr(self.pts), dv.ptr(self.eps),
                                     dv.ptr(self.n_real), self.nbp, float(self.mu), dv.ptr(self.K), F64, self.n, st),
               "bucket assembly")
-        check(L.flg_convert_f64_f32(self.n, self.n, dv.ptr(self.K), self.n, dv.ptr(self.K32), self.ld32, st), "convert")
-        check(L.flg_convert_f64_f32(self.n, self.n, dv.ptr(self.K), self.n, dv.ptr(self.A32), self.ld32, st), "convert")
+        check(L.flg_convert_f64_f32x2(self.n, self.n, dv.ptr(self.K), self.n, dv.ptr(self.K32), dv.ptr(self.A32),
+                                      self.ld32, st), "convert")
         check(L.flg_lu_factor_lowp_async(self.n, dv.ptr(self.K32), self.ld32, self.mode, dv.ptr(self.dinv),
                                          dv.ptr(self.flags), dv.ptr(self.lu_ws), self.lu_bytes, st), "LU")
 
@@ -257,15 +260,27 @@ class SolveServer:
 
     # ---- plan pool (lock held) ----------------------------------------------------------
     def _key(self, req, b):
-        lu = self._lu_for(req, b) or "tune"
-        return (kernel_params(req.kernel)[0], b, float(req.mu), lu)
+        """Pool key of the plan a request runs on: resistance plans per (kernel, bucket, mu, LU
+        mode); swimmer plans per (kernel, force and quadrature point counts, eps, mu)."""
+        if isinstance(req, ResistanceRequest):
+            lu = self._lu_for(req, b) or "tune"
+            return ("res", kernel_params(req.kernel)[0], b, float(req.mu), lu)
+        kind = kernel_params(req.kernel if req.kernel is not None else Stokeslet3D())[0]
+        return ("swim", kind, len(req.shape.x), len(req.shape.X), float(req.eps), float(req.mu))
+
+    @staticmethod
+    def _need(req, b):
+        if isinstance(req, ResistanceRequest):
+            return plan_bytes(b)
+        n = 3 * len(req.shape.x) + 6
+        return 16 * n * n + (64 << 20)
 
     def _evict_free(self, need):
         """Free least-recently-used idle plans until `need` more bytes fit the budget."""
         while self._used + need > self.budget and self._lru:
             plan = self._lru.pop(0)
             self._free[plan.key].remove(plan)
-            self._used -= plan_bytes(plan.nbp)
+            self._used -= plan.nbytes
             self.stats["plans_evicted"] += 1
 
     def _pick(self, slot):
@@ -273,24 +288,20 @@ class SolveServer:
         Returns (request, future, t_arrival, bucket, plan or None, reserved bytes) or None."""
         cand = None
         for k, (req, fut, t, b) in enumerate(self._pending[: self.lookahead]):
-            if isinstance(req, ResistanceRequest) and self._free.get(self._key(req, b)):
+            if self._free.get(self._key(req, b)):
                 cand = k
                 break
         if cand is None:
             cand = 0
         req, fut, t, b = self._pending[cand]
-        if isinstance(req, ResistanceRequest):
-            key = self._key(req, b)
-            if self._free.get(key):
-                plan = self._free[key].pop()
-                self._lru.remove(plan)
-                self._pending.pop(cand)
-                self._busy[slot] = True
-                return req, fut, t, b, plan, 0
-            need = plan_bytes(b)
-        else:
-            n = 3 * len(req.shape.x) + 6
-            need = 16 * n * n + (64 << 20)
+        key = self._key(req, b)
+        if self._free.get(key):
+            plan = self._free[key].pop()
+            self._lru.remove(plan)
+            self._pending.pop(cand)
+            self._busy[slot] = True
+            return req, fut, t, b, plan, 0
+        need = self._need(req, b)
         if self._used + need > self.budget:
             self._evict_free(need)
             if self._used + need > self.budget and any(self._busy):
@@ -313,7 +324,7 @@ class SolveServer:
             if isinstance(req, ResistanceRequest):
                 res, plan = self._resistance(slot, stream, req, b, plan)
             else:
-                res = self._swimmer(stream, req)
+                res, plan = self._swimmer(stream, req, plan)
             stream.synchronize()
         return res, plan
 
@@ -336,15 +347,17 @@ class SolveServer:
                 res.t_arrival, res.t_start, res.t_done, res.slot = t_arr, t0, time.perf_counter(), slot
                 fut.set_result(res)
                 with self._cv:
-                    if isinstance(req, ResistanceRequest) and plan is not None:
+                    if plan is not None:  # back into the pool, counted against the budget
+                        if reserved:
+                            plan.nbytes = reserved
                         plan.key = self._key(req, b)
                         self._free.setdefault(plan.key, []).append(plan)
                         self._lru.append(plan)
                     else:
-                        self._used -= reserved  # swimmer systems are transient
+                        self._used -= reserved
             except Exception as e:  # noqa: BLE001 - delivered to the caller
                 with self._cv:
-                    self._used -= reserved if reserved else (plan_bytes(b) if plan is not None else 0)
+                    self._used -= reserved if reserved else getattr(plan, "nbytes", 0)
                 fut.set_exception(e)
             finally:
                 with self._cv:
@@ -413,11 +426,34 @@ class SolveServer:
             self.stats["tuned"][f"{kernel_params(req.kernel)[0]}:{b}"] = lu
         return lu
 
-    def _swimmer(self, stream, req):
-        from .swimming import swimming_problem
+    def _swimmer(self, stream, req, plan):
+        """The free-swimmer instant on a pooled SwimmerPlan of its shape size: one captured graph
+        (nearest map -> nearest-neighbour assembly -> constraint rows -> FP32 copies ->
+        tensor-core LU) replayed with this request's points, then FP64 GMRES-IR."""
+        from .swimming import SwimmerPlan, SwimState, swimming_problem
 
-        st = swimming_problem(req.shape, req.x0, req.B, req.eps, req.mu, req.kernel, precision="mixed", rtol=self.rtol)
-        return Result(st, float("nan"), 0, 0, 0, 0, 0, "tf32", 0)
+        if not self.graphs:  # eager: the mixed-precision swimmer solve, no plan
+            st = swimming_problem(req.shape, req.x0, req.B, req.eps, req.mu, req.kernel, precision="mixed",
+                                  rtol=self.rtol)
+            return Result(st, float("nan"), 0, 0, 0, 0, 0, "tf32", 0), None
+        kernel = Stokeslet3D() if req.kernel is None else req.kernel
+        x0 = np.asarray(req.x0, float)
+        B = np.asarray(req.B, float)
+        x = x0 + np.asarray(req.shape.x, float) @ B.T
+        X = x0 + np.asarray(req.shape.X, float) @ B.T
+        v = np.asarray(req.shape.v, float) @ B.T
+        N = len(x)
+        if plan is None:
+            plan = SwimmerPlan(kernel, N, len(X), req.eps, req.mu, stream=stream)
+            with self._cv:
+                self.stats["plans_built"] += 1
+                self.stats["captures"] += 1
+        rhs = np.zeros(3 * N + 6)
+        rhs[:3 * N] = v.ravel()
+        U, Om, F, nn = plan.solve(x, X, x0, rhs, rtol=self.rtol, stream=stream)
+        with self._cv:
+            self.stats["graph_replays"] += 1
+        return Result(SwimState(U, Om, F, x, X, nn), plan.last_residual, 0, 0, 0, 0, 0, "tf32", 0), plan
 
 
 # ---- the served mixed workload ------------------------------------------------------

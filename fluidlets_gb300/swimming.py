@@ -97,14 +97,15 @@ class SwimmerPlan:
     Each ``solve`` writes the stage's points into the buffers, replays the graph and refines
     with FP64 GMRES-IR; ``swim(..., precision="mixed")`` keeps one plan for all stages."""
 
-    def __init__(self, kernel, N, Q, eps, mu=1.0, lu="tf32", nearest=None):
+    def __init__(self, kernel, N, Q, eps, mu=1.0, lu="tf32", nearest=None, stream=None):
         L = load()
         dev = dv.require_cuda()
         if complex(mu).imag != 0.0:
             raise ValueError("swimming needs a real viscosity")
         self.N, self.Q, self.n = N, Q, 3 * N + 6
         n = self.n
-        self.stream = torch.cuda.Stream(device=dev)
+        self.stream = torch.cuda.Stream(device=dev) if stream is None else stream
+        self.last_residual = float("nan")
         f64 = dict(dtype=torch.float64, device=dev)
         self.x = torch.zeros((N, 3), **f64)
         self.X = torch.zeros((Q, 3), **f64)
@@ -133,16 +134,18 @@ class SwimmerPlan:
                                              dv.ptr(self.ws), wb, st, ctypes.byref(self.graph)), "swimmer graph")
         self.stream.synchronize()
 
-    def solve(self, x, X, x0, rhs, rtol=1e-10):
+    def solve(self, x, X, x0, rhs, rtol=1e-10, stream=None):
         """(U, Omega, forces, nearest) for world-frame force points x, quadrature points X,
-        origin x0 and right-hand side rhs (3N + 6)."""
+        origin x0 and right-hand side rhs (3N + 6), on `stream` (default: the plan's own);
+        the refinement's final FP64 residual is left in last_residual."""
         L = load()
-        with torch.cuda.stream(self.stream):
+        st = self.stream if stream is None else stream
+        with torch.cuda.stream(st):
             self.x.copy_(torch.from_numpy(np.ascontiguousarray(x, float)))
             self.X.copy_(torch.from_numpy(np.ascontiguousarray(X, float)))
             self.x0.copy_(torch.from_numpy(np.asarray(x0, float)))
             b = torch.from_numpy(np.ascontiguousarray(rhs, float)).to(self.x.device)
-            check(L.flg_graph_launch(self.graph, ctypes.c_void_p(self.stream.cuda_stream)), "swimmer graph replay")
+            check(L.flg_graph_launch(self.graph, ctypes.c_void_p(st.cuda_stream)), "swimmer graph replay")
             fl = self.flags.cpu()
             if int(fl[2]):
                 raise ValueError("nearest indices must lie in [0, n_force)")
@@ -150,8 +153,8 @@ class SwimmerPlan:
                 raise RuntimeError("low-precision LU: a bounded device wait timed out")
             if int(fl[0]):
                 raise np.linalg.LinAlgError(f"zero or non-finite pivot at row {int(fl[0]) - 1} in the low-precision LU")
-            sol, *_ = _gmres_ir_dense_dev(self.A, self.K32, self.ld32, self.dinv, b, rtol * 1e-2, 60, 200,
-                                          required=rtol, A32=self.A32)
+            sol, _, _, self.last_residual = _gmres_ir_dense_dev(self.A, self.K32, self.ld32, self.dinv, b, rtol * 1e-2,
+                                                                60, 200, required=rtol, A32=self.A32)
             sol = dv.to_host(sol)
             nn = self.nn.cpu().numpy()
         N = self.N

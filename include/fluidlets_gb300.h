@@ -363,6 +363,10 @@ int flg_gemv_f32(int64_t n_rows, int64_t n_cols, const float *A, int64_t ld, con
 /* dst (FP32, ldd) = (float) src (FP64, lds), n_rows x n_cols */
 int flg_convert_f64_f32(int64_t n_rows, int64_t n_cols, const double *src, int64_t lds, float *dst, int64_t ldd,
                         void *stream);
+/* dst1 = dst2 = (float) src in one pass over src (dst2 may be NULL): the mixed
+ * solve's factored copy and inner-matvec copy.  No counterpart in the reference. */
+int flg_convert_f64_f32x2(int64_t n_rows, int64_t n_cols, const double *src, int64_t lds, float *dst1, float *dst2,
+                          int64_t ldd, void *stream);
 
 /* ---- measurement ----------------------------------------------------------
  * Throughput microbenchmarks used as roofline denominators (FFMA FP32, DFMA

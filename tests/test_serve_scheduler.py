@@ -104,7 +104,7 @@ def test_autotuner_keeps_the_fastest_candidate_that_converges(monkeypatch):
     import fluidlets_gb300.serve as sv
 
     cost = {"tf32": 0.012, "tf32:128": 0.018, "tf32:256": 0.009, "bf16": 0.006, "bf16:128": 0.003,
-            "bf16:256": 0.015}
+            "bf16:256": 0.015, "fp32": 0.020}
     resid = dict.fromkeys(cost, 1e-12)
     resid["bf16:128"] = 1e-6  # fastest, but does not converge
     tried = []
