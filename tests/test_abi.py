@@ -55,7 +55,7 @@ def test_lu_mode_names_match_the_header(lib):
         assert lib.LU_MODE[f"{prec}:128"] == c[f"FLG_LU_{prec.upper()}"] | c["FLG_LU_TILE_N128"]
         assert lib.LU_MODE[f"{prec}:256"] == c[f"FLG_LU_{prec.upper()}"] | c["FLG_LU_TILE_N256"]
     from fluidlets_gb300.serve import TUNE_CANDIDATES
-    assert set(TUNE_CANDIDATES) <= set(lib.LU_MODE) and len(set(TUNE_CANDIDATES)) == 6
+    assert set(TUNE_CANDIDATES) <= set(lib.LU_MODE) and len(set(TUNE_CANDIDATES)) == 7
 
 
 def test_lu_workspace_does_not_depend_on_the_tile_width(lib):
