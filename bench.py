@@ -304,7 +304,74 @@ def wall_lu_section(dev, n_points=8192, h=1.05, reps=3):
                               "rel_force_err_vs_fp64": err, "residual": im.residual, "ir_steps": im.ir_steps,
                               "gmres_iterations": im.iterations,
                               "speedup_vs_fp64": res["fp64_gpu"]["ms"] / float(np.mean(ms))}
+        # the tensor-core trailing updates of one solve: 2/3 n^3 flops over their own launches' time
+        # (CUDA events on the launching stream); the denominator is a cuBLAS GEMM of the same operand
+        # type measured below
+        from fluidlets_gb300 import _lib
+
+        L = _lib.load()
+        L.flg_profile_enable(1)
+        fl.resistance(k, X, U, e, method="lu", precision="mixed", lu=lu)
+        import ctypes
+
+        upd_ms, upd_n = ctypes.c_double(0), ctypes.c_int64(0)
+        L.flg_profile_read(_lib.SLOT["lu_update"], ctypes.byref(upd_ms), ctypes.byref(upd_n))
+        app_ms, app_n = ctypes.c_double(0), ctypes.c_int64(0)
+        L.flg_profile_read(_lib.SLOT["lu_solve"], ctypes.byref(app_ms), ctypes.byref(app_n))
+        L.flg_profile_enable(0)
+        n = 3 * n_points
+        res[f"mixed_{lu}"]["tensor_updates"] = {"ms": upd_ms.value, "launches": upd_n.value,
+                                                "tflops": 2.0 / 3.0 * n ** 3 / (upd_ms.value * 1e-3) / 1e12}
+        ld32 = (n + 31) // 32 * 32
+        res[f"mixed_{lu}"]["preconditioner_apply"] = {
+            "ms_per_application": app_ms.value / max(app_n.value, 1), "applications": app_n.value,
+            "gbs": 4.0 * n * ld32 / (app_ms.value / max(app_n.value, 1) * 1e-3) / 1e9,
+            "bytes": "L and U once: 4 n^2 bytes (FP32) per application"}
+    res["cublas_peaks"] = gemm_peaks(dev)
+    for lu in ("tf32", "bf16"):
+        peak = res["cublas_peaks"][lu]
+        res[f"mixed_{lu}"]["tensor_updates"]["frac_of_cublas"] = res[f"mixed_{lu}"]["tensor_updates"]["tflops"] / peak
+        res[f"mixed_{lu}"]["preconditioner_apply"]["frac_of_hbm"] = (
+            res[f"mixed_{lu}"]["preconditioner_apply"]["gbs"] / hbm_peak_gbs())
     return res
+
+
+def hbm_peak_gbs():
+    """Measured copy bandwidth of the GB300s (generated MEASURED_PEAKS.json), or the
+    stated fallback of 6,800 GB/s when the file is absent."""
+    try:
+        return float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"])
+    except (OSError, ValueError, KeyError):
+        return 6800.0
+
+
+def gemm_peaks(dev, n=8192, reps=5):
+    """Dense tensor-core denominators for the LU updates: cuBLAS (through torch.matmul) TF32 and BF16
+    GEMMs of n^3, best of `reps` (CUDA events), in TFLOP/s."""
+    import torch
+
+    out = {}
+    prev = torch.backends.cuda.matmul.allow_tf32
+    try:
+        for name, dt in (("tf32", torch.float32), ("bf16", torch.bfloat16)):
+            torch.backends.cuda.matmul.allow_tf32 = name == "tf32"
+            a = torch.randn(n, n, device=dev, dtype=dt)
+            b = torch.randn(n, n, device=dev, dtype=dt)
+            torch.matmul(a, b)
+            best = float("inf")
+            for _ in range(reps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                torch.matmul(a, b)
+                e1.record()
+                torch.cuda.synchronize()
+                best = min(best, e0.elapsed_time(e1))
+            out[name] = 2.0 * n ** 3 / (best * 1e-3) / 1e12
+            del a, b
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+    out["source"] = f"cuBLAS via torch.matmul, {n}^3, best of {reps} (measured in this run)"
+    return out
 
 
 def serve_section(n_requests=512, rate=200.0, slots=6):
