@@ -337,6 +337,50 @@ def _gmres_ir_dense_dev(K, K32, ld32, dinv, b, rtol, restart, maxiter, required=
     return x, iters.value, outer.value, resid.value
 
 
+class IrGraph:
+    """The FP64 GMRES-IR of K x = b (low-precision factors K32/dinv as preconditioner, inner
+    matvecs on the FP32 copy A32) as one replayable CUDA graph over fixed buffers: the loops run
+    as conditional graph nodes steered on the device, so ``launch`` costs no host round trip and
+    ``result`` reads the outcome once.  b and x are fixed device vectors; write a new right-hand
+    side into b before a replay."""
+
+    def __init__(self, K, A32, K32, ld32, dinv, b, x, rtol, m=30, max_outer=60, stream=None):
+        L = load()
+        n = K.shape[0]
+        self.nbytes = L.flg_gmres_ir_graph_workspace(n, m)
+        self.ws = dv.workspace(self.nbytes)
+        self.graph = ctypes.c_void_p(0)
+        st = stream if stream is not None else torch.cuda.current_stream()
+        if st.cuda_stream == 0:
+            raise ValueError("IrGraph needs a non-default stream")
+        check(L.flg_gmres_ir_graph_create(n, dv.ptr(K), K.stride(0), dv.ptr(A32), ld32, dv.ptr(K32), ld32, dv.ptr(dinv),
+                                          dv.ptr(b), dv.ptr(x), float(rtol), int(m), int(max_outer), dv.ptr(self.ws),
+                                          self.nbytes, ctypes.c_void_p(st.cuda_stream), ctypes.byref(self.graph)),
+              "GMRES-IR graph")
+        self._keep = (K, A32, K32, dinv, b, x)
+
+    def launch(self, stream):
+        check(load().flg_graph_launch(self.graph, ctypes.c_void_p(stream.cuda_stream)), "GMRES-IR graph replay")
+
+    def result(self, stream):
+        """(status, inner iterations, refinement steps, final FP64 residual) of the last replay."""
+        it, outer, resid = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_double(0.0)
+        st = load().flg_gmres_ir_graph_result(dv.ptr(self.ws), ctypes.byref(it), ctypes.byref(outer),
+                                              ctypes.byref(resid), ctypes.c_void_p(stream.cuda_stream))
+        return st, it.value, outer.value, resid.value
+
+    def close(self):
+        if self.graph:
+            load().flg_graph_destroy(self.graph)
+            self.graph = ctypes.c_void_p(0)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001 - interpreter shutdown
+            pass
+
+
 def _mixed_lu_solve_dev(K: torch.Tensor, U: torch.Tensor, rtol, restart, maxiter, lu_name, required=None):
     """TF32/BF16 tensor-core LU of K (no pivoting) + FP64 GMRES iterative refinement."""
     K32, ld32, dinv, A32 = _lowp_factor_dev(K, lu_name)

@@ -30,6 +30,12 @@ static ProfSlot g_slots[FLG_NUM_SLOTS];
 
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
+// while a graph body is being captured on this thread, no timing events are recorded
+// (event nodes are not allowed inside conditional graph bodies)
+static thread_local int g_prof_suppressed = 0;
+ProfSuppress::ProfSuppress() { g_prof_suppressed++; }
+ProfSuppress::~ProfSuppress() { g_prof_suppressed--; }
+
 static void prof_reset_locked() {
     for (auto &s : g_slots) {
         for (auto e : s.begin) cudaEventDestroy(e);
@@ -41,7 +47,7 @@ static void prof_reset_locked() {
 }
 
 void prof_begin(int slot, cudaStream_t st) {
-    if (!g_prof_on.load(std::memory_order_relaxed)) return;
+    if (!g_prof_on.load(std::memory_order_relaxed) || g_prof_suppressed) return;
     std::lock_guard<std::mutex> lk(g_prof_mu);
     cudaEvent_t e;
     if (cudaEventCreate(&e) != cudaSuccess) return;
@@ -50,7 +56,7 @@ void prof_begin(int slot, cudaStream_t st) {
 }
 
 void prof_end(int slot, cudaStream_t st) {
-    if (!g_prof_on.load(std::memory_order_relaxed)) return;
+    if (!g_prof_on.load(std::memory_order_relaxed) || g_prof_suppressed) return;
     std::lock_guard<std::mutex> lk(g_prof_mu);
     cudaEvent_t e;
     if (cudaEventCreate(&e) != cudaSuccess) return;

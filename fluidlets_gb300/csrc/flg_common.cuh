@@ -45,6 +45,11 @@ void count_launch();
 // CUDA-event timing of profiled kernels (flg_profile_enable)
 void prof_begin(int slot, cudaStream_t st);
 void prof_end(int slot, cudaStream_t st);
+// scope in which this thread's launches record no timing events (graph capture)
+struct ProfSuppress {
+    ProfSuppress();
+    ~ProfSuppress();
+};
 
 #define FLG_TRY(call)            \
     do {                         \

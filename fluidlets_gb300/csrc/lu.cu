@@ -1298,6 +1298,16 @@ size_t lu_solve_lowp_bytes(int64_t n) {
     return c.bytes();
 }
 
+// the kernel attributes of the solve, set once (before any graph capture that includes it)
+int lu_solve_lowp_prepare() {
+    static bool attr_set = false;
+    if (!attr_set) {
+        FLG_CUDA(cudaFuncSetAttribute(lowp_apply_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kApplySmem));
+        attr_set = true;
+    }
+    return FLG_OK;
+}
+
 int lu_solve_lowp_apply(int64_t n, const float *LU, int64_t ld, const float *dinv, const double *b, double *x,
                         void *work, size_t work_bytes, cudaStream_t st) {
     FLG_REQUIRE(ld % 4 == 0 && ((uintptr_t)LU & 15) == 0, "LU rows must be 16-byte aligned (ld % 4 == 0)");
@@ -1323,11 +1333,7 @@ int lu_solve_lowp_apply(int64_t n, const float *LU, int64_t ld, const float *din
     FLG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
     ApplyArgs aa{n, q, bf, y, z, err};
     void *args[] = {&mLU, &mD, &aa};
-    static bool attr_set = false;
-    if (!attr_set) {
-        FLG_CUDA(cudaFuncSetAttribute(lowp_apply_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kApplySmem));
-        attr_set = true;
-    }
+    FLG_TRY(lu_solve_lowp_prepare());
     prof_begin(FLG_SLOT_LU_SOLVE, st);
     FLG_CUDA(cudaLaunchCooperativeKernel((void *)lowp_apply_kernel, dim3(G), dim3(kApplyThreads), args, kApplySmem,
                                          st));

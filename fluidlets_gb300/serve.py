@@ -124,6 +124,8 @@ class BucketPlan:
         self.b = torch.zeros(n, dtype=torch.float64, device=dev)
         self.x = torch.zeros(n, dtype=torch.float64, device=dev)
         self.graph = None
+        self.ir = None
+        self.rtol_ir = 1e-12  # the refinement's target: rtol / 100 for the server's rtol 1e-10
         self.stream = stream
         self.mode = mode
 
@@ -156,11 +158,23 @@ class BucketPlan:
                                        self.lu_bytes, ctypes.c_void_p(self.stream.cuda_stream), ctypes.byref(h))
         if st == 0 and h.value:
             self.graph = h.value
+            # the refinement as a second graph over the same buffers (conditional loops steered
+            # on the device): a request then costs one host synchronization, at the end
+            from .core import IrGraph
+
+            try:
+                self.ir = IrGraph(self.K, self.A32, self.K32, self.ld32, self.dinv, self.b, self.x,
+                                  self.rtol_ir, stream=self.stream)
+            except (RuntimeError, ValueError) as e:
+                self.ir = None
+                self.capture_error = str(e)
         else:
             self.graph = None
             self.capture_error = L.flg_last_error().decode(errors="replace")
 
     def __del__(self):
+        if getattr(self, "ir", None) is not None:
+            self.ir.close()
         if getattr(self, "graph", None):
             try:
                 load().flg_graph_destroy(ctypes.c_void_p(self.graph))
@@ -179,6 +193,8 @@ class BucketPlan:
             self._run()
 
     def solve(self, U: torch.Tensor, rtol: float, restart: int = 60, maxiter: int = 200):
+        if getattr(self, "ir", None) is not None and rtol * 1e-2 == self.rtol_ir:
+            return self._solve_graph(U, rtol)
         L = load()
         N = U.shape[0]
         self.b.zero_()
@@ -201,6 +217,24 @@ class BucketPlan:
                                   ctypes.c_void_p(self.stream.cuda_stream))
         _accept(st, resid.value, rtol, "GMRES-IR")
         return self.x[:3 * N].reshape(N, 3).clone(), iters.value, outer.value, resid.value
+
+
+    def _solve_graph(self, U: torch.Tensor, rtol: float):
+        """The captured refinement: one replay, then the LU's flags and the refinement's outcome."""
+        from .core import _accept
+
+        N = U.shape[0]
+        self.b.zero_()
+        self.b[:3 * N].copy_(U.reshape(-1))
+        self.ir.launch(self.stream)
+        st, it, outer, resid = self.ir.result(self.stream)
+        flags = self.flags.cpu()
+        if int(flags[1]):
+            raise RuntimeError("low-precision LU: a bounded device wait timed out")
+        if int(flags[0]):
+            raise np.linalg.LinAlgError(f"zero pivot at row {int(flags[0]) - 1} in the low-precision LU")
+        _accept(st, resid, rtol, "GMRES-IR")
+        return self.x[:3 * N].reshape(N, 3).clone(), it, outer, resid
 
 
 class SolveServer:
@@ -388,6 +422,7 @@ class SolveServer:
                 self.stats["plans_built"] += 1
             if self.graphs:
                 plan.stream = stream
+                plan.rtol_ir = self.rtol * 1e-2
                 plan.capture()
                 with self._cv:
                     self.stats["captures"] += 1

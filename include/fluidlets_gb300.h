@@ -368,6 +368,26 @@ int flg_convert_f64_f32(int64_t n_rows, int64_t n_cols, const double *src, int64
 int flg_convert_f64_f32x2(int64_t n_rows, int64_t n_cols, const double *src, int64_t lds, float *dst1, float *dst2,
                           int64_t ldd, void *stream);
 
+/* FP64 GMRES-based iterative refinement of K x = b (the same algorithm as
+ * flg_gmres_ir_dense, with one restart cycle of at most m inner columns per
+ * refinement step) as one instantiated CUDA graph over fixed buffers: the
+ * refinement and inner loops are conditional WHILE nodes whose conditions
+ * single-thread control kernels set on the device, and every scalar (norms,
+ * Hessenberg matrix, rotations) stays in device memory, so a replay
+ * (flg_graph_launch) costs no host round trip.  Tolerance rtol on
+ * ||b - K x|| / ||b|| with the FP64 K; at most max_outer refinement steps;
+ * m <= 64.  The workspace (flg_gmres_ir_graph_workspace) belongs to the graph;
+ * flg_gmres_ir_graph_result reads the last replay's outcome from it
+ * (synchronizes): FLG_OK, or FLG_ERR_NOT_CONVERGED on stagnation or the step
+ * limit.  The creating stream must be a non-default stream.  No counterpart in
+ * the reference (its solves run on the host, core/solve.py:64-79). */
+size_t flg_gmres_ir_graph_workspace(int64_t n, int m);
+int flg_gmres_ir_graph_create(int64_t n, const double *K, int64_t ld, const float *A32, int64_t lda32,
+                              const float *LU32, int64_t ld32, const float *dinv, const double *b, double *x,
+                              double rtol, int m, int max_outer, void *work, size_t work_bytes, void *stream,
+                              void **graph_exec);
+int flg_gmres_ir_graph_result(const void *work, int *iters, int *outer, double *resid, void *stream);
+
 /* ---- measurement ----------------------------------------------------------
  * Throughput microbenchmarks used as roofline denominators (FFMA FP32, DFMA
  * FP64), in TFLOP/s, timed with CUDA events on `stream`.  Synchronizes. */
