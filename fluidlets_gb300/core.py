@@ -15,6 +15,7 @@ TF32/BF16 tensor-core LU + FP64 GMRES iterative refinement for solves).
 from __future__ import annotations
 
 import ctypes
+import threading
 from dataclasses import dataclass
 
 import numpy as np
@@ -381,6 +382,72 @@ class IrGraph:
             pass
 
 
+class _DensePlan:
+    """Device buffers of a mixed-precision dense solve of one size n (K, its two FP32 copies, the
+    diagonal-block inverses, the LU workspace, b, x) and the refinement captured over them as an
+    IrGraph.  resistance() keeps the last one per host thread, so repeated solves of one size
+    reuse both the buffers and the graph (release_plans() frees them)."""
+
+    def __init__(self, n, dev, rtol_ir, m):
+        L = load()
+        self.n, self.dev, self.rtol_ir, self.m = n, dev, rtol_ir, m
+        self.ld32 = (n + 31) // 32 * 32
+        self.K = torch.empty((n, n), dtype=torch.float64, device=dev)
+        self.K32 = torch.empty((n, self.ld32), dtype=torch.float32, device=dev)
+        self.A32 = torch.empty_like(self.K32)
+        self.dinv = torch.empty(L.flg_lu_lowp_dinv_elems(n), dtype=torch.float32, device=dev)
+        self.lu_bytes = max(L.flg_lu_factor_lowp_workspace(n, lu_mode(x)) for x in ("tf32", "bf16", "fp32"))
+        self.lu_ws = dv.workspace(self.lu_bytes)
+        self.b = torch.zeros(n, dtype=torch.float64, device=dev)
+        self.x = torch.zeros(n, dtype=torch.float64, device=dev)
+        self.stream = torch.cuda.Stream(device=dev)  # graph capture needs a non-default stream
+        torch.cuda.current_stream(dev).synchronize()
+        self.ir = IrGraph(self.K, self.A32, self.K32, self.ld32, self.dinv, self.b, self.x, rtol_ir, m=m,
+                          stream=self.stream)
+        self.stream.synchronize()
+
+    def close(self):
+        self.ir.close()
+
+
+_plans = threading.local()
+
+
+def release_plans():
+    """Free the device buffers that resistance() keeps for repeated mixed-precision solves."""
+    p = getattr(_plans, "plan", None)
+    if p is not None:
+        p.close()
+        _plans.plan = None
+
+
+def _dense_plan(n, dev, rtol_ir, m):
+    p = getattr(_plans, "plan", None)
+    if p is None or (p.n, p.dev, p.rtol_ir, p.m) != (n, dev, rtol_ir, m):
+        release_plans()
+        p = _plans.plan = _DensePlan(n, dev, rtol_ir, m)
+    return p
+
+
+def _mixed_lu_planned(kernel, X, e, mu, eps, U, rtol_ir, restart, lu_name, required):
+    """The mixed dense solve on the cached plan of its size: assembly into the plan's K, the two
+    FP32 copies, the tensor-core LU, then one replay of the captured refinement."""
+    L = load()
+    n = 3 * X.shape[0]
+    p = _dense_plan(n, X.device, rtol_ir, min(restart, 64))
+    _assemble_dev(kernel, X, X, e, mu, out=p.K, ld=n, sym_eps=_uniform_eps(eps), reciprocal=True)
+    check(L.flg_convert_f64_f32x2(n, n, dv.ptr(p.K), n, dv.ptr(p.K32), dv.ptr(p.A32), p.ld32, dv.stream()), "convert")
+    info = ctypes.c_int(0)
+    check(L.flg_lu_factor_lowp(n, dv.ptr(p.K32), p.ld32, lu_mode(lu_name), dv.ptr(p.dinv), ctypes.byref(info),
+                               dv.ptr(p.lu_ws), p.lu_bytes, dv.stream()), "low-precision LU")
+    p.b.copy_(U.reshape(-1))
+    cur = torch.cuda.current_stream(X.device)
+    p.ir.launch(cur)
+    st, iters, outer, resid = p.ir.result(cur)
+    _accept(st, resid, required, "GMRES-IR")
+    return p.x.clone(), iters, outer, resid
+
+
 def _mixed_lu_solve_dev(K: torch.Tensor, U: torch.Tensor, rtol, restart, maxiter, lu_name, required=None):
     """TF32/BF16 tensor-core LU of K (no pivoting) + FP64 GMRES iterative refinement."""
     K32, ld32, dinv, A32 = _lowp_factor_dev(K, lu_name)
@@ -441,7 +508,10 @@ def resistance(kernel, points, velocities, eps, mu=1.0, method="auto", rtol=1e-1
     # not only the residual, is within rtol (error <= condition number x residual)
     rtol_ir = rtol * 1e-2 if prec == PREC["mixed"] else rtol
     resid = None
-    if method == "lu":
+    if method == "lu" and prec == PREC["mixed"] and not kc and not mu_c and not Uc and restart <= 64:
+        # real mixed dense solve: the cached plan of this size and its captured refinement
+        f, iterations, ir_steps, resid = _mixed_lu_planned(kernel, X, e, mu, eps, U, rtol_ir, restart, lu, rtol)
+    elif method == "lu":
         K = _assemble_dev(kernel, X, X, e, mu, sym_eps=_uniform_eps(eps), reciprocal=prec == PREC["mixed"])
         if prec == PREC["mixed"] and not K.is_complex() and not Uc:
             # the refinement's last residual is ||U - K f|| / ||U|| with the FP64 K: reported as is
