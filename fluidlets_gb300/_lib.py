@@ -76,6 +76,8 @@ SIGNATURES = {
     "flg_gmres_ir_graph_create": (c_int, [c_int64, _P, c_int64, _P, c_int64, _P, c_int64, _P, _P, _P, c_double, c_int,
                                           c_int, _P, c_size_t, _P, POINTER(c_void_p)]),
     "flg_gmres_ir_graph_result": (c_int, [_P, POINTER(c_int), POINTER(c_int), POINTER(c_double), _P]),
+    "flg_lowp_factor_graph_create": (c_int, [c_int64, _P, c_int64, _P, _P, c_int64, c_int, _P, _P, _P, c_size_t, _P,
+                                             POINTER(c_void_p)]),
     "flg_graph_launch": (c_int, [_P, _P]),
     "flg_graph_destroy": (c_int, [_P]),
     "flg_assemble_nearest_async": (c_int, [c_int, c_double, c_double, _P, c_int64, _P, _P, _P, c_int64, c_int64,

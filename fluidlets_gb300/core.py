@@ -22,7 +22,7 @@ import numpy as np
 import torch
 
 from . import _device as dv
-from ._lib import BF16, C128, F32, F64, FLG_ERR_NOT_CONVERGED, KIND, PREC, check, load, lu_mode
+from ._lib import BF16, C128, F32, F64, FLG_ERR_NOT_CONVERGED, KIND, PREC, LinAlgError, check, load, lu_mode
 from .kernels import kernel_params
 
 #: above this many unknowns, method="auto" switches from dense LU to GMRES (core/solve.py:20)
@@ -400,14 +400,35 @@ class _DensePlan:
         self.lu_ws = dv.workspace(self.lu_bytes)
         self.b = torch.zeros(n, dtype=torch.float64, device=dev)
         self.x = torch.zeros(n, dtype=torch.float64, device=dev)
+        self.flags = torch.zeros(2, dtype=torch.int32, device=dev)
+        self.factor_graphs = {}  # LU mode -> captured FP32 copies + tensor-core LU
         self.stream = torch.cuda.Stream(device=dev)  # graph capture needs a non-default stream
         torch.cuda.current_stream(dev).synchronize()
         self.ir = IrGraph(self.K, self.A32, self.K32, self.ld32, self.dinv, self.b, self.x, rtol_ir, m=m,
                           stream=self.stream)
         self.stream.synchronize()
 
+    def factor_graph(self, mode):
+        """The captured copies + LU for one LU mode (made on first use, on the plan's stream)."""
+        g = self.factor_graphs.get(mode)
+        if g is None:
+            L = load()
+            torch.cuda.current_stream(self.dev).synchronize()
+            h = ctypes.c_void_p(0)
+            check(L.flg_lowp_factor_graph_create(self.n, dv.ptr(self.K), self.n, dv.ptr(self.K32), dv.ptr(self.A32),
+                                                 self.ld32, mode, dv.ptr(self.dinv), dv.ptr(self.flags),
+                                                 dv.ptr(self.lu_ws), self.lu_bytes,
+                                                 ctypes.c_void_p(self.stream.cuda_stream), ctypes.byref(h)),
+                  "factor graph")
+            self.stream.synchronize()
+            g = self.factor_graphs[mode] = h
+        return g
+
     def close(self):
         self.ir.close()
+        for g in self.factor_graphs.values():
+            load().flg_graph_destroy(g)
+        self.factor_graphs = {}
 
 
 _plans = threading.local()
@@ -435,15 +456,18 @@ def _mixed_lu_planned(kernel, X, e, mu, eps, U, rtol_ir, restart, lu_name, requi
     L = load()
     n = 3 * X.shape[0]
     p = _dense_plan(n, X.device, rtol_ir, min(restart, 64))
-    _assemble_dev(kernel, X, X, e, mu, out=p.K, ld=n, sym_eps=_uniform_eps(eps), reciprocal=True)
-    check(L.flg_convert_f64_f32x2(n, n, dv.ptr(p.K), n, dv.ptr(p.K32), dv.ptr(p.A32), p.ld32, dv.stream()), "convert")
-    info = ctypes.c_int(0)
-    check(L.flg_lu_factor_lowp(n, dv.ptr(p.K32), p.ld32, lu_mode(lu_name), dv.ptr(p.dinv), ctypes.byref(info),
-                               dv.ptr(p.lu_ws), p.lu_bytes, dv.stream()), "low-precision LU")
-    p.b.copy_(U.reshape(-1))
+    fg = p.factor_graph(lu_mode(lu_name))
     cur = torch.cuda.current_stream(X.device)
+    _assemble_dev(kernel, X, X, e, mu, out=p.K, ld=n, sym_eps=_uniform_eps(eps), reciprocal=True)
+    check(L.flg_graph_launch(fg, ctypes.c_void_p(cur.cuda_stream)), "factor graph replay")
+    p.b.copy_(U.reshape(-1))
     p.ir.launch(cur)
-    st, iters, outer, resid = p.ir.result(cur)
+    st, iters, outer, resid = p.ir.result(cur)  # synchronizes
+    flags = p.flags.cpu()
+    if int(flags[1]):
+        raise RuntimeError("low-precision LU: a bounded device wait timed out")
+    if int(flags[0]):
+        raise LinAlgError(f"zero or non-finite pivot at row {int(flags[0]) - 1} in the low-precision LU")
     _accept(st, resid, required, "GMRES-IR")
     return p.x.clone(), iters, outer, resid
 

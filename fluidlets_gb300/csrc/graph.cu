@@ -9,6 +9,9 @@
 // point count is read from device memory by the assembly kernel, so one graph
 // serves every problem size of its bucket.
 //
+// flg_lowp_factor_graph_create captures the FP32 copies and the tensor-core LU of
+// an already assembled K (resistance(), which assembles eagerly).
+//
 // flg_swimmer_graph_create does the same for the free-swimmer system of one
 // shape size (force and quadrature point counts), for the stages of swim():
 //   flg_nearest_neighbors -> flg_assemble_nearest_async ->
@@ -58,6 +61,17 @@ extern "C" int flg_bucket_graph_create(int kind, double alpha_re, double alpha_i
         FLG_TRY(flg_assemble_bucket(kind, alpha_re, alpha_im, points, eps, n_real, n_cap, mu_re, K, FLG_F64, n,
                                     stream));
         FLG_TRY(flg_convert_f64_f32x2(n, n, K, n, K32, A32, ld32, stream));
+        return flg_lu_factor_lowp_async(n, K32, ld32, mode, dinv, flags, work, work_bytes, stream);
+    };
+    return capture_graph(stream, seq, graph_exec);
+}
+
+extern "C" int flg_lowp_factor_graph_create(int64_t n, const double *K, int64_t ld, float *K32, float *A32,
+                                            int64_t ld32, int mode, float *dinv, int *flags, void *work,
+                                            size_t work_bytes, void *stream, void **graph_exec) {
+    FLG_REQUIRE(n >= 1 && ld >= n && ld32 >= n && K && K32 && dinv && flags, "bad factor graph arguments");
+    auto seq = [&]() -> int {
+        FLG_TRY(flg_convert_f64_f32x2(n, n, K, ld, K32, A32, ld32, stream));
         return flg_lu_factor_lowp_async(n, K32, ld32, mode, dinv, flags, work, work_bytes, stream);
     };
     return capture_graph(stream, seq, graph_exec);

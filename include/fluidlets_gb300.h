@@ -306,6 +306,13 @@ int flg_bucket_graph_create(int kind, double alpha_re, double alpha_im, const do
                             const int64_t *n_real, int64_t n_cap, double mu_re, double *K, float *A32, float *K32,
                             int64_t ld32, int mode, float *dinv, int *flags, void *work, size_t work_bytes,
                             void *stream, void **graph_exec);
+/* The FP32 copies (flg_convert_f64_f32x2) and the tensor-core LU
+ * (flg_lu_factor_lowp_async) of an assembled FP64 K as one captured graph over
+ * fixed buffers (replay with flg_graph_launch; flags as in
+ * flg_lu_factor_lowp_async).  No counterpart in the reference. */
+int flg_lowp_factor_graph_create(int64_t n, const double *K, int64_t ld, float *K32, float *A32, int64_t ld32,
+                                 int mode, float *dinv, int *flags, void *work, size_t work_bytes, void *stream,
+                                 void **graph_exec);
 /* Captured graph of the free-swimmer system (swimming.py:66-102) for N force
  * points and Q quadrature points, over fixed device buffers: x (N x 3), x0 (3),
  * X (Q x 3), eps (Q), nearest (Q; recomputed from x and X on every replay when
