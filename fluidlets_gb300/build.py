@@ -69,7 +69,7 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
     with cf.ThreadPoolExecutor(jobs) as ex:
         list(ex.map(lambda so: _compile(so[0], so[1], verbose), zip(srcs, objs)))
     tmp = OUT_DIR / f"{LIB_NAME}.{os.getpid()}"
-    cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart"]
+    cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart", "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

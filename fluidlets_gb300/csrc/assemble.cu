@@ -558,6 +558,7 @@ using namespace flg;
 extern "C" int flg_assemble(int kind, double alpha_re, double alpha_im, const double *targets, int64_t M,
                             const double *sources, const double *eps, int64_t N, double mu_re, double mu_im,
                             void *out, int out_type, int64_t ld, void *stream) {
+    FLG_RANGE("flg_assemble");
     AsmArgs a{};
     FLG_TRY(prepare(kind, alpha_re, alpha_im, mu_re, mu_im, out_type, a));
     FLG_REQUIRE(M >= 0 && N >= 0, "negative sizes");
@@ -582,6 +583,7 @@ extern "C" int flg_assemble(int kind, double alpha_re, double alpha_im, const do
 extern "C" int flg_assemble_self_uniform(int kind, double alpha_re, double alpha_im, const double *points, int64_t N,
                                          double eps, double mu_re, double mu_im, void *out, int out_type, int64_t ld,
                                          void *stream) {
+    FLG_RANGE("flg_assemble_self_uniform");
     AsmArgs a{};
     FLG_TRY(prepare(kind, alpha_re, alpha_im, mu_re, mu_im, out_type, a));
     FLG_REQUIRE(N >= 0, "negative size");
@@ -611,6 +613,7 @@ extern "C" int flg_assemble_self_uniform(int kind, double alpha_re, double alpha
 extern "C" int flg_assemble_bucket(int kind, double alpha_re, double alpha_im, const double *points, const double *eps,
                                    const int64_t *n_real, int64_t n_cap, double mu_re, void *out, int out_type,
                                    int64_t ld, void *stream) {
+    FLG_RANGE("flg_assemble_bucket");
     AsmArgs a{};
     FLG_TRY(prepare(kind, alpha_re, alpha_im, mu_re, 0.0, out_type, a));
     FLG_REQUIRE(!(kind == FLG_BRINKMANLET && alpha_im != 0.0), "bucket assembly is real only");
@@ -707,6 +710,7 @@ extern "C" int flg_assemble_nearest(int kind, double alpha_re, double alpha_im, 
                                     const double *quad, const int64_t *nearest, const double *eps, int64_t Q,
                                     int64_t n_force, double mu_re, double mu_im, void *out, int out_type, int64_t ld,
                                     void *work, size_t work_bytes, void *stream) {
+    FLG_RANGE("flg_assemble_nearest");
     return assemble_nearest_impl(kind, alpha_re, alpha_im, targets, M, quad, nearest, eps, Q, n_force, mu_re, mu_im,
                                  out, out_type, ld, work, work_bytes, stream, nullptr);
 }
@@ -724,6 +728,7 @@ extern "C" int flg_assemble_nearest_async(int kind, double alpha_re, double alph
 extern "C" int flg_swimmer_constraints(const double *x, int64_t N, const double *x0_host, const double *X,
                                        const int64_t *nearest, int64_t Q, void *A, int out_type, int64_t ld,
                                        void *stream) {
+    FLG_RANGE("flg_swimmer_constraints");
     FLG_REQUIRE(N >= 0 && Q >= 0, "negative sizes");
     FLG_REQUIRE(out_type == FLG_F64 || out_type == FLG_F32, "swimmer system is FLG_F64 or FLG_F32");
     FLG_REQUIRE(ld >= 3 * N + 6, "ld < 3N + 6");
@@ -829,6 +834,7 @@ __global__ void __launch_bounds__(256) nearest_kernel(const double *quad, int64_
 
 extern "C" int flg_nearest_neighbors(const double *quad, int64_t Q, const double *force, int64_t N, int64_t *out,
                                      void *stream) {
+    FLG_RANGE("flg_nearest_neighbors");
     FLG_REQUIRE(Q >= 0 && N >= 0, "negative sizes");
     if (Q == 0) return FLG_OK;
     FLG_REQUIRE(N > 0, "no force points to search");

@@ -1,6 +1,7 @@
 // flg_common.cuh -- shared definitions of libfluidlets_gb300 (sm_103a).
 #pragma once
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 #include <stdio.h>
 #include <string.h>
@@ -95,6 +96,14 @@ struct CountingArena {
 };
 
 inline cudaStream_t as_stream(void *s) { return (cudaStream_t)s; }
+
+// NVTX range around a C-ABI entry point (a profiler shows the library's calls on the host
+// timeline; without a tool attached a push/pop costs a few nanoseconds)
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+};
+#define FLG_RANGE(name) ::flg::NvtxRange flg_nvtx_range_(name)
 
 __host__ __device__ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 

@@ -56,6 +56,7 @@ extern "C" int flg_bucket_graph_create(int kind, double alpha_re, double alpha_i
                                        const double *eps, const int64_t *n_real, int64_t n_cap, double mu_re,
                                        double *K, float *A32, float *K32, int64_t ld32, int mode, float *dinv,
                                        int *flags, void *work, size_t work_bytes, void *stream, void **graph_exec) {
+    FLG_RANGE("flg_bucket_graph_create");
     const int64_t n = 3 * n_cap;
     auto seq = [&]() -> int {
         FLG_TRY(flg_assemble_bucket(kind, alpha_re, alpha_im, points, eps, n_real, n_cap, mu_re, K, FLG_F64, n,
@@ -69,6 +70,7 @@ extern "C" int flg_bucket_graph_create(int kind, double alpha_re, double alpha_i
 extern "C" int flg_lowp_factor_graph_create(int64_t n, const double *K, int64_t ld, float *K32, float *A32,
                                             int64_t ld32, int mode, float *dinv, int *flags, void *work,
                                             size_t work_bytes, void *stream, void **graph_exec) {
+    FLG_RANGE("flg_lowp_factor_graph_create");
     FLG_REQUIRE(n >= 1 && ld >= n && ld32 >= n && K && K32 && dinv && flags, "bad factor graph arguments");
     auto seq = [&]() -> int {
         FLG_TRY(flg_convert_f64_f32x2(n, n, K, ld, K32, A32, ld32, stream));
@@ -86,6 +88,7 @@ extern "C" int flg_swimmer_graph_create(int kind, double alpha_re, double alpha_
                                         int64_t *nearest, int recompute_nearest, double mu_re, double *A, float *A32,
                                         float *K32, int64_t ld32, int mode, float *dinv, int *flags, void *work,
                                         size_t work_bytes, void *stream, void **graph_exec) {
+    FLG_RANGE("flg_swimmer_graph_create");
     FLG_REQUIRE(N > 0 && Q >= 0 && flags && A && K32 && dinv, "bad swimmer graph arguments");
     const int64_t n = 3 * N + 6;
     FLG_REQUIRE(work_bytes >= flg_swimmer_graph_workspace(N, Q, mode), "workspace too small for the swimmer graph");
@@ -102,6 +105,7 @@ extern "C" int flg_swimmer_graph_create(int kind, double alpha_re, double alpha_
 }
 
 extern "C" int flg_graph_launch(void *graph_exec, void *stream) {
+    FLG_RANGE("flg_graph_launch");
     FLG_REQUIRE(graph_exec, "null graph");
     FLG_CUDA(cudaGraphLaunch((cudaGraphExec_t)graph_exec, flg::as_stream(stream)));
     return FLG_OK;

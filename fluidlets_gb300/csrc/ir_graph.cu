@@ -313,6 +313,7 @@ extern "C" int flg_gmres_ir_graph_create(int64_t n, const double *K, int64_t ld,
                                          const float *LU32, int64_t ld32, const float *dinv, const double *b,
                                          double *x, double rtol, int m, int max_outer, void *work,
                                          size_t work_bytes, void *stream, void **graph_exec) {
+    FLG_RANGE("flg_gmres_ir_graph_create");
     FLG_REQUIRE(graph_exec, "null graph handle");
     *graph_exec = nullptr;
     FLG_REQUIRE(n >= 1 && ld >= n && lda32 >= n && ld32 >= n, "bad GMRES-IR graph sizes");

@@ -595,6 +595,7 @@ extern "C" int flg_gmres(int kind, double alpha_re, double alpha_im, const doubl
                          double mu_re, double mu_im, const double *b, double *x, int is_complex, double rtol,
                          int restart, int maxiter, int precision, double inner_rtol, int *iters, int *outer,
                          double *resid, void *work, size_t work_bytes, void *stream) {
+    FLG_RANGE("flg_gmres");
     FLG_TRY(check_kernel_args(kind, alpha_re, alpha_im));
     FLG_REQUIRE(N >= 0 && restart >= 1 && maxiter >= 1, "bad GMRES sizes");
     FLG_REQUIRE(rtol >= 0.0 && inner_rtol > 0.0, "tolerances must be non-negative");
@@ -631,6 +632,7 @@ extern "C" size_t flg_gmres_ir_dense_workspace(int64_t n, int restart) {
 extern "C" int flg_gmres_ir_dense(int64_t n, const double *A, int64_t ld, const float *A32, int64_t lda32,
                                   const float *LU32, int64_t ld32, const float *dinv, const double *b, double *x, double rtol, int restart, int maxiter, int *iters,
                                   int *outer, double *resid, void *work, size_t work_bytes, void *stream) {
+    FLG_RANGE("flg_gmres_ir_dense");
     FLG_REQUIRE(n >= 0 && ld >= n && ld32 >= n && restart >= 1 && maxiter >= 1, "bad GMRES-IR arguments");
     FLG_REQUIRE(iters && outer && resid, "null output pointer");
     *iters = 0;

@@ -1397,6 +1397,7 @@ static int f64_streams(F64Streams **out) {
 
 extern "C" int flg_lu_factor_f64(int64_t n, double *A, int64_t ld, int32_t *ipiv, int *info, void *work,
                                  size_t work_bytes, void *stream) {
+    FLG_RANGE("flg_lu_factor_f64");
     FLG_REQUIRE(n >= 0 && ld >= n && info, "bad LU arguments");
     *info = 0;
     if (n == 0) return FLG_OK;
@@ -1506,6 +1507,7 @@ extern "C" int flg_lu_factor_f64(int64_t n, double *A, int64_t ld, int32_t *ipiv
 
 extern "C" int flg_lu_solve_f64(int64_t n, int64_t nrhs, const double *LU, int64_t ld, const int32_t *ipiv, double *B,
                                 int64_t ldb, void *stream) {
+    FLG_RANGE("flg_lu_solve_f64");
     FLG_REQUIRE(n >= 0 && nrhs >= 0 && ld >= n && ldb >= nrhs, "bad LU solve arguments");
     if (n == 0 || nrhs == 0) return FLG_OK;
     cudaStream_t st = as_stream(stream);
@@ -1618,6 +1620,7 @@ extern "C" size_t flg_lu_factor_lowp_workspace(int64_t n, int mode) {
 
 extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mode, float *dinv, int *flags, void *work,
                                         size_t work_bytes, void *stream) {
+    FLG_RANGE("flg_lu_factor_lowp_async");
     FLG_REQUIRE(n >= 0 && ld >= n && flags, "bad LU arguments");
     const int tbits = mode & (FLG_LU_TILE_N128 | FLG_LU_TILE_N256);
     FLG_REQUIRE(tbits != (FLG_LU_TILE_N128 | FLG_LU_TILE_N256), "two tile widths in LU mode %d", mode);
@@ -1805,6 +1808,7 @@ extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mod
 
 extern "C" int flg_lu_factor_lowp(int64_t n, float *A, int64_t ld, int mode, float *dinv, int *info, void *work,
                                   size_t work_bytes, void *stream) {
+    FLG_RANGE("flg_lu_factor_lowp");
     FLG_REQUIRE(info, "null info");
     *info = 0;
     FLG_REQUIRE(n >= 0 && ld >= n, "bad LU arguments");
@@ -1834,6 +1838,7 @@ extern "C" size_t flg_lu_solve_lowp_workspace(int64_t n) { return lu_solve_lowp_
 
 extern "C" int flg_lu_solve_lowp(int64_t n, const float *LU, int64_t ld, const float *dinv, const double *b, double *x,
                                  void *work, size_t work_bytes, void *stream) {
+    FLG_RANGE("flg_lu_solve_lowp");
     FLG_REQUIRE(n >= 0 && ld >= n, "bad solve arguments");
     if (n == 0) return FLG_OK;
     return lu_solve_lowp_apply(n, LU, ld, dinv, b, x, work, work_bytes, as_stream(stream));

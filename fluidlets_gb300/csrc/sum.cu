@@ -942,6 +942,7 @@ extern "C" int flg_evaluate(int kind, double alpha_re, double alpha_im, const do
                             const double *sources, const double *eps, int64_t N, const double *strengths,
                             int strengths_complex, double mu_re, double mu_im, double *out, int precision,
                             void *work, size_t work_bytes, void *stream) {
+    FLG_RANGE("flg_evaluate");
     FLG_TRY(check_kernel_args(kind, alpha_re, alpha_im));
     FLG_REQUIRE(M >= 0 && N >= 0, "negative sizes M=%lld N=%lld", (long long)M, (long long)N);
     FLG_REQUIRE(precision == FLG_PREC_FP64 || precision == FLG_PREC_MIXED, "unknown precision %d", precision);

@@ -462,6 +462,7 @@ extern "C" size_t flg_tc_rank_update_workspace(int64_t m, int64_t nc, int mode) 
 
 extern "C" int flg_tc_rank_update(float *C, int64_t ldc, const float *A, int64_t lda, const float *Bt, int64_t ldb,
                                   int64_t m, int64_t nc, int mode, void *work, size_t work_bytes, void *stream) {
+    FLG_RANGE("flg_tc_rank_update");
     FLG_REQUIRE(ldb == 128, "Bt must be compact (ldb == 128)");
     FLG_REQUIRE(lda >= 128 && ldc >= nc, "bad leading dimensions");
     return flg::tc_update(C, ldc, A, lda, Bt, 128, m, nc, 128, mode, work, work_bytes, flg::as_stream(stream), nullptr,
