@@ -310,8 +310,13 @@ def wall_lu_section(dev, n_points=8192, h=1.05, reps=3):
         from fluidlets_gb300 import _lib
 
         L = _lib.load()
+        # one solve through the eager kernels (the graph replays of resistance() record no events)
+        from fluidlets_gb300.core import _assemble_dev, _mixed_lu_solve_dev
+
+        K = _assemble_dev(k, X, X, e, 1.0, sym_eps=eps, reciprocal=True)
         L.flg_profile_enable(1)
-        fl.resistance(k, X, U, e, method="lu", precision="mixed", lu=lu)
+        _mixed_lu_solve_dev(K, U.reshape(-1), 1e-12, 60, 200, lu, required=1e-10)
+        del K
         import ctypes
 
         upd_ms, upd_n = ctypes.c_double(0), ctypes.c_int64(0)

@@ -32,7 +32,11 @@ static int capture_graph(void *stream, F &&seq, void **graph_exec) {
     FLG_TRY(seq());
     FLG_CUDA(cudaStreamSynchronize(st));
     FLG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    int s = seq();
+    int s;
+    {
+        flg::ProfSuppress quiet;  // no timing events inside a graph
+        s = seq();
+    }
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(st, &g);
     if (s != FLG_OK || e != cudaSuccess || g == nullptr) {
