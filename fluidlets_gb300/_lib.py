@@ -46,6 +46,8 @@ SIGNATURES = {
                                           c_int, c_int64, _P]),
     "flg_assemble_bucket": (c_int, [c_int, c_double, c_double, _P, _P, _P, c_int64, c_double, _P, c_int, c_int64,
                                     _P]),
+    "flg_assemble_bucket_uniform": (c_int, [c_int, c_double, c_double, _P, _P, _P, c_int64, c_double, _P, c_int,
+                                            c_int64, _P]),
     "flg_assemble_nearest_workspace": (c_size_t, [c_int64, c_int64]),
     "flg_assemble_nearest": (c_int, [c_int, c_double, c_double, _P, c_int64, _P, _P, _P, c_int64, c_int64,
                                      c_double, c_double, _P, c_int, c_int64, _P, c_size_t, _P]),
@@ -70,8 +72,8 @@ SIGNATURES = {
     "flg_gmres_ir_dense_workspace": (c_size_t, [c_int64, c_int]),
     "flg_gmres_ir_dense": (c_int, [c_int64, _P, c_int64, _P, c_int64, _P, c_int64, _P, _P, _P, c_double, c_int, c_int,
                                    POINTER(c_int), POINTER(c_int), POINTER(c_double), _P, c_size_t, _P]),
-    "flg_bucket_graph_create": (c_int, [c_int, c_double, c_double, _P, _P, _P, c_int64, c_double, _P, _P, _P, c_int64,
-                                        c_int, _P, _P, _P, c_size_t, _P, POINTER(c_void_p)]),
+    "flg_bucket_graph_create": (c_int, [c_int, c_double, c_double, _P, _P, c_int, _P, c_int64, c_double, _P, _P, _P,
+                                        c_int64, c_int, _P, _P, _P, c_size_t, _P, POINTER(c_void_p)]),
     "flg_gmres_ir_graph_workspace": (c_size_t, [c_int64, c_int]),
     "flg_gmres_ir_graph_create": (c_int, [c_int64, _P, c_int64, _P, c_int64, _P, c_int64, _P, _P, _P, c_double, c_int,
                                           c_int, _P, c_size_t, _P, POINTER(c_void_p)]),

@@ -186,6 +186,56 @@ __global__ void __launch_bounds__(128) assemble_bucket_kernel(AsmArgs a, const i
     }
 }
 
+// The same with one blob width for every point (eps[0], read from device memory at replay):
+// the symmetric assembly of assemble_sym_kernel (pairs i <= j, the mirror written as is, or
+// transposed for the wall kernel by reciprocity) with the bucket's identity padding.
+template <int KIND, bool TRANSPOSE>
+__global__ void __launch_bounds__(128) assemble_bucket_sym_kernel(AsmArgs a, const int64_t *n_real_p) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= a.N) return;
+    const int64_t nr = *n_real_p;
+    const bool jr = j < nr;
+    const double e = a.eps[0], e2 = e * e;
+    double sx = 0, sy = 0, sz = 0;
+    if (jr) {
+        sx = a.src[3 * j];
+        sy = a.src[3 * j + 1];
+        sz = a.src[3 * j + 2];
+    }
+    AsmArgs id = a;  // identity / zero blocks of the padding: unscaled
+    id.scale = 1.0;
+    id.imu_re = 1.0;
+    id.imu_im = 0.0;
+    for (int64_t i0 = (int64_t)blockIdx.y * kSymTile; i0 <= j; i0 += (int64_t)gridDim.y * kSymTile) {
+        for (int t = 0; t < kSymTile; t++) {
+            const int64_t i = i0 + t;
+            if (i > j) break;
+            double G[9], Gi[9];
+            if (jr) {  // i <= j < nr: a real pair
+                block_f64<KIND, false>(a.src[3 * i], a.src[3 * i + 1], a.src[3 * i + 2], sx, sy, sz, e2, a.are,
+                                       a.aim, G, Gi);
+                store_block(a, i, 3 * j, G, Gi, false);
+                if (i == j) continue;
+                if (TRANSPOSE) {
+#pragma unroll
+                    for (int r = 0; r < 3; r++)
+#pragma unroll
+                        for (int c = r + 1; c < 3; c++) {
+                            const double u = G[3 * r + c];
+                            G[3 * r + c] = G[3 * c + r];
+                            G[3 * c + r] = u;
+                        }
+                }
+                store_block(a, j, 3 * i, G, Gi, false);
+            } else {
+                for (int q = 0; q < 9; q++) G[q] = (i == j && (q == 0 || q == 4 || q == 8)) ? 1.0 : 0.0;
+                store_block(id, i, 3 * j, G, G, false);
+                if (i != j) store_block(id, j, 3 * i, G, G, false);
+            }
+        }
+    }
+}
+
 // nearest-neighbour assembly: thread per (target i, force group j), members of
 // group j (ascending quadrature index) summed in FP64
 struct NearestArgs {
@@ -605,6 +655,35 @@ extern "C" int flg_assemble_self_uniform(int kind, double alpha_re, double alpha
     else if (kind == FLG_WALL) assemble_sym_kernel<FLG_WALL, false, true><<<grid, 128, 0, st>>>(a, e2);
     else if (alpha_im != 0.0) assemble_sym_kernel<FLG_BRINKMANLET, true, false><<<grid, 128, 0, st>>>(a, e2);
     else assemble_sym_kernel<FLG_BRINKMANLET, false, false><<<grid, 128, 0, st>>>(a, e2);
+    FLG_LAUNCH_CHECK();
+    prof_end(FLG_SLOT_ASSEMBLE, st);
+    return FLG_OK;
+}
+
+extern "C" int flg_assemble_bucket_uniform(int kind, double alpha_re, double alpha_im, const double *points,
+                                           const double *eps, const int64_t *n_real, int64_t n_cap, double mu_re,
+                                           void *out, int out_type, int64_t ld, void *stream) {
+    FLG_RANGE("flg_assemble_bucket_uniform");
+    AsmArgs a{};
+    FLG_TRY(prepare(kind, alpha_re, alpha_im, mu_re, 0.0, out_type, a));
+    FLG_REQUIRE(!(kind == FLG_BRINKMANLET && alpha_im != 0.0), "bucket assembly is real only");
+    FLG_REQUIRE(out_type == FLG_F64 || out_type == FLG_F32, "bucket assembly writes FLG_F64 or FLG_F32");
+    FLG_REQUIRE(n_cap >= 0 && ld >= 3 * n_cap, "bad bucket shape");
+    if (n_cap == 0) return FLG_OK;
+    FLG_REQUIRE(points && eps && n_real && out, "null pointer");
+    a.tg = points;
+    a.M = n_cap;
+    a.src = points;
+    a.eps = eps;
+    a.N = n_cap;
+    a.out = out;
+    a.ld = ld;
+    cudaStream_t st = as_stream(stream);
+    const dim3 grid((unsigned)ceil_div(n_cap, 128), (unsigned)std::min<int64_t>(ceil_div(n_cap, kSymTile), 65535));
+    prof_begin(FLG_SLOT_ASSEMBLE, st);
+    if (kind == FLG_STOKESLET) assemble_bucket_sym_kernel<FLG_STOKESLET, false><<<grid, 128, 0, st>>>(a, n_real);
+    else if (kind == FLG_WALL) assemble_bucket_sym_kernel<FLG_WALL, true><<<grid, 128, 0, st>>>(a, n_real);
+    else assemble_bucket_sym_kernel<FLG_BRINKMANLET, false><<<grid, 128, 0, st>>>(a, n_real);
     FLG_LAUNCH_CHECK();
     prof_end(FLG_SLOT_ASSEMBLE, st);
     return FLG_OK;

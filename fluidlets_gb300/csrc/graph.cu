@@ -57,14 +57,19 @@ static int capture_graph(void *stream, F &&seq, void **graph_exec) {
 }
 
 extern "C" int flg_bucket_graph_create(int kind, double alpha_re, double alpha_im, const double *points,
-                                       const double *eps, const int64_t *n_real, int64_t n_cap, double mu_re,
+                                       const double *eps, int uniform_eps, const int64_t *n_real, int64_t n_cap,
+                                       double mu_re,
                                        double *K, float *A32, float *K32, int64_t ld32, int mode, float *dinv,
                                        int *flags, void *work, size_t work_bytes, void *stream, void **graph_exec) {
     FLG_RANGE("flg_bucket_graph_create");
     const int64_t n = 3 * n_cap;
     auto seq = [&]() -> int {
-        FLG_TRY(flg_assemble_bucket(kind, alpha_re, alpha_im, points, eps, n_real, n_cap, mu_re, K, FLG_F64, n,
-                                    stream));
+        if (uniform_eps)
+            FLG_TRY(flg_assemble_bucket_uniform(kind, alpha_re, alpha_im, points, eps, n_real, n_cap, mu_re, K,
+                                                FLG_F64, n, stream));
+        else
+            FLG_TRY(flg_assemble_bucket(kind, alpha_re, alpha_im, points, eps, n_real, n_cap, mu_re, K, FLG_F64, n,
+                                        stream));
         FLG_TRY(flg_convert_f64_f32x2(n, n, K, n, K32, A32, ld32, stream));
         return flg_lu_factor_lowp_async(n, K32, ld32, mode, dinv, flags, work, work_bytes, stream);
     };

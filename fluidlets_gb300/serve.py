@@ -48,6 +48,12 @@ BUCKET_BASE = 128
 TUNE_CANDIDATES = ("tf32", "tf32:128", "tf32:256", "bf16", "bf16:128", "bf16:256", "fp32")
 
 
+def _uniform(eps) -> bool:
+    """One blob width for every point (a scalar, or an array of equal entries)."""
+    a = np.asarray(eps, dtype=np.float64)
+    return a.ndim == 0 or a.size == 0 or bool(np.all(a == a.reshape(-1)[0]))
+
+
 def bucket_of(n_points: int) -> int:
     """Smallest bucket >= n_points: multiples of 128 on a 2^(1/4) geometric grid."""
     b = BUCKET_BASE
@@ -101,9 +107,10 @@ def plan_bytes(nb_points: int) -> int:
 class BucketPlan:
     """Device buffers and the captured assemble + factor graph of one bucket size."""
 
-    def __init__(self, kernel, nb_points: int, mu: float, lu: str, stream):
+    def __init__(self, kernel, nb_points: int, mu: float, lu: str, stream, uniform: bool = False):
         L = load()
         self.kernel, self.mu, self.lu, self.nbp = kernel, mu, lu, nb_points
+        self.uniform = uniform  # one blob width for every point: the symmetric assembly, half the pairs
         self.kind, self.are, self.aim = kernel_params(kernel)
         dev = torch.device("cuda", torch.cuda.current_device())
         n = 3 * nb_points
@@ -132,7 +139,8 @@ class BucketPlan:
     def _run(self):
         L = load()
         st = ctypes.c_void_p(self.stream.cuda_stream)
-        check(L.flg_assemble_bucket(self.kind, self.are, self.aim, dv.ptr(self.pts), dv.ptr(self.eps),
+        asm = L.flg_assemble_bucket_uniform if self.uniform else L.flg_assemble_bucket
+        check(asm(self.kind, self.are, self.aim, dv.ptr(self.pts), dv.ptr(self.eps),
                                     dv.ptr(self.n_real), self.nbp, float(self.mu), dv.ptr(self.K), F64, self.n, st),
               "bucket assembly")
         check(L.flg_convert_f64_f32x2(self.n, self.n, dv.ptr(self.K), self.n, dv.ptr(self.K32), dv.ptr(self.A32),
@@ -152,6 +160,7 @@ class BucketPlan:
         L = load()
         h = ctypes.c_void_p(0)
         st = L.flg_bucket_graph_create(self.kind, self.are, self.aim, dv.ptr(self.pts), dv.ptr(self.eps),
+                                       int(self.uniform),
                                        dv.ptr(self.n_real), self.nbp, float(self.mu), dv.ptr(self.K), dv.ptr(self.A32),
                                        dv.ptr(self.K32),
                                        self.ld32, self.mode, dv.ptr(self.dinv), dv.ptr(self.flags), dv.ptr(self.lu_ws),
@@ -298,7 +307,7 @@ class SolveServer:
         mode); swimmer plans per (kernel, force and quadrature point counts, eps, mu)."""
         if isinstance(req, ResistanceRequest):
             lu = self._lu_for(req, b) or "tune"
-            return ("res", kernel_params(req.kernel)[0], b, float(req.mu), lu)
+            return ("res", kernel_params(req.kernel)[0], b, float(req.mu), lu, _uniform(req.eps))
         kind = kernel_params(req.kernel if req.kernel is not None else Stokeslet3D())[0]
         return ("swim", kind, len(req.shape.x), len(req.shape.X), float(req.eps), float(req.mu))
 
@@ -417,7 +426,7 @@ class SolveServer:
                 lu = self._autotune(req, b, stream, X, e, U)
                 with self._cv:
                     self._tuned[(kernel_params(req.kernel)[0], b)] = lu
-            plan = BucketPlan(req.kernel, b, req.mu, lu, stream)
+            plan = BucketPlan(req.kernel, b, req.mu, lu, stream, uniform=_uniform(req.eps))
             with self._cv:
                 self.stats["plans_built"] += 1
             if self.graphs:
@@ -440,7 +449,7 @@ class SolveServer:
     def _autotune(self, req, b, stream, X, e, U):
         """Time factor + solve of this request for every candidate LU mode on one eager plan
         (one untimed run each first); the fastest whose residual meets rtol wins."""
-        p = BucketPlan(req.kernel, b, req.mu, "tf32", stream)
+        p = BucketPlan(req.kernel, b, req.mu, "tf32", stream, uniform=_uniform(req.eps))
         best = None
         for lu in TUNE_CANDIDATES:
             p.set_lu(lu)

@@ -161,6 +161,13 @@ int flg_assemble_self_uniform(int kind, double alpha_re, double alpha_im,
 int flg_assemble_bucket(int kind, double alpha_re, double alpha_im, const double *points, const double *eps,
                         const int64_t *n_real, int64_t n_cap, double mu_re, void *out, int out_type,
                         int64_t ld, void *stream);
+/* The same when every point has one blob width, eps[0] (read at replay time):
+ * half the pair evaluations (the mirror of block (i, j) written at (j, i) as
+ * is, or transposed for the wall kernel by reciprocity, as in
+ * flg_assemble_self_uniform).  No counterpart in the reference. */
+int flg_assemble_bucket_uniform(int kind, double alpha_re, double alpha_im, const double *points, const double *eps,
+                                const int64_t *n_real, int64_t n_cap, double mu_re, void *out, int out_type,
+                                int64_t ld, void *stream);
 
 /* Replaces fluidlets.assemble_nearest (core/assemble.py:68-101) and
  * _fill_nearest (49-58): K[:, group j] = sum_{k: nearest[k] = j} G(x_i, X_k)/mu.
@@ -301,9 +308,12 @@ int flg_gmres_ir_dense(int64_t n, const double *A, int64_t ld, const float *A32,
  * LU workspace) on `stream` (not the default stream) in thread-local capture
  * mode, after one eager pass, and returns the instantiated graph.  Replay with
  * flg_graph_launch; the real point count is read from *n_real at replay time.
+ * uniform_eps != 0: every point has the blob width eps[0] (read at replay time)
+ * and the assembly is flg_assemble_bucket_uniform, from half the pairs.
  * No counterpart in the reference. */
 int flg_bucket_graph_create(int kind, double alpha_re, double alpha_im, const double *points, const double *eps,
-                            const int64_t *n_real, int64_t n_cap, double mu_re, double *K, float *A32, float *K32,
+                            int uniform_eps, const int64_t *n_real, int64_t n_cap, double mu_re, double *K,
+                            float *A32, float *K32,
                             int64_t ld32, int mode, float *dinv, int *flags, void *work, size_t work_bytes,
                             void *stream, void **graph_exec);
 /* The FP32 copies (flg_convert_f64_f32x2) and the tensor-core LU

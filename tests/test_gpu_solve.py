@@ -491,3 +491,39 @@ def test_resistance_matrix_sphere_and_consistency():
     U, Om, _ = fl.rigid_body_mobility(W, E, 0.05, F, T)
     RE = fl.resistance_matrix(W, E, 0.05)
     assert rel_err(RE @ np.r_[U, Om], np.r_[F, T]) < 1e-9
+
+
+# ---- bucket assembly (solve server) -------------------------------------------------------------
+@pytest.mark.parametrize("kind", ["stokeslet", "wall", "brinkman"])
+def test_bucket_assembly_uniform_matches_full_and_pads_with_identity(kind):
+    """flg_assemble_bucket_uniform (one blob width, half the pairs) equals flg_assemble_bucket:
+    bit for bit for the free kernels, to rounding for the wall kernel (its mirror blocks are the
+    transposes, by reciprocity); padded rows and columns are the identity."""
+    L = _lib.load()
+    rng = np.random.default_rng(11)
+    n_cap, n_real = 384, 301
+    pts = np.zeros((n_cap, 3))
+    pts[:n_real] = np.c_[rng.uniform(-1, 1, (n_real, 2)), rng.uniform(0.1, 1.5, n_real)]
+    P = torch.tensor(pts, device="cuda")
+    E = torch.full((n_cap,), 0.07, dtype=torch.float64, device="cuda")
+    NR = torch.tensor([n_real], dtype=torch.int64, device="cuda")
+    code = _lib.KIND[kind]
+    are = 2.5 if kind == "brinkman" else 0.0
+    n = 3 * n_cap
+    out = {}
+    for name in ("flg_assemble_bucket", "flg_assemble_bucket_uniform"):
+        K = torch.full((n, n), float("nan"), dtype=torch.float64, device="cuda")
+        _lib.check(getattr(L, name)(code, are, 0.0, dv.ptr(P), dv.ptr(E), dv.ptr(NR), n_cap, 1.0, dv.ptr(K), _lib.F64,
+                                    n, dv.stream()))
+        out[name] = K.cpu().numpy()
+    full, sym = out["flg_assemble_bucket"], out["flg_assemble_bucket_uniform"]
+    assert np.isfinite(sym).all()
+    if kind == "wall":
+        assert rel_err(sym, full) < 1e-14
+    else:
+        assert np.array_equal(sym, full)
+    r = 3 * n_real
+    assert np.array_equal(sym[r:, r:], np.eye(n - r)) and not sym[:r, r:].any() and not sym[r:, :r].any()
+    ref = O.assemble({"stokeslet": "stokeslet", "wall": "wall", "brinkman": "brinkman"}[kind], pts[:n_real],
+                     pts[:n_real], 0.07, alpha=are)
+    assert_close(sym[:r, :r], ref, 1e-12, 1e-14)

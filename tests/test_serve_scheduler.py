@@ -110,7 +110,7 @@ def test_autotuner_keeps_the_fastest_candidate_that_converges(monkeypatch):
     tried = []
 
     class Plan:
-        def __init__(self, kernel, nbp, mu, lu, stream):
+        def __init__(self, kernel, nbp, mu, lu, stream, **kw):
             self.lu = lu
 
         def set_lu(self, lu):
