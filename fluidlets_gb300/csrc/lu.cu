@@ -1585,23 +1585,26 @@ static int side_stream(SideStream **out) {
 extern "C" int64_t flg_lu_lowp_dinv_elems(int64_t n) { return 2 * ceil_div(std::max<int64_t>(n, 1), kNB) * kNB * kNB; }
 
 // Tensor-core modes defer most of the trailing update: blocks are grouped into
-// outer panels of kOuter x 128 columns [K0, E).  Inner step k0 (diagonal block,
+// outer panels of W columns [K0, E), W = outer_width(n).  Inner step k0 (diagonal block,
 // panels) updates only the L-shaped part of the Schur complement that the next
 // inner steps read -- rows > k0 x columns (k0, E), and rows (k0, E) x columns
 // >= E -- with rank-128 updates; the rest, rows and columns >= E, receives one
 // rank-(E - K0) update per outer panel, which moves the trailing matrix through
-// HBM kOuter times less often.  The K-major copy of U (UtB: one row of
-// kOuter x 128 per column >= K0) feeds both.
-constexpr int kOuter = 4;
-constexpr int kOuterW = kOuter * kNB;
+// HBM W / 128 times less often.  The K-major copy of U (UtB: one row of W
+// per column >= K0) feeds both.  A wider W halves the trailing traffic again but
+// lengthens the chain of inner steps that nothing overlaps; measured on the
+// tensor-core modes (TF32 / BF16, factor + refinement): 1,024 columns is 6-9%
+// faster from n = 12,288 up and 2% slower at n = 4,608, so 512 below n = 8,192.
+static int64_t outer_width(int64_t n) { return (n >= 8192 ? 8 : 4) * (int64_t)kNB; }
 
 template <class Ar>
 static void lowp_carve(Ar &ar, int64_t n, int mode, float **U12, float **L21, float **UtB, char **tcw,
                        size_t *tcb) {
     *U12 = ar.template take<float>((size_t)kNB * n);
     *L21 = ar.template take<float>((size_t)n * kNB);
-    *UtB = ar.template take<float>((size_t)n * kOuterW);
-    *tcb = (mode == FLG_LU_FP32) ? 0 : tc_update_bytes(n, n, kOuterW, mode);
+    const int64_t W = outer_width(n);
+    *UtB = ar.template take<float>((size_t)n * W);
+    *tcb = (mode == FLG_LU_FP32) ? 0 : tc_update_bytes(n, n, W, mode);
     *tcw = ar.template take<char>(*tcb);
 }
 
@@ -1650,6 +1653,7 @@ extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mod
     }
     const bool tc = mode != FLG_LU_FP32;
     const int64_t nblk = ceil_div(n, kNB);
+    const int64_t W = outer_width(n);  // outer panel width
     float *Linv = dinv, *Uinv = dinv + nblk * kNB * kNB;
     SideStream *side = nullptr;
     if (tc) FLG_TRY(side_stream(&side));
@@ -1686,7 +1690,7 @@ extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mod
         FLG_LAUNCH_CHECK();
         FLG_CUDA(cudaEventRecord(side->join, side->s));
         if (t.Ut) {
-            transpose_f32_kernel<<<dim3(kNB / 32, (unsigned)ceil_div(t.nr, 32)), tb, 0, side->s>>>(t.Ut, kOuterW,
+            transpose_f32_kernel<<<dim3(kNB / 32, (unsigned)ceil_div(t.nr, 32)), tb, 0, side->s>>>(t.Ut, W,
                                                                                                    t.A12, ld, t.nr,
                                                                                                    kNB);
             FLG_LAUNCH_CHECK();
@@ -1695,8 +1699,8 @@ extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mod
         pending = true;
         return FLG_OK;
     };
-    for (int64_t K0 = 0; K0 < n; K0 += kOuterW) {
-        const int64_t E = std::min<int64_t>(n, K0 + kOuterW);
+    for (int64_t K0 = 0; K0 < n; K0 += W) {
+        const int64_t E = std::min<int64_t>(n, K0 + W);
         for (int64_t k0 = K0; k0 < E; k0 += kNB) {
             const int64_t k = k0 / kNB;
             const int nb = (int)std::min<int64_t>(kNB, n - k0);
@@ -1713,7 +1717,7 @@ extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mod
             prof_begin(FLG_SLOT_LU_PANEL, st);
             // (nb < kNB only for the last block, which has no trailing part)
             float *A12 = A + k0 * ld + c0, *A21 = A + c0 * ld + k0, *A22 = A + c0 * ld + c0;
-            float *Ut = UtB + (c0 - K0) * kOuterW + (k0 - K0);  // row: column - K0; K offset: k0 - K0
+            float *Ut = UtB + (c0 - K0) * W + (k0 - K0);  // row: column - K0; K offset: k0 - K0
             // an inner step whose next diagonal block runs ahead defers its transpose-back
             const bool defer_t = tcp && E > c0 && n - c0 > kNB;
             if (tcp) {
@@ -1731,10 +1735,10 @@ extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mod
                 transpose_f32_kernel<<<dim3((unsigned)ceil_div(nr, 32), kNB / 32), tb, 0, st>>>(A12, ld, T12, kNB,
                                                                                                  kNB, nr);
                 FLG_LAUNCH_CHECK();
-                FLG_TRY(tc_update(Ut, kOuterW, T12, kNB, Linv + k * kNB * kNB, kNB, nr, kNB, kNB, FLG_LU_TF32, tcw,
+                FLG_TRY(tc_update(Ut, W, T12, kNB, Linv + k * kNB * kNB, kNB, nr, kNB, kNB, FLG_LU_TF32, tcw,
                                   tcb, st, dinfo + 1, true));
                 if (!defer_t) {
-                    transpose_f32_kernel<<<dim3(kNB / 32, (unsigned)ceil_div(nr, 32)), tb, 0, st>>>(Ut, kOuterW, A12,
+                    transpose_f32_kernel<<<dim3(kNB / 32, (unsigned)ceil_div(nr, 32)), tb, 0, st>>>(Ut, W, A12,
                                                                                                      ld, nr, kNB);
                     FLG_LAUNCH_CHECK();
                 }
@@ -1743,7 +1747,7 @@ extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mod
                 // U12 = Linv A12 (+ its K-major copy), L21 = A21 Uinv: one launch, in place
                 const int ntu = (int)ceil_div(nr, 32), ntl = (int)ceil_div(nr, 32);
                 lowp_panel_kernel<<<ntu + ntl, 256, 0, st>>>(A, ld, k0, nr, Linv + k * kNB * kNB, Uinv + k * kNB * kNB,
-                                                             Ut, kOuterW, ntu);
+                                                             Ut, W, ntu);
                 FLG_LAUNCH_CHECK();
             } else {
                 FLG_TRY(sgemm(st, nb, nr, nb, 1.0f, Linv + k * kNB * kNB, kNB, A12, ld, 0.0f, U12, nr));
@@ -1759,40 +1763,40 @@ extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mod
                 if (n - c0 > kNB) {
                     // the next diagonal block first, then it factors beside the rest:
                     // rows > c0 + 128 x its columns, rows > k0 x columns (c0 + 128, E)
-                    FLG_TRY(tc_update(A22, ld, A21, ld, Ut, kOuterW, kNB, kNB, kNB, mode, tcw, tcb, st, dinfo + 1,
+                    FLG_TRY(tc_update(A22, ld, A21, ld, Ut, W, kNB, kNB, kNB, mode, tcw, tcb, st, dinfo + 1,
                                       false, tile));
                     FLG_TRY(look_ahead(c0, Deferred{Ut, A12, nr}));
-                    FLG_TRY(tc_update(A22 + kNB * ld, ld, A21 + kNB * ld, ld, Ut, kOuterW, nr - kNB, kNB, kNB, mode,
+                    FLG_TRY(tc_update(A22 + kNB * ld, ld, A21 + kNB * ld, ld, Ut, W, nr - kNB, kNB, kNB, mode,
                                       tcw, tcb, st, dinfo + 1, false, tile, cap));
                     if (E > c0 + kNB)
-                        FLG_TRY(tc_update(A22 + kNB, ld, A21, ld, Ut + kNB * kOuterW, kOuterW, nr, E - c0 - kNB, kNB,
+                        FLG_TRY(tc_update(A22 + kNB, ld, A21, ld, Ut + kNB * W, W, nr, E - c0 - kNB, kNB,
                                           mode, tcw, tcb, st, dinfo + 1, false, tile, cap));
                 } else {
                     // rows > k0 x columns (k0, E)
-                    FLG_TRY(tc_update(A22, ld, A21, ld, Ut, kOuterW, nr, E - c0, kNB, mode, tcw, tcb, st, dinfo + 1,
+                    FLG_TRY(tc_update(A22, ld, A21, ld, Ut, W, nr, E - c0, kNB, mode, tcw, tcb, st, dinfo + 1,
                                       false, tile));
                 }
                 // rows (k0, E) x columns >= E
                 if (n > E)
-                    FLG_TRY(tc_update(A + c0 * ld + E, ld, A21, ld, Ut + (E - c0) * kOuterW, kOuterW, E - c0, n - E,
+                    FLG_TRY(tc_update(A + c0 * ld + E, ld, A21, ld, Ut + (E - c0) * W, W, E - c0, n - E,
                                       kNB, mode, tcw, tcb, st, dinfo + 1, false, tile, pending ? cap : 0));
             }
             prof_end(FLG_SLOT_LU_UPDATE, st);
         }
-        if (tc && n > E) {  // the deferred rank-(E - K0) update of rows and columns >= E (E - K0 = kOuterW here)
+        if (tc && n > E) {  // the deferred rank-(E - K0) update of rows and columns >= E (E - K0 = W here)
             prof_begin(FLG_SLOT_LU_UPDATE, st);
-            float *C = A + E * ld + E, *Lp = A + E * ld + K0, *Up = UtB + (E - K0) * kOuterW;
+            float *C = A + E * ld + E, *Lp = A + E * ld + K0, *Up = UtB + (E - K0) * W;
             if (n - E > kNB) {
                 // the next outer panel's first diagonal block first, then it factors beside the rest
-                FLG_TRY(tc_update(C, ld, Lp, ld, Up, kOuterW, kNB, kNB, E - K0, mode, tcw, tcb, st, dinfo + 1, false,
+                FLG_TRY(tc_update(C, ld, Lp, ld, Up, W, kNB, kNB, E - K0, mode, tcw, tcb, st, dinfo + 1, false,
                                   tile));
                 FLG_TRY(look_ahead(E, Deferred{}));
-                FLG_TRY(tc_update(C + kNB * ld, ld, Lp + kNB * ld, ld, Up, kOuterW, n - E - kNB, kNB, E - K0, mode,
+                FLG_TRY(tc_update(C + kNB * ld, ld, Lp + kNB * ld, ld, Up, W, n - E - kNB, kNB, E - K0, mode,
                                   tcw, tcb, st, dinfo + 1, false, tile, cap));
-                FLG_TRY(tc_update(C + kNB, ld, Lp, ld, Up + kNB * kOuterW, kOuterW, n - E, n - E - kNB, E - K0, mode,
+                FLG_TRY(tc_update(C + kNB, ld, Lp, ld, Up + kNB * W, W, n - E, n - E - kNB, E - K0, mode,
                                   tcw, tcb, st, dinfo + 1, false, tile, cap));
             } else {
-                FLG_TRY(tc_update(C, ld, Lp, ld, Up, kOuterW, n - E, n - E, E - K0, mode, tcw, tcb, st, dinfo + 1,
+                FLG_TRY(tc_update(C, ld, Lp, ld, Up, W, n - E, n - E, E - K0, mode, tcw, tcb, st, dinfo + 1,
                                   false, tile));
             }
             prof_end(FLG_SLOT_LU_UPDATE, st);
