@@ -48,6 +48,8 @@ SIGNATURES = {
                                     _P]),
     "flg_assemble_bucket_uniform": (c_int, [c_int, c_double, c_double, _P, _P, _P, c_int64, c_double, _P, c_int,
                                             c_int64, _P]),
+    "flg_assemble_bucket_batched": (c_int, [c_int, c_double, c_double, _P, _P, c_int, _P, c_int64, c_int, c_double,
+                                            _P, c_int, c_int64, c_int64, _P]),
     "flg_assemble_nearest_workspace": (c_size_t, [c_int64, c_int64]),
     "flg_assemble_nearest": (c_int, [c_int, c_double, c_double, _P, c_int64, _P, _P, _P, c_int64, c_int64,
                                      c_double, c_double, _P, c_int, c_int64, _P, c_size_t, _P]),
@@ -60,6 +62,9 @@ SIGNATURES = {
     "flg_lu_factor_lowp_workspace": (c_size_t, [c_int64, c_int]),
     "flg_lu_factor_lowp": (c_int, [c_int64, _P, c_int64, c_int, _P, POINTER(c_int), _P, c_size_t, _P]),
     "flg_lu_factor_lowp_async": (c_int, [c_int64, _P, c_int64, c_int, _P, _P, _P, c_size_t, _P]),
+    "flg_lu_factor_lowp_batched_workspace": (c_size_t, [c_int64, c_int, c_int]),
+    "flg_lu_factor_lowp_batched_async": (c_int, [c_int64, c_int, _P, c_int64, c_int64, c_int, _P, _P, _P, c_size_t,
+                                                 _P]),
     "flg_lu_solve_lowp_workspace": (c_size_t, [c_int64]),
     "flg_lu_solve_lowp": (c_int, [c_int64, _P, c_int64, _P, _P, _P, _P, c_size_t, _P]),
     "flg_tc_rank_update_workspace": (c_size_t, [c_int64, c_int64, c_int]),
@@ -74,6 +79,9 @@ SIGNATURES = {
                                    POINTER(c_int), POINTER(c_int), POINTER(c_double), _P, c_size_t, _P]),
     "flg_bucket_graph_create": (c_int, [c_int, c_double, c_double, _P, _P, c_int, _P, c_int64, c_double, _P, _P, _P,
                                         c_int64, c_int, _P, _P, _P, c_size_t, _P, POINTER(c_void_p)]),
+    "flg_bucket_batch_graph_create": (c_int, [c_int, c_double, c_double, _P, _P, c_int, _P, c_int64, c_int, c_double,
+                                              _P, _P, _P, c_int64, c_int, _P, _P, _P, c_size_t, _P,
+                                              POINTER(c_void_p)]),
     "flg_gmres_ir_graph_workspace": (c_size_t, [c_int64, c_int]),
     "flg_gmres_ir_graph_create": (c_int, [c_int64, _P, c_int64, _P, c_int64, _P, c_int64, _P, _P, _P, c_double, c_int,
                                           c_int, _P, c_size_t, _P, POINTER(c_void_p)]),

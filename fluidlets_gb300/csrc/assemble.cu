@@ -35,6 +35,7 @@ struct AsmArgs {
     int out_type;
     int64_t ld;
     int64_t col_off;  // first column written (nearest: group index scale)
+    int64_t sys_stride;  // bucket batches: elements between the outputs of consecutive systems
 };
 
 // 3x3 block (row-major, before scale / mu); complex part only for complex alpha
@@ -156,8 +157,21 @@ __global__ void __launch_bounds__(128) assemble_sym_kernel(AsmArgs a, double e2)
 
 // Bucket assembly for graph replay: points padded to n_cap, the real count
 // read from device memory; entries with i or j >= n_real form an identity block.
+// A batch of systems of one bucket is one launch: system z = blockIdx.z has its
+// points at + 3 z n_cap, blob widths at + z n_cap, real count at + z, and its
+// matrix at out + z sys_stride.
+__device__ __forceinline__ void bucket_system(AsmArgs &a, const int64_t *&n_real_p) {
+    const int64_t z = blockIdx.z;
+    a.tg += 3 * z * a.M;
+    a.src += 3 * z * a.N;
+    a.eps += z * a.N;
+    a.out = (char *)a.out + z * a.sys_stride * (a.out_type == FLG_F64 ? 8 : 4);
+    n_real_p += z;
+}
+
 template <int KIND>
 __global__ void __launch_bounds__(128) assemble_bucket_kernel(AsmArgs a, const int64_t *n_real_p) {
+    bucket_system(a, n_real_p);
     const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= a.N) return;
     const int64_t nr = *n_real_p;
@@ -191,6 +205,7 @@ __global__ void __launch_bounds__(128) assemble_bucket_kernel(AsmArgs a, const i
 // transposed for the wall kernel by reciprocity) with the bucket's identity padding.
 template <int KIND, bool TRANSPOSE>
 __global__ void __launch_bounds__(128) assemble_bucket_sym_kernel(AsmArgs a, const int64_t *n_real_p) {
+    bucket_system(a, n_real_p);
     const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= a.N) return;
     const int64_t nr = *n_real_p;
@@ -660,15 +675,17 @@ extern "C" int flg_assemble_self_uniform(int kind, double alpha_re, double alpha
     return FLG_OK;
 }
 
-extern "C" int flg_assemble_bucket_uniform(int kind, double alpha_re, double alpha_im, const double *points,
-                                           const double *eps, const int64_t *n_real, int64_t n_cap, double mu_re,
-                                           void *out, int out_type, int64_t ld, void *stream) {
-    FLG_RANGE("flg_assemble_bucket_uniform");
+// nbat systems of one bucket (bucket_system), the symmetric form when every point of a
+// system has the blob width eps[0] of that system
+static int assemble_bucket_batch(int kind, double alpha_re, double alpha_im, const double *points, const double *eps,
+                                 bool uniform, const int64_t *n_real, int64_t n_cap, int nbat, double mu_re,
+                                 void *out, int out_type, int64_t ld, int64_t stride_out, cudaStream_t st) {
     AsmArgs a{};
     FLG_TRY(prepare(kind, alpha_re, alpha_im, mu_re, 0.0, out_type, a));
     FLG_REQUIRE(!(kind == FLG_BRINKMANLET && alpha_im != 0.0), "bucket assembly is real only");
     FLG_REQUIRE(out_type == FLG_F64 || out_type == FLG_F32, "bucket assembly writes FLG_F64 or FLG_F32");
     FLG_REQUIRE(n_cap >= 0 && ld >= 3 * n_cap, "bad bucket shape");
+    FLG_REQUIRE(nbat >= 1 && nbat <= 65535 && (nbat == 1 || stride_out >= 3 * n_cap * ld), "bad bucket batch");
     if (n_cap == 0) return FLG_OK;
     FLG_REQUIRE(points && eps && n_real && out, "null pointer");
     a.tg = points;
@@ -678,44 +695,49 @@ extern "C" int flg_assemble_bucket_uniform(int kind, double alpha_re, double alp
     a.N = n_cap;
     a.out = out;
     a.ld = ld;
-    cudaStream_t st = as_stream(stream);
-    const dim3 grid((unsigned)ceil_div(n_cap, 128), (unsigned)std::min<int64_t>(ceil_div(n_cap, kSymTile), 65535));
+    a.sys_stride = stride_out;
     prof_begin(FLG_SLOT_ASSEMBLE, st);
-    if (kind == FLG_STOKESLET) assemble_bucket_sym_kernel<FLG_STOKESLET, false><<<grid, 128, 0, st>>>(a, n_real);
-    else if (kind == FLG_WALL) assemble_bucket_sym_kernel<FLG_WALL, true><<<grid, 128, 0, st>>>(a, n_real);
-    else assemble_bucket_sym_kernel<FLG_BRINKMANLET, false><<<grid, 128, 0, st>>>(a, n_real);
+    if (uniform) {
+        const dim3 grid((unsigned)ceil_div(n_cap, 128), (unsigned)std::min<int64_t>(ceil_div(n_cap, kSymTile), 65535),
+                        (unsigned)nbat);
+        if (kind == FLG_STOKESLET) assemble_bucket_sym_kernel<FLG_STOKESLET, false><<<grid, 128, 0, st>>>(a, n_real);
+        else if (kind == FLG_WALL) assemble_bucket_sym_kernel<FLG_WALL, true><<<grid, 128, 0, st>>>(a, n_real);
+        else assemble_bucket_sym_kernel<FLG_BRINKMANLET, false><<<grid, 128, 0, st>>>(a, n_real);
+    } else {
+        dim3 grid = asm_grid(n_cap, n_cap);
+        grid.z = (unsigned)nbat;
+        if (kind == FLG_STOKESLET) assemble_bucket_kernel<FLG_STOKESLET><<<grid, 128, 0, st>>>(a, n_real);
+        else if (kind == FLG_WALL) assemble_bucket_kernel<FLG_WALL><<<grid, 128, 0, st>>>(a, n_real);
+        else assemble_bucket_kernel<FLG_BRINKMANLET><<<grid, 128, 0, st>>>(a, n_real);
+    }
     FLG_LAUNCH_CHECK();
     prof_end(FLG_SLOT_ASSEMBLE, st);
     return FLG_OK;
+}
+
+extern "C" int flg_assemble_bucket_uniform(int kind, double alpha_re, double alpha_im, const double *points,
+                                           const double *eps, const int64_t *n_real, int64_t n_cap, double mu_re,
+                                           void *out, int out_type, int64_t ld, void *stream) {
+    FLG_RANGE("flg_assemble_bucket_uniform");
+    return assemble_bucket_batch(kind, alpha_re, alpha_im, points, eps, true, n_real, n_cap, 1, mu_re, out, out_type,
+                                 ld, 0, as_stream(stream));
 }
 
 extern "C" int flg_assemble_bucket(int kind, double alpha_re, double alpha_im, const double *points, const double *eps,
                                    const int64_t *n_real, int64_t n_cap, double mu_re, void *out, int out_type,
                                    int64_t ld, void *stream) {
     FLG_RANGE("flg_assemble_bucket");
-    AsmArgs a{};
-    FLG_TRY(prepare(kind, alpha_re, alpha_im, mu_re, 0.0, out_type, a));
-    FLG_REQUIRE(!(kind == FLG_BRINKMANLET && alpha_im != 0.0), "bucket assembly is real only");
-    FLG_REQUIRE(out_type == FLG_F64 || out_type == FLG_F32, "bucket assembly writes FLG_F64 or FLG_F32");
-    FLG_REQUIRE(n_cap >= 0 && ld >= 3 * n_cap, "bad bucket shape");
-    if (n_cap == 0) return FLG_OK;
-    FLG_REQUIRE(points && eps && n_real && out, "null pointer");
-    a.tg = points;
-    a.M = n_cap;
-    a.src = points;
-    a.eps = eps;
-    a.N = n_cap;
-    a.out = out;
-    a.ld = ld;
-    cudaStream_t st = as_stream(stream);
-    const dim3 grid = asm_grid(n_cap, n_cap);
-    prof_begin(FLG_SLOT_ASSEMBLE, st);
-    if (kind == FLG_STOKESLET) assemble_bucket_kernel<FLG_STOKESLET><<<grid, 128, 0, st>>>(a, n_real);
-    else if (kind == FLG_WALL) assemble_bucket_kernel<FLG_WALL><<<grid, 128, 0, st>>>(a, n_real);
-    else assemble_bucket_kernel<FLG_BRINKMANLET><<<grid, 128, 0, st>>>(a, n_real);
-    FLG_LAUNCH_CHECK();
-    prof_end(FLG_SLOT_ASSEMBLE, st);
-    return FLG_OK;
+    return assemble_bucket_batch(kind, alpha_re, alpha_im, points, eps, false, n_real, n_cap, 1, mu_re, out, out_type,
+                                 ld, 0, as_stream(stream));
+}
+
+extern "C" int flg_assemble_bucket_batched(int kind, double alpha_re, double alpha_im, const double *points,
+                                           const double *eps, int uniform_eps, const int64_t *n_real, int64_t n_cap,
+                                           int nbat, double mu_re, void *out, int out_type, int64_t ld,
+                                           int64_t stride_out, void *stream) {
+    FLG_RANGE("flg_assemble_bucket_batched");
+    return assemble_bucket_batch(kind, alpha_re, alpha_im, points, eps, uniform_eps != 0, n_real, n_cap, nbat, mu_re,
+                                 out, out_type, ld, stride_out, as_stream(stream));
 }
 
 extern "C" size_t flg_assemble_nearest_workspace(int64_t Q, int64_t n_force) {

@@ -107,4 +107,11 @@ struct NvtxRange {
 
 __host__ __device__ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
+// the same tensor-core update applied to `count` independent systems: C, Lp and Ut of
+// system z at + z * (sC, sL, sU) elements (tc_gemm.cu)
+struct TcBatch {
+    int count = 1;
+    int64_t sC = 0, sL = 0, sU = 0;
+};
+
 }  // namespace flg

@@ -9,6 +9,10 @@
 // point count is read from device memory by the assembly kernel, so one graph
 // serves every problem size of its bucket.
 //
+// flg_bucket_batch_graph_create captures the same for a batch of systems of one
+// bucket: one batched assembly launch, one FP32 conversion pass over all of them,
+// and the batched tensor-core LU (every step's kernels cover all systems).
+//
 // flg_lowp_factor_graph_create captures the FP32 copies and the tensor-core LU of
 // an already assembled K (resistance(), which assembles eagerly).
 //
@@ -72,6 +76,26 @@ extern "C" int flg_bucket_graph_create(int kind, double alpha_re, double alpha_i
                                         stream));
         FLG_TRY(flg_convert_f64_f32x2(n, n, K, n, K32, A32, ld32, stream));
         return flg_lu_factor_lowp_async(n, K32, ld32, mode, dinv, flags, work, work_bytes, stream);
+    };
+    return capture_graph(stream, seq, graph_exec);
+}
+
+extern "C" int flg_bucket_batch_graph_create(int kind, double alpha_re, double alpha_im, const double *points,
+                                             const double *eps, int uniform_eps, const int64_t *n_real, int64_t n_cap,
+                                             int nbat, double mu_re, double *K, float *A32, float *K32, int64_t ld32,
+                                             int mode, float *dinv, int *flags, void *work, size_t work_bytes,
+                                             void *stream, void **graph_exec) {
+    FLG_RANGE("flg_bucket_batch_graph_create");
+    FLG_REQUIRE(n_cap >= 1 && nbat >= 1 && ld32 >= 3 * n_cap && K && A32 && K32 && dinv && flags,
+                "bad batched bucket graph arguments");
+    const int64_t n = 3 * n_cap;
+    auto seq = [&]() -> int {
+        FLG_TRY(flg_assemble_bucket_batched(kind, alpha_re, alpha_im, points, eps, uniform_eps, n_real, n_cap, nbat,
+                                            mu_re, K, FLG_F64, n, n * n, stream));
+        // system z of K (n x n) and of the FP32 copies (n x ld32) are consecutive: one tall matrix
+        FLG_TRY(flg_convert_f64_f32x2(nbat * n, n, K, n, K32, A32, ld32, stream));
+        return flg_lu_factor_lowp_batched_async(n, nbat, K32, ld32, n * ld32, mode, dinv, flags, work, work_bytes,
+                                                stream);
     };
     return capture_graph(stream, seq, graph_exec);
 }

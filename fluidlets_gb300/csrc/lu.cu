@@ -761,9 +761,17 @@ __device__ __forceinline__ void diag_store_step(int s, const float *D, const flo
         }
 }
 
+// One CTA per system of a batch: system z = blockIdx.x at A + z sA, Linv / Uinv + z sD,
+// UinvT + z sT, its flags at info + 2 z.
 __global__ void __launch_bounds__(512) diag_lowp_kernel(float *A, int64_t ld, int64_t k0, int nb, float *Linv,
-                                                        float *Uinv, float *UinvT, int *info) {
+                                                        float *Uinv, float *UinvT, int *info, int64_t sA, int64_t sD,
+                                                        int64_t sT) {
     extern __shared__ __align__(16) float sm[];
+    {
+        const int64_t z = blockIdx.x;
+        A += z * sA, Linv += z * sD, Uinv += z * sD, info += 2 * z;
+        if (UinvT) UinvT += z * sT;
+    }
     float *D = sm, *X = sm + kNB * kLD, *Y = sm + 2 * kNB * kLD;
     __shared__ __align__(16) float R[2 * kSB], Lc[kSB * kSB];
     __shared__ int flag;
@@ -966,10 +974,11 @@ __global__ void copy2d_f32_kernel(const float *src, int64_t lds, float *dst, int
         if (c < cols) dst[r * ldd + c] = src[r * lds + c];
 }
 
-// dst (cols x rows, ldd) = src^T (rows x cols, lds)
+// dst (cols x rows, ldd) = src^T (rows x cols, lds); system blockIdx.z at src + z ss, dst + z sd
 __global__ void transpose_f32_kernel(const float *src, int64_t lds, float *dst, int64_t ldd, int64_t rows,
-                                     int64_t cols) {
+                                     int64_t cols, int64_t ss, int64_t sd) {
     __shared__ float t[32][33];
+    src += blockIdx.z * ss, dst += blockIdx.z * sd;
     const int64_t r0 = (int64_t)blockIdx.y * 32, c0 = (int64_t)blockIdx.x * 32;
     for (int i = threadIdx.y; i < 32; i += blockDim.y) {
         const int64_t r = r0 + i, c = c0 + threadIdx.x;
@@ -982,11 +991,12 @@ __global__ void transpose_f32_kernel(const float *src, int64_t lds, float *dst, 
     }
 }
 
-// tensor-core update (tc_gemm.cu): C (m x nc, ldc) -= Lp (m x K, ldl) * Ut^T (nc x K, ldu), K % 128 == 0
-size_t tc_update_bytes(int64_t m, int64_t nc, int64_t K, int mode);
+// tensor-core update (tc_gemm.cu): C (m x nc, ldc) -= Lp (m x K, ldl) * Ut^T (nc x K, ldu), K % 128 == 0,
+// for one system or a batch of them (TcBatch)
+size_t tc_update_bytes(int64_t m, int64_t nc, int64_t K, int mode, int nb = 1);
 int tc_update(float *C, int64_t ldc, const float *Lp, int64_t ldl, const float *Ut, int64_t ldu, int64_t m,
               int64_t nc, int64_t K, int mode, void *work, size_t work_bytes, cudaStream_t st, int *err_dev,
-              bool store = false, int tile = 0, int max_ctas = 0);
+              bool store = false, int tile = 0, int max_ctas = 0, const TcBatch &bt = TcBatch{});
 
 static int sgemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, float alpha, const float *A, int64_t lda,
                  const float *B, int64_t ldb, float beta, float *C, int64_t ldc) {
@@ -1597,14 +1607,15 @@ extern "C" int64_t flg_lu_lowp_dinv_elems(int64_t n) { return 2 * ceil_div(std::
 // faster from n = 12,288 up and 2% slower at n = 4,608, so 512 below n = 8,192.
 static int64_t outer_width(int64_t n) { return (n >= 8192 ? 8 : 4) * (int64_t)kNB; }
 
+// scratch of nbat systems, system z's at + z * (kNB n, n kNB, n W) floats
 template <class Ar>
-static void lowp_carve(Ar &ar, int64_t n, int mode, float **U12, float **L21, float **UtB, char **tcw,
+static void lowp_carve(Ar &ar, int64_t n, int nbat, int mode, float **U12, float **L21, float **UtB, char **tcw,
                        size_t *tcb) {
-    *U12 = ar.template take<float>((size_t)kNB * n);
-    *L21 = ar.template take<float>((size_t)n * kNB);
+    *U12 = ar.template take<float>((size_t)nbat * kNB * n);
+    *L21 = ar.template take<float>((size_t)nbat * n * kNB);
     const int64_t W = outer_width(n);
-    *UtB = ar.template take<float>((size_t)n * W);
-    *tcb = (mode == FLG_LU_FP32) ? 0 : tc_update_bytes(n, n, W, mode);
+    *UtB = ar.template take<float>((size_t)nbat * n * W);
+    *tcb = (mode == FLG_LU_FP32) ? 0 : tc_update_bytes(n, n, W, mode, nbat);
     *tcw = ar.template take<char>(*tcb);
 }
 
@@ -1617,34 +1628,52 @@ extern "C" size_t flg_lu_factor_lowp_workspace(int64_t n, int mode) {
     float *a, *b, *d;
     char *w;
     size_t t;
-    lowp_carve(c, n, mode, &a, &b, &d, &w, &t);
+    lowp_carve(c, n, 1, mode, &a, &b, &d, &w, &t);
     return c.bytes() + 256;  // + the flags of flg_lu_factor_lowp, at the end
 }
 
-extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mode, float *dinv, int *flags, void *work,
-                                        size_t work_bytes, void *stream) {
-    FLG_RANGE("flg_lu_factor_lowp_async");
-    FLG_REQUIRE(n >= 0 && ld >= n && flags, "bad LU arguments");
+extern "C" size_t flg_lu_factor_lowp_batched_workspace(int64_t n, int nbat, int mode) {
+    mode = lu_prec(mode);
+    CountingArena c;
+    float *a, *b, *d;
+    char *w;
+    size_t t;
+    lowp_carve(c, n, std::max(nbat, 1), mode, &a, &b, &d, &w, &t);
+    return c.bytes();
+}
+
+// The low-precision LU of nbat systems of order n in one sequence of launches: system z at
+// A + z sA (row stride ld), its block inverses at dinv + z flg_lu_lowp_dinv_elems(n), its
+// flags at flags + 2 z.  Every kernel of a step covers all systems (one CTA per system for
+// the diagonal blocks; the tensor-core updates walk the tiles of all systems).
+static int lowp_factor(int64_t n, int nbat, float *A, int64_t ld, int64_t sA, int mode, float *dinv, int *flags,
+                       void *work, size_t work_bytes, cudaStream_t st) {
+    FLG_REQUIRE(n >= 0 && ld >= n && flags && nbat >= 1, "bad LU arguments");
     const int tbits = mode & (FLG_LU_TILE_N128 | FLG_LU_TILE_N256);
     FLG_REQUIRE(tbits != (FLG_LU_TILE_N128 | FLG_LU_TILE_N256), "two tile widths in LU mode %d", mode);
     const int tile = tbits == FLG_LU_TILE_N128 ? 128 : tbits == FLG_LU_TILE_N256 ? 256 : 0;
     mode = lu_prec(mode);
     FLG_REQUIRE(mode == FLG_LU_TF32 || mode == FLG_LU_BF16 || (mode == FLG_LU_FP32 && tile == 0), "unknown LU mode %d",
                 mode | tbits);
+    FLG_REQUIRE(nbat == 1 || mode != FLG_LU_FP32, "batched LU needs a tensor-core mode (TF32 or BF16)");
+    FLG_REQUIRE(nbat == 1 || (sA >= n * ld && sA % 4 == 0), "bad system stride");
     FLG_REQUIRE(ld % 4 == 0, "ld must be a multiple of 4 (16-byte rows)");
-    cudaStream_t st = as_stream(stream);
-    FLG_CUDA(cudaMemsetAsync(flags, 0, 2 * sizeof(int), st));
+    FLG_CUDA(cudaMemsetAsync(flags, 0, 2 * sizeof(int) * nbat, st));
     if (n == 0) return FLG_OK;
     FLG_REQUIRE(A && dinv, "null pointer");
     Arena ar(work, work_bytes);
     float *U12, *L21, *UtB;
     char *tcw;
     size_t tcb;
-    lowp_carve(ar, n, mode, &U12, &L21, &UtB, &tcw, &tcb);
+    lowp_carve(ar, n, nbat, mode, &U12, &L21, &UtB, &tcw, &tcb);
     FLG_REQUIRE(U12 && L21 && UtB && (tcb == 0 || tcw), "workspace too small for LU (%zu bytes)", work_bytes);
     // the tensor-core panels use the partial-block scratch: U12 for A12^T, L21 for Uinv^T
     float *T12 = U12, *UinvT = L21;
     int *dinfo = flags;  // [0] first bad pivot, [1] tensor-core wait timed out
+    const int64_t W = outer_width(n);  // outer panel width
+    // per-system strides: the matrix, the block inverses, A12^T / Uinv^T scratch, U's K-major copy
+    const int64_t sD = flg_lu_lowp_dinv_elems(n), sT = (int64_t)kNB * n, sUt = n * W;
+    const TcBatch bA{nbat, sA, sA, sUt}, bU{nbat, sUt, sT, sD}, bL{nbat, sA, sA, sT};
     const size_t dsmem = kDiagSmem;
     static bool attr_set = false;  // set once, so a later call can be captured in a graph
     if (!attr_set) {
@@ -1653,19 +1682,18 @@ extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mod
     }
     const bool tc = mode != FLG_LU_FP32;
     const int64_t nblk = ceil_div(n, kNB);
-    const int64_t W = outer_width(n);  // outer panel width
     float *Linv = dinv, *Uinv = dinv + nblk * kNB * kNB;
     SideStream *side = nullptr;
     if (tc) FLG_TRY(side_stream(&side));
-    // the persistent updates that run beside a look-ahead diagonal block leave it an SM
-    const int cap = std::max(1, sm_count() - 1);
+    // the persistent updates that run beside the look-ahead diagonal blocks leave them an SM each
+    const int cap = std::max(1, sm_count() - nbat);
     auto diag = [&](int64_t d0, cudaStream_t s) {
         const int64_t kd = d0 / kNB;
         const int nbd = (int)std::min<int64_t>(kNB, n - d0);
         const bool tcp = tc && nbd == kNB && n - (d0 + nbd) > 0;  // tensor-core panels follow
         prof_begin(FLG_SLOT_LU_DIAG, s);
-        diag_lowp_kernel<<<1, 512, dsmem, s>>>(A, ld, d0, nbd, Linv + kd * kNB * kNB, Uinv + kd * kNB * kNB,
-                                               tcp ? UinvT : nullptr, dinfo);
+        diag_lowp_kernel<<<nbat, 512, dsmem, s>>>(A, ld, d0, nbd, Linv + kd * kNB * kNB, Uinv + kd * kNB * kNB,
+                                                  tcp ? UinvT : nullptr, dinfo, sA, sD, sT);
         prof_end(FLG_SLOT_LU_DIAG, s);
     };
     // Look-ahead: once the 128 x 128 block at d0 has its last update (launched on st), the
@@ -1690,9 +1718,8 @@ extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mod
         FLG_LAUNCH_CHECK();
         FLG_CUDA(cudaEventRecord(side->join, side->s));
         if (t.Ut) {
-            transpose_f32_kernel<<<dim3(kNB / 32, (unsigned)ceil_div(t.nr, 32)), tb, 0, side->s>>>(t.Ut, W,
-                                                                                                   t.A12, ld, t.nr,
-                                                                                                   kNB);
+            transpose_f32_kernel<<<dim3(kNB / 32, (unsigned)ceil_div(t.nr, 32), nbat), tb, 0, side->s>>>(
+                t.Ut, W, t.A12, ld, t.nr, kNB, sUt, sA);
             FLG_LAUNCH_CHECK();
             side_busy = true;
         }
@@ -1730,16 +1757,16 @@ extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mod
                 FLG_CUDA(cudaEventRecord(side->lfork, st));
                 FLG_CUDA(cudaStreamWaitEvent(side->s, side->lfork, 0));
                 FLG_TRY(tc_update(A21, ld, A21, ld, UinvT, kNB, nr, kNB, kNB, FLG_LU_TF32, tcw, tcb, side->s,
-                                  dinfo + 1, true));
+                                  dinfo + 1, true, 0, 0, bL));
                 FLG_CUDA(cudaEventRecord(side->ljoin, side->s));
-                transpose_f32_kernel<<<dim3((unsigned)ceil_div(nr, 32), kNB / 32), tb, 0, st>>>(A12, ld, T12, kNB,
-                                                                                                 kNB, nr);
+                transpose_f32_kernel<<<dim3((unsigned)ceil_div(nr, 32), kNB / 32, nbat), tb, 0, st>>>(
+                    A12, ld, T12, kNB, kNB, nr, sA, sT);
                 FLG_LAUNCH_CHECK();
                 FLG_TRY(tc_update(Ut, W, T12, kNB, Linv + k * kNB * kNB, kNB, nr, kNB, kNB, FLG_LU_TF32, tcw,
-                                  tcb, st, dinfo + 1, true));
+                                  tcb, st, dinfo + 1, true, 0, 0, bU));
                 if (!defer_t) {
-                    transpose_f32_kernel<<<dim3(kNB / 32, (unsigned)ceil_div(nr, 32)), tb, 0, st>>>(Ut, W, A12,
-                                                                                                     ld, nr, kNB);
+                    transpose_f32_kernel<<<dim3(kNB / 32, (unsigned)ceil_div(nr, 32), nbat), tb, 0, st>>>(
+                        Ut, W, A12, ld, nr, kNB, sUt, sA);
                     FLG_LAUNCH_CHECK();
                 }
                 FLG_CUDA(cudaStreamWaitEvent(st, side->ljoin, 0));
@@ -1764,22 +1791,22 @@ extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mod
                     // the next diagonal block first, then it factors beside the rest:
                     // rows > c0 + 128 x its columns, rows > k0 x columns (c0 + 128, E)
                     FLG_TRY(tc_update(A22, ld, A21, ld, Ut, W, kNB, kNB, kNB, mode, tcw, tcb, st, dinfo + 1,
-                                      false, tile));
+                                      false, tile, 0, bA));
                     FLG_TRY(look_ahead(c0, Deferred{Ut, A12, nr}));
                     FLG_TRY(tc_update(A22 + kNB * ld, ld, A21 + kNB * ld, ld, Ut, W, nr - kNB, kNB, kNB, mode,
-                                      tcw, tcb, st, dinfo + 1, false, tile, cap));
+                                      tcw, tcb, st, dinfo + 1, false, tile, cap, bA));
                     if (E > c0 + kNB)
                         FLG_TRY(tc_update(A22 + kNB, ld, A21, ld, Ut + kNB * W, W, nr, E - c0 - kNB, kNB,
-                                          mode, tcw, tcb, st, dinfo + 1, false, tile, cap));
+                                          mode, tcw, tcb, st, dinfo + 1, false, tile, cap, bA));
                 } else {
                     // rows > k0 x columns (k0, E)
                     FLG_TRY(tc_update(A22, ld, A21, ld, Ut, W, nr, E - c0, kNB, mode, tcw, tcb, st, dinfo + 1,
-                                      false, tile));
+                                      false, tile, 0, bA));
                 }
                 // rows (k0, E) x columns >= E
                 if (n > E)
                     FLG_TRY(tc_update(A + c0 * ld + E, ld, A21, ld, Ut + (E - c0) * W, W, E - c0, n - E,
-                                      kNB, mode, tcw, tcb, st, dinfo + 1, false, tile, pending ? cap : 0));
+                                      kNB, mode, tcw, tcb, st, dinfo + 1, false, tile, pending ? cap : 0, bA));
             }
             prof_end(FLG_SLOT_LU_UPDATE, st);
         }
@@ -1789,15 +1816,15 @@ extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mod
             if (n - E > kNB) {
                 // the next outer panel's first diagonal block first, then it factors beside the rest
                 FLG_TRY(tc_update(C, ld, Lp, ld, Up, W, kNB, kNB, E - K0, mode, tcw, tcb, st, dinfo + 1, false,
-                                  tile));
+                                  tile, 0, bA));
                 FLG_TRY(look_ahead(E, Deferred{}));
                 FLG_TRY(tc_update(C + kNB * ld, ld, Lp + kNB * ld, ld, Up, W, n - E - kNB, kNB, E - K0, mode,
-                                  tcw, tcb, st, dinfo + 1, false, tile, cap));
+                                  tcw, tcb, st, dinfo + 1, false, tile, cap, bA));
                 FLG_TRY(tc_update(C + kNB, ld, Lp, ld, Up + kNB * W, W, n - E, n - E - kNB, E - K0, mode,
-                                  tcw, tcb, st, dinfo + 1, false, tile, cap));
+                                  tcw, tcb, st, dinfo + 1, false, tile, cap, bA));
             } else {
                 FLG_TRY(tc_update(C, ld, Lp, ld, Up, W, n - E, n - E, E - K0, mode, tcw, tcb, st, dinfo + 1,
-                                  false, tile));
+                                  false, tile, 0, bA));
             }
             prof_end(FLG_SLOT_LU_UPDATE, st);
         }
@@ -1808,6 +1835,20 @@ extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mod
         FLG_CUDA(cudaStreamWaitEvent(st, side->tail, 0));
     }
     return FLG_OK;
+}
+
+extern "C" int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mode, float *dinv, int *flags, void *work,
+                                        size_t work_bytes, void *stream) {
+    FLG_RANGE("flg_lu_factor_lowp_async");
+    return lowp_factor(n, 1, A, ld, 0, mode, dinv, flags, work, work_bytes, as_stream(stream));
+}
+
+extern "C" int flg_lu_factor_lowp_batched_async(int64_t n, int nbat, float *A, int64_t ld, int64_t stride_a, int mode,
+                                                float *dinv, int *flags, void *work, size_t work_bytes,
+                                                void *stream) {
+    FLG_RANGE("flg_lu_factor_lowp_batched_async");
+    FLG_REQUIRE(nbat >= 1 && nbat <= 64, "batch of %d systems (1 .. 64)", nbat);
+    return lowp_factor(n, nbat, A, ld, stride_a, mode, dinv, flags, work, work_bytes, as_stream(stream));
 }
 
 extern "C" int flg_lu_factor_lowp(int64_t n, float *A, int64_t ld, int mode, float *dinv, int *info, void *work,

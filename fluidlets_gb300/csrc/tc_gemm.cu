@@ -4,9 +4,12 @@
 //   (or, in store mode, C = A * B^T)
 //
 // Both operands are K-major (K contiguous per row, K a multiple of 128).  A
-// persistent kernel, one CTA per SM (the caller may cap the grid below the SM
-// count), walks the 128 x BN tiles of C (BN = 256, or 128 for narrow or small
-// updates, chosen per call):
+// batch of equally shaped updates of independent systems (fixed strides
+// between their C, A and Bt) is one launch: the tensor maps are 3-D, the
+// system index their outer coordinate.  A persistent kernel, one CTA per SM
+// (the caller may cap the grid below the SM count), walks the 128 x BN tiles
+// of C over all systems (BN = 256, or 128 for narrow or small updates, chosen
+// per call):
 //   * warp 0 (one lane) streams K-blocks of A and B (128 B = 32 TF32 or 64 BF16
 //     per row) with TMA (cp.async.bulk.tensor, 128-byte swizzle) into a
 //     shared-memory ring guarded by mbarriers (4 stages at BN = 256, 6 at 128);
@@ -55,24 +58,26 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar, int x, int y) {
+// 3-D tiles: x (innermost, 16-byte aligned), row y, system z
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, uint64_t *bar, int x, int y, int z) {
     asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
-            smem_u32(dst)),
-        "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(x), "r"(y)
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], "
+        "[%2];" ::"r"(smem_u32(dst)),
+        "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(x), "r"(y), "r"(z)
         : "memory");
 }
-__device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, const void *src, int x, int y) {
-    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.tile.bulk_group [%0, {%2, %3}], [%1];" ::"l"(
+__device__ __forceinline__ void tma_store_3d(const CUtensorMap *map, const void *src, int x, int y, int z) {
+    asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%2, %3, %4}], [%1];" ::"l"(
                      (uint64_t)map),
-                 "r"(smem_u32(src)), "r"(x), "r"(y)
+                 "r"(smem_u32(src)), "r"(x), "r"(y), "r"(z)
                  : "memory");
 }
-__device__ __forceinline__ void tma_reduce_add_2d(const CUtensorMap *map, const void *src, int x, int y) {
-    asm volatile("cp.reduce.async.bulk.tensor.2d.global.shared::cta.add.tile.bulk_group [%0, {%2, %3}], [%1];" ::"l"(
-                     (uint64_t)map),
-                 "r"(smem_u32(src)), "r"(x), "r"(y)
-                 : "memory");
+__device__ __forceinline__ void tma_reduce_add_3d(const CUtensorMap *map, const void *src, int x, int y, int z) {
+    asm volatile(
+        "cp.reduce.async.bulk.tensor.3d.global.shared::cta.add.tile.bulk_group [%0, {%2, %3, %4}], [%1];" ::"l"(
+            (uint64_t)map),
+        "r"(smem_u32(src)), "r"(x), "r"(y), "r"(z)
+        : "memory");
 }
 
 // shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart
@@ -96,7 +101,7 @@ template <int MODE, int TC_BN>
 __global__ void __launch_bounds__(TC_THREADS, 1) tc_update_kernel(const __grid_constant__ CUtensorMap tmA,
                                                                   const __grid_constant__ CUtensorMap tmB,
                                                                   const __grid_constant__ CUtensorMap tmC, int m,
-                                                                  int nc, int nkb, int store, int *err) {
+                                                                  int nc, int nkb, int nbat, int store, int *err) {
     constexpr int KBLK = MODE == FLG_LU_TF32 ? 32 : 64;  // elements per 128-byte row
     constexpr int KSTEP_BYTES = 32;                       // one MMA consumes 32 bytes of each row
     constexpr uint32_t IDESC = tc_idesc(MODE == FLG_LU_TF32 ? 2u : 1u, TC_BN);
@@ -108,7 +113,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_update_kernel(const __grid_c
     __shared__ __align__(8) uint64_t full[TC_STAGES], empty[TC_STAGES], accf[2], acce[2], mma_done;
     __shared__ uint32_t tmem_base;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int ntx = (nc + TC_BN - 1) / TC_BN, nty = (m + TC_BM - 1) / TC_BM, ntiles = ntx * nty;
+    // tile t: system t / (ntx nty), then row block, then column block
+    const int ntx = (nc + TC_BN - 1) / TC_BN, nty = (m + TC_BM - 1) / TC_BM, nper = ntx * nty, ntiles = nper * nbat;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < TC_STAGES; s++) {
@@ -138,7 +144,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_update_kernel(const __grid_c
             uint32_t g = 0;
             bool ok = true;
             for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-                const int m0 = (t / ntx) * TC_BM, n0 = (t % ntx) * TC_BN;
+                const int z = t / nper, tr = t - z * nper, m0 = (tr / ntx) * TC_BM, n0 = (tr % ntx) * TC_BN;
                 for (int kb = 0; kb < nkb; kb++, g++) {
                     const int s = g % TC_STAGES;
                     const uint32_t use = g / TC_STAGES;
@@ -147,8 +153,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_update_kernel(const __grid_c
                         break;
                     }
                     mbar_expect_tx(&full[s], TC_A_BYTES + TC_B_BYTES);
-                    tma_load_2d(sA + s * TC_A_BYTES, &tmA, &full[s], kb * KBLK, m0);
-                    tma_load_2d(sB + s * TC_B_BYTES, &tmB, &full[s], kb * KBLK, n0);
+                    tma_load_3d(sA + s * TC_A_BYTES, &tmA, &full[s], kb * KBLK, m0, z);
+                    tma_load_3d(sB + s * TC_B_BYTES, &tmB, &full[s], kb * KBLK, n0, z);
                 }
             }
             // the last (up to S) loads issued must have landed before the CTA exits
@@ -219,7 +225,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_update_kernel(const __grid_c
             // warp-uniform: tcgen05.ld.sync.aligned must be executed by the whole warp
             if (!__all_sync(0xffffffffu, mbar_wait(&accf[buf], ause & 1, err, kWaitLimitNs))) break;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const int m0 = (t / ntx) * TC_BM, n0 = (t % ntx) * TC_BN;
+            const int z = t / nper, tr = t - z * nper, m0 = (tr / ntx) * TC_BM, n0 = (tr % ntx) * TC_BN;
 #pragma unroll 1
             for (int ch = 0; ch < TC_BN / 32; ch++, nst++) {
                 uint32_t v[32];
@@ -250,8 +256,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_update_kernel(const __grid_c
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 __syncwarp();
                 if (lane == 0) {
-                    if (store) tma_store_2d(&tmC, box, n0 + ch * 32, m0 + q * 32);
-                    else tma_reduce_add_2d(&tmC, box, n0 + ch * 32, m0 + q * 32);
+                    if (store) tma_store_3d(&tmC, box, n0 + ch * 32, m0 + q * 32, z);
+                    else tma_reduce_add_3d(&tmC, box, n0 + ch * 32, m0 + q * 32, z);
                     asm volatile("cp.async.bulk.commit_group;" ::: "memory");
                 }
             }
@@ -270,11 +276,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_update_kernel(const __grid_c
                      : "memory");
 }
 
-__global__ void f32_to_bf16_rows_kernel(const float *src, int64_t lds, __nv_bfloat16 *dst, int64_t rows, int64_t K) {
+// system blockIdx.y: src + y ss (rows x K, row stride lds) -> dst + y rows K (compact)
+__global__ void f32_to_bf16_rows_kernel(const float *src, int64_t lds, int64_t ss, __nv_bfloat16 *dst, int64_t rows,
+                                        int64_t K) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= rows * K) return;
     const int64_t r = i / K, k = i % K;
-    dst[i] = __float2bfloat16_rn(src[r * lds + k]);
+    dst[blockIdx.y * rows * K + i] = __float2bfloat16_rn(src[blockIdx.y * ss + r * lds + k]);
 }
 
 // ---- host side ---------------------------------------------------------------------------
@@ -291,19 +299,27 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     return fn;
 }
 
-// operand map: rows x K K-major elements (row stride ld_elems), box box_rows x 128 bytes, 128B swizzle
+// the stride between systems of a batch in bytes (one system: the matrix's own extent)
+static int64_t system_stride_bytes(int nb, int64_t stride_elems, int64_t rows, int64_t ld_elems, size_t esz) {
+    return (int64_t)esz * (nb > 1 ? stride_elems : std::max<int64_t>(rows, 1) * ld_elems);
+}
+
+// operand map: nb systems (stride sb elements) of rows x K K-major elements (row stride
+// ld_elems), box box_rows x 128 bytes x 1 system, 128B swizzle
 static int make_operand_map(CUtensorMap *map, const void *base, int64_t rows, int64_t K, int64_t ld_elems, int mode,
-                            int box_rows) {
+                            int box_rows, int nb = 1, int64_t sb = 0) {
     auto fn = encode_fn();
     FLG_REQUIRE(fn != nullptr, "cuTensorMapEncodeTiled unavailable");
     const bool bf = mode == FLG_LU_BF16;
     const size_t esz = bf ? 2 : 4;
-    FLG_REQUIRE(((uintptr_t)base & 15) == 0 && (ld_elems * esz) % 16 == 0, "TMA operand not 16-byte aligned");
-    cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
-    cuuint64_t strides[1] = {(cuuint64_t)(ld_elems * esz)};
-    cuuint32_t box[2] = {(cuuint32_t)(128 / esz), (cuuint32_t)box_rows};
-    cuuint32_t estr[2] = {1, 1};
-    CUresult r = fn(map, bf ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+    const int64_t sbb = system_stride_bytes(nb, sb, rows, ld_elems, esz);
+    FLG_REQUIRE(((uintptr_t)base & 15) == 0 && (ld_elems * esz) % 16 == 0 && sbb % 16 == 0,
+                "TMA operand not 16-byte aligned");
+    cuuint64_t dims[3] = {(cuuint64_t)K, (cuuint64_t)rows, (cuuint64_t)nb};
+    cuuint64_t strides[2] = {(cuuint64_t)(ld_elems * esz), (cuuint64_t)sbb};
+    cuuint32_t box[3] = {(cuuint32_t)(128 / esz), (cuuint32_t)box_rows, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = fn(map, bf ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
                     const_cast<void *>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                     CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -311,16 +327,18 @@ static int make_operand_map(CUtensorMap *map, const void *base, int64_t rows, in
     return FLG_OK;
 }
 
-// C map: m x nc FP32 (row stride ldc), 32 x 32 boxes, 128B swizzle (the epilogue's staging layout)
-static int make_c_map(CUtensorMap *map, float *C, int64_t m, int64_t nc, int64_t ldc) {
+// C map: nb systems (stride sb elements) of m x nc FP32 (row stride ldc), 32 x 32 x 1 boxes,
+// 128B swizzle (the epilogue's staging layout)
+static int make_c_map(CUtensorMap *map, float *C, int64_t m, int64_t nc, int64_t ldc, int nb = 1, int64_t sb = 0) {
     auto fn = encode_fn();
     FLG_REQUIRE(fn != nullptr, "cuTensorMapEncodeTiled unavailable");
-    FLG_REQUIRE(((uintptr_t)C & 15) == 0 && (ldc * 4) % 16 == 0, "C not 16-byte aligned");
-    cuuint64_t dims[2] = {(cuuint64_t)nc, (cuuint64_t)m};
-    cuuint64_t strides[1] = {(cuuint64_t)(ldc * 4)};
-    cuuint32_t box[2] = {32, 32};
-    cuuint32_t estr[2] = {1, 1};
-    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, C, dims, strides, box, estr,
+    const int64_t sbb = system_stride_bytes(nb, sb, m, ldc, 4);
+    FLG_REQUIRE(((uintptr_t)C & 15) == 0 && (ldc * 4) % 16 == 0 && sbb % 16 == 0, "C not 16-byte aligned");
+    cuuint64_t dims[3] = {(cuuint64_t)nc, (cuuint64_t)m, (cuuint64_t)nb};
+    cuuint64_t strides[2] = {(cuuint64_t)(ldc * 4), (cuuint64_t)sbb};
+    cuuint32_t box[3] = {32, 32, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, C, dims, strides, box, estr,
                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     FLG_REQUIRE(r == CUDA_SUCCESS, "cuTensorMapEncodeTiled failed for C (%d)", (int)r);
@@ -360,12 +378,12 @@ static int sm_count_of_current_device() {
     return cached[dev];
 }
 
-size_t tc_update_bytes(int64_t m, int64_t nc, int64_t K, int mode) {
+size_t tc_update_bytes(int64_t m, int64_t nc, int64_t K, int mode, int nb) {
     CountingArena c;
     c.take<int>(1);
     if (mode == FLG_LU_BF16) {
-        c.take<__nv_bfloat16>((size_t)m * K);
-        c.take<__nv_bfloat16>((size_t)nc * K);
+        c.take<__nv_bfloat16>((size_t)nb * m * K);
+        c.take<__nv_bfloat16>((size_t)nb * nc * K);
     }
     return c.bytes();
 }
@@ -374,25 +392,25 @@ size_t tc_update_bytes(int64_t m, int64_t nc, int64_t K, int mode) {
 // least time, a 128 x BN tile costing about (128 + BN) units (operand bytes per
 // K-block).  BN = 256 reads 25 % fewer operand bytes per output; BN = 128 gives
 // twice the tiles for small updates and wastes nothing on updates of 128 columns.
-int tc_pick_tile(int64_t m, int64_t nc, int sms) {
-    const int64_t ty = ceil_div(m, TC_BM);
+int tc_pick_tile(int64_t m, int64_t nc, int sms, int nb = 1) {
+    const int64_t ty = nb * ceil_div(m, TC_BM);
     const int64_t w256 = ceil_div(ty * ceil_div(nc, 256), sms), w128 = ceil_div(ty * ceil_div(nc, 128), sms);
     return w128 * (128 + 128) < w256 * (128 + 256) ? 128 : 256;
 }
 
 template <int MODE, int BN>
 static int tc_launch(const CUtensorMap &ma, const CUtensorMap &mb, const CUtensorMap &mc, int64_t m, int64_t nc,
-                     int nkb, bool store, int *err, int sms, cudaStream_t st) {
+                     int nkb, int nb, bool store, int *err, int sms, cudaStream_t st) {
     static bool attr_set = false;  // set once, so a later call can be captured in a graph
     if (!attr_set) {
         FLG_CUDA(cudaFuncSetAttribute(tc_update_kernel<MODE, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)TcTile<BN>::SMEM));
         attr_set = true;
     }
-    const int64_t ntiles = ceil_div(m, TC_BM) * ceil_div(nc, BN);
+    const int64_t ntiles = nb * ceil_div(m, TC_BM) * ceil_div(nc, BN);
     FLG_REQUIRE(ntiles < (1LL << 31), "too many tiles");
     const unsigned grid = (unsigned)std::min<int64_t>(ntiles, sms);
-    tc_update_kernel<MODE, BN><<<grid, TC_THREADS, TcTile<BN>::SMEM, st>>>(ma, mb, mc, (int)m, (int)nc, nkb,
+    tc_update_kernel<MODE, BN><<<grid, TC_THREADS, TcTile<BN>::SMEM, st>>>(ma, mb, mc, (int)m, (int)nc, nkb, nb,
                                                                            store ? 1 : 0, err);
     FLG_LAUNCH_CHECK();
     return FLG_OK;
@@ -402,46 +420,50 @@ static int tc_launch(const CUtensorMap &ma, const CUtensorMap &mb, const CUtenso
 // the workspace and the call synchronizes to check it; the LU passes its own
 // flag and checks it once at the end of the factorization.  tile: 0 picks the
 // tile width (tc_pick_tile), 128 or 256 forces it.  max_ctas > 0 caps the
-// persistent grid (leaving SMs to work on another stream).
+// persistent grid (leaving SMs to work on another stream).  bt: the same update
+// of bt.count systems, C, Lp and Ut of system z at + z * (bt.sC, bt.sL, bt.sU).
 int tc_update(float *C, int64_t ldc, const float *Lp, int64_t ldl, const float *Ut, int64_t ldu, int64_t m,
               int64_t nc, int64_t K, int mode, void *work, size_t work_bytes, cudaStream_t st, int *err_dev,
-              bool store, int tile, int max_ctas) {
+              bool store, int tile, int max_ctas, const TcBatch &bt) {
     FLG_REQUIRE(mode == FLG_LU_TF32 || mode == FLG_LU_BF16, "tensor-core mode must be TF32 or BF16");
     FLG_REQUIRE(m >= 0 && nc >= 0 && m < (1LL << 31) && nc < (1LL << 31), "bad tensor-core update shape");
+    FLG_REQUIRE(bt.count >= 1 && bt.count <= 65535, "bad batch count %d", bt.count);
+    const int nb = bt.count;
     FLG_REQUIRE(K > 0 && K % 128 == 0 && K <= (1 << 20), "tensor-core update depth must be a multiple of 128");
     FLG_REQUIRE(tile == 0 || tile == 128 || tile == 256, "tile width must be 128 or 256 (or 0 to choose)");
     if (m == 0 || nc == 0) return FLG_OK;
     const int sms = max_ctas > 0 ? std::min(max_ctas, sm_count_of_current_device()) : sm_count_of_current_device();
-    const int bn = tile ? tile : tc_pick_tile(m, nc, sms);
+    const int bn = tile ? tile : tc_pick_tile(m, nc, sms, nb);
     Arena ar(work, work_bytes);
     int *own = ar.take<int>(1);
     int *err = err_dev ? err_dev : own;
     FLG_REQUIRE(err != nullptr && own != nullptr, "workspace too small for the tensor-core update");
     CUtensorMap ma, mb, mc;
     if (mode == FLG_LU_TF32) {
-        FLG_TRY(make_operand_map(&ma, Lp, m, K, ldl, mode, TC_BM));
-        FLG_TRY(make_operand_map(&mb, Ut, nc, K, ldu, mode, bn));
+        FLG_TRY(make_operand_map(&ma, Lp, m, K, ldl, mode, TC_BM, nb, bt.sL));
+        FLG_TRY(make_operand_map(&mb, Ut, nc, K, ldu, mode, bn, nb, bt.sU));
     } else {
-        __nv_bfloat16 *La = ar.take<__nv_bfloat16>((size_t)m * K);
-        __nv_bfloat16 *Ub = ar.take<__nv_bfloat16>((size_t)nc * K);
+        __nv_bfloat16 *La = ar.take<__nv_bfloat16>((size_t)nb * m * K);
+        __nv_bfloat16 *Ub = ar.take<__nv_bfloat16>((size_t)nb * nc * K);
         FLG_REQUIRE(La && Ub, "workspace too small for the BF16 operands");
-        f32_to_bf16_rows_kernel<<<(unsigned)ceil_div(m * K, 256), 256, 0, st>>>(Lp, ldl, La, m, K);
+        f32_to_bf16_rows_kernel<<<dim3((unsigned)ceil_div(m * K, 256), nb), 256, 0, st>>>(Lp, ldl, bt.sL, La, m, K);
         FLG_LAUNCH_CHECK();
-        f32_to_bf16_rows_kernel<<<(unsigned)ceil_div(nc * K, 256), 256, 0, st>>>(Ut, ldu, Ub, nc, K);
+        f32_to_bf16_rows_kernel<<<dim3((unsigned)ceil_div(nc * K, 256), nb), 256, 0, st>>>(Ut, ldu, bt.sU, Ub, nc,
+                                                                                             K);
         FLG_LAUNCH_CHECK();
-        FLG_TRY(make_operand_map(&ma, La, m, K, K, mode, TC_BM));
-        FLG_TRY(make_operand_map(&mb, Ub, nc, K, K, mode, bn));
+        FLG_TRY(make_operand_map(&ma, La, m, K, K, mode, TC_BM, nb, m * K));
+        FLG_TRY(make_operand_map(&mb, Ub, nc, K, K, mode, bn, nb, nc * K));
     }
-    FLG_TRY(make_c_map(&mc, C, m, nc, ldc));
+    FLG_TRY(make_c_map(&mc, C, m, nc, ldc, nb, bt.sC));
     if (!err_dev) FLG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
     const int nkb = (int)(K / (mode == FLG_LU_TF32 ? 32 : 64));
     int rc;
     if (mode == FLG_LU_TF32)
-        rc = bn == 128 ? tc_launch<FLG_LU_TF32, 128>(ma, mb, mc, m, nc, nkb, store, err, sms, st)
-                       : tc_launch<FLG_LU_TF32, 256>(ma, mb, mc, m, nc, nkb, store, err, sms, st);
+        rc = bn == 128 ? tc_launch<FLG_LU_TF32, 128>(ma, mb, mc, m, nc, nkb, nb, store, err, sms, st)
+                       : tc_launch<FLG_LU_TF32, 256>(ma, mb, mc, m, nc, nkb, nb, store, err, sms, st);
     else
-        rc = bn == 128 ? tc_launch<FLG_LU_BF16, 128>(ma, mb, mc, m, nc, nkb, store, err, sms, st)
-                       : tc_launch<FLG_LU_BF16, 256>(ma, mb, mc, m, nc, nkb, store, err, sms, st);
+        rc = bn == 128 ? tc_launch<FLG_LU_BF16, 128>(ma, mb, mc, m, nc, nkb, nb, store, err, sms, st)
+                       : tc_launch<FLG_LU_BF16, 256>(ma, mb, mc, m, nc, nkb, nb, store, err, sms, st);
     FLG_TRY(rc);
     if (err_dev) return FLG_OK;
     int herr = 0;
@@ -457,7 +479,7 @@ int tc_update(float *C, int64_t ldc, const float *Lp, int64_t ldl, const float *
 }  // namespace flg
 
 extern "C" size_t flg_tc_rank_update_workspace(int64_t m, int64_t nc, int mode) {
-    return flg::tc_update_bytes(m, nc, 128, mode);
+    return flg::tc_update_bytes(m, nc, 128, mode, 1);
 }
 
 extern "C" int flg_tc_rank_update(float *C, int64_t ldc, const float *A, int64_t lda, const float *Bt, int64_t ldb,
@@ -466,5 +488,5 @@ extern "C" int flg_tc_rank_update(float *C, int64_t ldc, const float *A, int64_t
     FLG_REQUIRE(ldb == 128, "Bt must be compact (ldb == 128)");
     FLG_REQUIRE(lda >= 128 && ldc >= nc, "bad leading dimensions");
     return flg::tc_update(C, ldc, A, lda, Bt, 128, m, nc, 128, mode, work, work_bytes, flg::as_stream(stream), nullptr,
-                          false, 0, 0);
+                          false, 0, 0, flg::TcBatch{});
 }

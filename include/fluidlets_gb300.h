@@ -168,6 +168,16 @@ int flg_assemble_bucket(int kind, double alpha_re, double alpha_im, const double
 int flg_assemble_bucket_uniform(int kind, double alpha_re, double alpha_im, const double *points, const double *eps,
                                 const int64_t *n_real, int64_t n_cap, double mu_re, void *out, int out_type,
                                 int64_t ld, void *stream);
+/* nbat systems of one bucket in one launch: system z has its points at
+ * points + 3 z n_cap, its blob widths at eps + z n_cap, its real count at
+ * n_real[z] (device) and its matrix at out + z stride_out elements
+ * (stride_out >= 3 n_cap ld); uniform_eps != 0 selects the symmetric form of
+ * flg_assemble_bucket_uniform (eps[z n_cap] for system z).  Each system's matrix
+ * is bit-identical to its own flg_assemble_bucket(_uniform) call.  No
+ * counterpart in the reference. */
+int flg_assemble_bucket_batched(int kind, double alpha_re, double alpha_im, const double *points, const double *eps,
+                                int uniform_eps, const int64_t *n_real, int64_t n_cap, int nbat, double mu_re,
+                                void *out, int out_type, int64_t ld, int64_t stride_out, void *stream);
 
 /* Replaces fluidlets.assemble_nearest (core/assemble.py:68-101) and
  * _fill_nearest (49-58): K[:, group j] = sum_{k: nearest[k] = j} G(x_i, X_k)/mu.
@@ -246,6 +256,19 @@ int flg_lu_factor_lowp(int64_t n, float *A, int64_t ld, int mode, float *dinv, i
  * timed out) for the caller to check after the stream. */
 int flg_lu_factor_lowp_async(int64_t n, float *A, int64_t ld, int mode, float *dinv, int *flags,
                              void *work, size_t work_bytes, void *stream);
+/* The same for nbat (1 .. 64) independent systems of order n in one sequence
+ * of launches: system z at A + z stride_a (stride_a >= n ld, a multiple of 4),
+ * its block inverses at dinv + z flg_lu_lowp_dinv_elems(n), its flags at
+ * flags[2 z], flags[2 z + 1] (2 nbat ints; flags[1] also reports a timed-out
+ * tensor-core wait of any system).  Every kernel of a step covers all systems:
+ * the diagonal blocks as one CTA per system, the panels and trailing updates
+ * as one tensor-core launch over the tiles of all systems (3-D tensor maps,
+ * the system index outermost).  Tensor-core modes only (TF32 / BF16, with or
+ * without a tile-width bit).  Each system's factors are bit-identical to its
+ * own flg_lu_factor_lowp_async call.  No counterpart in the reference. */
+size_t flg_lu_factor_lowp_batched_workspace(int64_t n, int nbat, int mode);
+int flg_lu_factor_lowp_batched_async(int64_t n, int nbat, float *A, int64_t ld, int64_t stride_a, int mode,
+                                     float *dinv, int *flags, void *work, size_t work_bytes, void *stream);
 /* x = (L U)^{-1} b in FP32 for one FP64 right-hand side (converted on the
  * fly), result written as FP64: one cooperative launch, a dataflow over the
  * 128-row blocks with bounded waits (a timed-out wait makes x NaN). */
@@ -316,6 +339,18 @@ int flg_bucket_graph_create(int kind, double alpha_re, double alpha_im, const do
                             float *A32, float *K32,
                             int64_t ld32, int mode, float *dinv, int *flags, void *work, size_t work_bytes,
                             void *stream, void **graph_exec);
+/* The batched form of flg_bucket_graph_create: nbat systems of one bucket
+ * (points, eps, n_real laid out as in flg_assemble_bucket_batched), K system z
+ * at K + z 9 n_cap^2 (ld 3 n_cap), A32 / K32 system z at + z 3 n_cap ld32,
+ * dinv and flags as in flg_lu_factor_lowp_batched_async, workspace
+ * flg_lu_factor_lowp_batched_workspace(3 n_cap, nbat, mode).  One graph:
+ * flg_assemble_bucket_batched -> one FP32 conversion pass over all systems ->
+ * flg_lu_factor_lowp_batched_async.  No counterpart in the reference. */
+int flg_bucket_batch_graph_create(int kind, double alpha_re, double alpha_im, const double *points,
+                                  const double *eps, int uniform_eps, const int64_t *n_real, int64_t n_cap, int nbat,
+                                  double mu_re, double *K, float *A32, float *K32, int64_t ld32, int mode,
+                                  float *dinv, int *flags, void *work, size_t work_bytes, void *stream,
+                                  void **graph_exec);
 /* The FP32 copies (flg_convert_f64_f32x2) and the tensor-core LU
  * (flg_lu_factor_lowp_async) of an assembled FP64 K as one captured graph over
  * fixed buffers (replay with flg_graph_launch; flags as in
