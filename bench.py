@@ -56,6 +56,8 @@ def parse():
     p.add_argument("--fp64", action="store_true", help="also run the plain FP64 GPU solve (slow at full size)")
     p.add_argument("--slots", type=int, default=6, help="solve-server slots (serve workload)")
     p.add_argument("--rates", default="50,200,800", help="Poisson arrival rates (serve workload)")
+    p.add_argument("--batch", type=int, default=4, help="most same-bucket requests per batched factorization "
+                                                        "(serve workload)")
     # one hot-path operation at a chosen size, for profiler captures (no JSON line)
     p.add_argument("--case", default=None, choices=["sum", "assemble", "lu", "resistance", "breakdown", "swim"],
                    help="run one operation at a chosen size for a profiler capture instead of the benchmark")

@@ -92,6 +92,7 @@ class Result:
     bucket: int = 0
     lu: str = ""
     ir_steps: int = 0
+    batch: int = 1              # requests factored together with this one (one batched graph)
 
     @property
     def latency(self) -> float:
@@ -105,165 +106,241 @@ def plan_bytes(nb_points: int) -> int:
 
 
 class BucketPlan:
-    """Device buffers and the captured assemble + factor graph of one bucket size."""
+    """Device buffers and captured graphs of one bucket size for up to `cap` systems.
 
-    def __init__(self, kernel, nb_points: int, mu: float, lu: str, stream, uniform: bool = False):
+    System z of a group has its own slice of every buffer (points, blob widths, real count,
+    K, the FP32 copies, the block inverses, flags, right-hand side, solution).  A group of
+    k <= cap requests of the bucket replays one captured graph of k systems: one batched
+    assembly launch, one FP32 conversion pass, and the batched tensor-core LU, whose steps
+    each cover all k systems.  Each system is then refined by its own captured FP64
+    refinement graph.  cap = 1 (and the FP32 LU, which is not batched) captures the
+    single-system graph."""
+
+    def __init__(self, kernel, nb_points: int, mu: float, lu: str, stream, uniform: bool = False, cap: int = 1):
         L = load()
         self.kernel, self.mu, self.lu, self.nbp = kernel, mu, lu, nb_points
         self.uniform = uniform  # one blob width for every point: the symmetric assembly, half the pairs
         self.kind, self.are, self.aim = kernel_params(kernel)
+        self.cap = 1 if lu.startswith("fp32") else max(1, int(cap))
         dev = torch.device("cuda", torch.cuda.current_device())
         n = 3 * nb_points
+        c = self.cap
         self.n = n
         self.ld32 = (n + 31) // 32 * 32
-        self.pts = torch.zeros((nb_points, 3), dtype=torch.float64, device=dev)
-        self.eps = torch.ones(nb_points, dtype=torch.float64, device=dev)
-        self.n_real = torch.zeros(1, dtype=torch.int64, device=dev)
-        self.K = torch.empty((n, n), dtype=torch.float64, device=dev)
-        self.K32 = torch.empty((n, self.ld32), dtype=torch.float32, device=dev)
-        self.A32 = torch.empty((n, self.ld32), dtype=torch.float32, device=dev)  # inner GMRES matvecs
-        self.dinv = torch.empty(L.flg_lu_lowp_dinv_elems(n), dtype=torch.float32, device=dev)
-        self.flags = torch.zeros(2, dtype=torch.int32, device=dev)
+        self.pts = torch.zeros((c, nb_points, 3), dtype=torch.float64, device=dev)
+        self.eps = torch.ones((c, nb_points), dtype=torch.float64, device=dev)
+        self.n_real = torch.zeros(c, dtype=torch.int64, device=dev)
+        self.K = torch.empty((c, n, n), dtype=torch.float64, device=dev)
+        self.K32 = torch.empty((c, n, self.ld32), dtype=torch.float32, device=dev)
+        self.A32 = torch.empty((c, n, self.ld32), dtype=torch.float32, device=dev)  # inner GMRES matvecs
+        self.dinv = torch.empty((c, L.flg_lu_lowp_dinv_elems(n)), dtype=torch.float32, device=dev)
+        self.flags = torch.zeros((c, 2), dtype=torch.int32, device=dev)
         mode = lu_mode(lu)
         # sized for either tensor-core precision, so the autotuner can switch modes on one plan
-        self.lu_bytes = max(L.flg_lu_factor_lowp_workspace(n, LU_MODE[m]) for m in ("tf32", "bf16"))
+        if c == 1:
+            self.lu_bytes = max(L.flg_lu_factor_lowp_workspace(n, LU_MODE[m]) for m in ("tf32", "bf16"))
+        else:
+            self.lu_bytes = max(L.flg_lu_factor_lowp_batched_workspace(n, c, LU_MODE[m]) for m in ("tf32", "bf16"))
         self.lu_ws = dv.workspace(self.lu_bytes)
-        self.b = torch.zeros(n, dtype=torch.float64, device=dev)
-        self.x = torch.zeros(n, dtype=torch.float64, device=dev)
-        self.graph = None
-        self.ir = None
+        self.b = torch.zeros((c, n), dtype=torch.float64, device=dev)
+        self.x = torch.zeros((c, n), dtype=torch.float64, device=dev)
+        self.graphs = {}  # systems in the group -> captured graph
+        self.irs = []     # per system: the captured refinement (after capture())
         self.rtol_ir = 1e-12  # the refinement's target: rtol / 100 for the server's rtol 1e-10
         self.stream = stream
         self.mode = mode
+        self.count = 0    # systems of the current group
 
-    def _run(self):
+    @property
+    def graph(self):
+        """The graph of a single system (None before capture() or when capture failed)."""
+        return self.graphs.get(1)
+
+    def _st(self):
+        return ctypes.c_void_p(self.stream.cuda_stream)
+
+    def _run(self, k: int):
         L = load()
-        st = ctypes.c_void_p(self.stream.cuda_stream)
-        asm = L.flg_assemble_bucket_uniform if self.uniform else L.flg_assemble_bucket
-        check(asm(self.kind, self.are, self.aim, dv.ptr(self.pts), dv.ptr(self.eps),
-                                    dv.ptr(self.n_real), self.nbp, float(self.mu), dv.ptr(self.K), F64, self.n, st),
-              "bucket assembly")
-        check(L.flg_convert_f64_f32x2(self.n, self.n, dv.ptr(self.K), self.n, dv.ptr(self.K32), dv.ptr(self.A32),
-                                      self.ld32, st), "convert")
-        check(L.flg_lu_factor_lowp_async(self.n, dv.ptr(self.K32), self.ld32, self.mode, dv.ptr(self.dinv),
-                                         dv.ptr(self.flags), dv.ptr(self.lu_ws), self.lu_bytes, st), "LU")
+        st = self._st()
+        n = self.n
+        if self.cap == 1:
+            asm = L.flg_assemble_bucket_uniform if self.uniform else L.flg_assemble_bucket
+            check(asm(self.kind, self.are, self.aim, dv.ptr(self.pts), dv.ptr(self.eps), dv.ptr(self.n_real),
+                      self.nbp, float(self.mu), dv.ptr(self.K), F64, n, st), "bucket assembly")
+        else:
+            check(L.flg_assemble_bucket_batched(self.kind, self.are, self.aim, dv.ptr(self.pts), dv.ptr(self.eps),
+                                                int(self.uniform), dv.ptr(self.n_real), self.nbp, k, float(self.mu),
+                                                dv.ptr(self.K), F64, n, n * n, st), "bucket assembly")
+        check(L.flg_convert_f64_f32x2(k * n, n, dv.ptr(self.K), n, dv.ptr(self.K32), dv.ptr(self.A32), self.ld32,
+                                      st), "convert")
+        if self.cap == 1:
+            check(L.flg_lu_factor_lowp_async(n, dv.ptr(self.K32), self.ld32, self.mode, dv.ptr(self.dinv),
+                                             dv.ptr(self.flags), dv.ptr(self.lu_ws), self.lu_bytes, st), "LU")
+        else:
+            check(L.flg_lu_factor_lowp_batched_async(n, k, dv.ptr(self.K32), self.ld32, n * self.ld32, self.mode,
+                                                     dv.ptr(self.dinv), dv.ptr(self.flags), dv.ptr(self.lu_ws),
+                                                     self.lu_bytes, st), "batched LU")
 
     def set_lu(self, lu: str):
         """Switch the LU mode of an uncaptured plan (the autotuner's candidates)."""
-        if self.graph is not None:
+        if self.graphs:
             raise RuntimeError("the LU mode of a captured plan is fixed")
+        if self.cap > 1 and lu.startswith("fp32"):
+            raise ValueError("the FP32 LU is not batched")
         self.lu, self.mode = lu, lu_mode(lu)
+
+    def _capture_group(self, k: int):
+        L = load()
+        h = ctypes.c_void_p(0)
+        args = (self.kind, self.are, self.aim, dv.ptr(self.pts), dv.ptr(self.eps), int(self.uniform),
+                dv.ptr(self.n_real), self.nbp)
+        tail = (float(self.mu), dv.ptr(self.K), dv.ptr(self.A32), dv.ptr(self.K32), self.ld32, self.mode,
+                dv.ptr(self.dinv), dv.ptr(self.flags), dv.ptr(self.lu_ws), self.lu_bytes, self._st(), ctypes.byref(h))
+        if self.cap == 1:
+            st = L.flg_bucket_graph_create(*args, *tail)
+        else:
+            st = L.flg_bucket_batch_graph_create(*args, k, *tail)
+        if st != 0 or not h.value:
+            raise RuntimeError(L.flg_last_error().decode(errors="replace"))
+        self.graphs[k] = h.value
 
     def capture(self):
         """Capture assembly -> FP32 copy -> tensor-core LU as a CUDA graph (in the library,
-        thread-local capture mode); on failure the plan stays eager."""
-        L = load()
-        h = ctypes.c_void_p(0)
-        st = L.flg_bucket_graph_create(self.kind, self.are, self.aim, dv.ptr(self.pts), dv.ptr(self.eps),
-                                       int(self.uniform),
-                                       dv.ptr(self.n_real), self.nbp, float(self.mu), dv.ptr(self.K), dv.ptr(self.A32),
-                                       dv.ptr(self.K32),
-                                       self.ld32, self.mode, dv.ptr(self.dinv), dv.ptr(self.flags), dv.ptr(self.lu_ws),
-                                       self.lu_bytes, ctypes.c_void_p(self.stream.cuda_stream), ctypes.byref(h))
-        if st == 0 and h.value:
-            self.graph = h.value
-            # the refinement as a second graph over the same buffers (conditional loops steered
-            # on the device): a request then costs one host synchronization, at the end
-            from .core import IrGraph
+        thread-local capture mode) for every group size up to cap, and each system's
+        refinement.  On failure the plan stays eager."""
+        try:
+            for k in range(1, self.cap + 1):
+                self._capture_group(k)
+        except RuntimeError as e:
+            self.capture_error = str(e)
+            for h in self.graphs.values():
+                load().flg_graph_destroy(ctypes.c_void_p(h))
+            self.graphs = {}
+            return
+        # the refinement as a second graph over the same buffers (conditional loops steered
+        # on the device): a request then costs one host synchronization, at the end
+        from .core import IrGraph
 
-            try:
-                self.ir = IrGraph(self.K, self.A32, self.K32, self.ld32, self.dinv, self.b, self.x,
-                                  self.rtol_ir, stream=self.stream)
-            except (RuntimeError, ValueError) as e:
-                self.ir = None
-                self.capture_error = str(e)
-        else:
-            self.graph = None
-            self.capture_error = L.flg_last_error().decode(errors="replace")
+        try:
+            self.irs = [IrGraph(self.K[z], self.A32[z], self.K32[z], self.ld32, self.dinv[z], self.b[z], self.x[z],
+                                self.rtol_ir, stream=self.stream) for z in range(self.cap)]
+        except (RuntimeError, ValueError) as e:
+            for ir in self.irs:
+                ir.close()
+            self.irs = []
+            self.capture_error = str(e)
 
     def __del__(self):
-        if getattr(self, "ir", None) is not None:
-            self.ir.close()
-        if getattr(self, "graph", None):
+        for ir in getattr(self, "irs", []):
+            ir.close()
+        for h in getattr(self, "graphs", {}).values():
             try:
-                load().flg_graph_destroy(ctypes.c_void_p(self.graph))
+                load().flg_graph_destroy(ctypes.c_void_p(h))
             except Exception:  # noqa: BLE001 - interpreter shutdown
                 pass
 
     def factor(self, X: torch.Tensor, eps: torch.Tensor):
-        N = X.shape[0]
-        self.pts[:N].copy_(X)
-        self.eps[:N].copy_(eps)
-        self.n_real.fill_(N)
-        if self.graph is not None:
-            check(load().flg_graph_launch(ctypes.c_void_p(self.graph), ctypes.c_void_p(self.stream.cuda_stream)),
-                  "graph launch")
-        else:
-            self._run()
+        self.factor_group([(X, eps)])
 
-    def solve(self, U: torch.Tensor, rtol: float, restart: int = 60, maxiter: int = 200):
-        if getattr(self, "ir", None) is not None and rtol * 1e-2 == self.rtol_ir:
-            return self._solve_graph(U, rtol)
-        L = load()
-        N = U.shape[0]
-        self.b.zero_()
-        self.b[:3 * N].copy_(U.reshape(-1))
-        self.x.zero_()
-        flags = self.flags.cpu()
-        if int(flags[1]):
+    def factor_group(self, items):
+        """Factor the systems of a group of k <= cap requests ((points, blob widths) each):
+        one replay of the k-system graph (captured on first use), or the eager sequence."""
+        k = len(items)
+        if not 1 <= k <= self.cap:
+            raise ValueError(f"a group of {k} systems on a plan of {self.cap}")
+        Ns = []
+        for z, (X, eps) in enumerate(items):
+            N = X.shape[0]
+            self.pts[z, :N].copy_(X)
+            self.eps[z, :N].copy_(eps)
+            Ns.append(N)
+        if k == 1:
+            self.n_real[:1].fill_(Ns[0])
+        else:
+            self.n_real[:k].copy_(torch.tensor(Ns, dtype=torch.int64), non_blocking=False)
+        self.count = k
+        if self.graph is not None:
+            if k not in self.graphs:
+                self._capture_group(k)
+            check(load().flg_graph_launch(ctypes.c_void_p(self.graphs[k]), self._st()), "graph launch")
+        else:
+            self._run(k)
+
+    def _flags(self, z):
+        flags = self.flags[z].cpu()
+        if int(flags[1]) or int(self.flags[0, 1]):
             raise RuntimeError("low-precision LU: a bounded device wait timed out")
         if int(flags[0]):
             raise np.linalg.LinAlgError(f"zero pivot at row {int(flags[0]) - 1} in the low-precision LU")
+
+    def solve(self, U: torch.Tensor, rtol: float, restart: int = 60, maxiter: int = 200, z: int = 0):
+        if self.irs and rtol * 1e-2 == self.rtol_ir:
+            return self._solve_graph(U, rtol, z)
+        L = load()
+        N = U.shape[0]
+        b, x = self.b[z], self.x[z]
+        b.zero_()
+        b[:3 * N].copy_(U.reshape(-1))
+        x.zero_()
+        self._flags(z)
         nbytes = L.flg_gmres_ir_dense_workspace(self.n, restart)
         ws = dv.workspace(nbytes)
         iters, outer, resid = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_double(0.0)
         from .core import _accept
 
-        st = L.flg_gmres_ir_dense(self.n, dv.ptr(self.K), self.n, dv.ptr(self.A32), self.ld32, dv.ptr(self.K32),
-                                  self.ld32, dv.ptr(self.dinv),
-                                  dv.ptr(self.b), dv.ptr(self.x), rtol * 1e-2, restart, maxiter, ctypes.byref(iters),
-                                  ctypes.byref(outer), ctypes.byref(resid), dv.ptr(ws), nbytes,
-                                  ctypes.c_void_p(self.stream.cuda_stream))
+        st = L.flg_gmres_ir_dense(self.n, dv.ptr(self.K[z]), self.n, dv.ptr(self.A32[z]), self.ld32,
+                                  dv.ptr(self.K32[z]), self.ld32, dv.ptr(self.dinv[z]), dv.ptr(b), dv.ptr(x),
+                                  rtol * 1e-2, restart, maxiter, ctypes.byref(iters), ctypes.byref(outer),
+                                  ctypes.byref(resid), dv.ptr(ws), nbytes, self._st())
         _accept(st, resid.value, rtol, "GMRES-IR")
-        return self.x[:3 * N].reshape(N, 3).clone(), iters.value, outer.value, resid.value
+        return x[:3 * N].reshape(N, 3).clone(), iters.value, outer.value, resid.value
 
+    def _solve_graph(self, U: torch.Tensor, rtol: float, z: int):
+        """The captured refinement of system z: one replay, then the LU's flags and the
+        refinement's outcome."""
+        self.launch_refinement(U, z)
+        return self.refinement_result(U.shape[0], rtol, z)
 
-    def _solve_graph(self, U: torch.Tensor, rtol: float):
-        """The captured refinement: one replay, then the LU's flags and the refinement's outcome."""
+    def launch_refinement(self, U: torch.Tensor, z: int):
+        N = U.shape[0]
+        b = self.b[z]
+        b.zero_()
+        b[:3 * N].copy_(U.reshape(-1))
+        self.irs[z].launch(self.stream)
+
+    def refinement_result(self, N: int, rtol: float, z: int):
         from .core import _accept
 
-        N = U.shape[0]
-        self.b.zero_()
-        self.b[:3 * N].copy_(U.reshape(-1))
-        self.ir.launch(self.stream)
-        st, it, outer, resid = self.ir.result(self.stream)
-        flags = self.flags.cpu()
-        if int(flags[1]):
-            raise RuntimeError("low-precision LU: a bounded device wait timed out")
-        if int(flags[0]):
-            raise np.linalg.LinAlgError(f"zero pivot at row {int(flags[0]) - 1} in the low-precision LU")
+        st, it, outer, resid = self.irs[z].result(self.stream)
+        self._flags(z)
         _accept(st, resid, rtol, "GMRES-IR")
-        return self.x[:3 * N].reshape(N, 3).clone(), it, outer, resid
+        return self.x[z, :3 * N].reshape(N, 3).clone(), it, outer, resid
 
 
 class SolveServer:
     """Continuous-batching server: submit() returns a Future of a Result.
 
     Bucket plans live in a shared pool, counted against the HBM budget: a
-    plan is checked out by one slot for one request and then returned; free
-    plans are evicted least-recently-used when a new plan or a swimmer system
-    needs the memory.  The scheduler takes the oldest request, preferring,
-    within a look-ahead window, one whose bucket has a free plan."""
+    plan is checked out by one slot for one group of requests and then
+    returned; free plans are evicted least-recently-used when a new plan or a
+    swimmer system needs the memory.  The scheduler takes the oldest request,
+    preferring, within a look-ahead window, one whose bucket has a free plan,
+    and adds up to `batch` - 1 pending requests of the same plan key (kernel,
+    bucket, mu, LU mode, one blob width or not) for buckets of at most
+    `batch_points` points: the group is factored by one replay of the batched
+    graph.  Nothing waits for a group to fill."""
 
     def __init__(self, slots: int = 6, hbm_budget_gb: float = 150.0, rtol: float = 1e-10, graphs: bool = True,
-                 lu: str = "auto", lookahead: int = 16):
+                 lu: str = "auto", lookahead: int = 16, batch: int = 4, batch_points: int = 2304):
         self.slots = slots
         self.budget = int(hbm_budget_gb * 2**30)
         self.rtol = rtol
         self.graphs = graphs
         self.lu = lu
         self.lookahead = lookahead
-        self._pending = []            # [(request, future, t_arrival, bucket)]
+        self.batch = max(1, int(batch))
+        self.batch_points = batch_points
+        self._pending = []            # [(request, future, t_arrival, bucket, group key)]
         self._cv = threading.Condition()
         self._used = 0                # bytes of pooled plans + in-flight swimmer systems
         self._free = {}               # plan key -> [free BucketPlan], most recently used last
@@ -272,7 +349,7 @@ class SolveServer:
         self._tuned = {}              # (kernel kind, bucket) -> LU mode name, e.g. "tf32:256"
         self._closed = False
         self.stats = {"graph_replays": 0, "eager_factors": 0, "captures": 0, "capture_errors": [], "plans_built": 0,
-                      "plans_evicted": 0, "tuned": {}}
+                      "plans_evicted": 0, "tuned": {}, "groups": {}}
         self._dev = self._device()
         self._threads = [threading.Thread(target=self._worker, args=(s,), daemon=True) for s in range(slots)]
         for t in self._threads:
@@ -283,8 +360,9 @@ class SolveServer:
         fut = Future()
         t = time.perf_counter() if t_arrival is None else t_arrival
         b = bucket_of(len(req.points)) if isinstance(req, ResistanceRequest) else 0
+        g = self._group_key(req, b)
         with self._cv:
-            self._pending.append((req, fut, t, b))
+            self._pending.append((req, fut, t, b, g))
             self._cv.notify_all()
         return fut
 
@@ -312,6 +390,22 @@ class SolveServer:
         return ("swim", kind, len(req.shape.x), len(req.shape.X), float(req.eps), float(req.mu))
 
     @staticmethod
+    def _group_key(req, b):
+        """Requests with equal group keys run on the same plan key (the LU mode is tuned per
+        kernel and bucket), so they can share a batched plan; None: never grouped."""
+        if not isinstance(req, ResistanceRequest):
+            return None
+        return (kernel_params(req.kernel)[0], b, float(req.mu), _uniform(req.eps))
+
+    def _cap(self, key, b):
+        """Systems per plan of this key: `batch` for tuned tensor-core resistance plans of at
+        most `batch_points` points, else 1."""
+        if key[0] != "res" or self.batch == 1 or b > self.batch_points:
+            return 1
+        lu = key[4]
+        return 1 if lu == "tune" or lu.startswith("fp32") else self.batch
+
+    @staticmethod
     def _need(req, b):
         if isinstance(req, ResistanceRequest):
             return plan_bytes(b)
@@ -327,32 +421,41 @@ class SolveServer:
             self.stats["plans_evicted"] += 1
 
     def _pick(self, slot):
-        """Oldest admissible request, preferring one with a free plan within the look-ahead window.
-        Returns (request, future, t_arrival, bucket, plan or None, reserved bytes) or None."""
+        """Oldest admissible request, preferring one with a free plan within the look-ahead window,
+        plus pending requests of its group key up to the plan's capacity.
+        Returns ([(request, future, t_arrival)], bucket, plan or None, reserved bytes) or None."""
         cand = None
-        for k, (req, fut, t, b) in enumerate(self._pending[: self.lookahead]):
+        for k, (req, fut, t, b, g) in enumerate(self._pending[: self.lookahead]):
             if self._free.get(self._key(req, b)):
                 cand = k
                 break
         if cand is None:
             cand = 0
-        req, fut, t, b = self._pending[cand]
+        req, fut, t, b, g = self._pending[cand]
         key = self._key(req, b)
+        plan, reserved = None, 0
         if self._free.get(key):
             plan = self._free[key].pop()
             self._lru.remove(plan)
-            self._pending.pop(cand)
-            self._busy[slot] = True
-            return req, fut, t, b, plan, 0
-        need = self._need(req, b)
-        if self._used + need > self.budget:
-            self._evict_free(need)
-            if self._used + need > self.budget and any(self._busy):
-                return None  # wait until running requests release memory
-        self._pending.pop(cand)
-        self._used += need
+            cap = getattr(plan, "cap", 1)
+        else:
+            cap = self._cap(key, b)
+            need = self._need(req, b) * cap
+            if self._used + need > self.budget:
+                self._evict_free(need)
+                if self._used + need > self.budget and any(self._busy):
+                    return None  # wait until running requests release memory
+            self._used += need
+            reserved = need
+        group = [self._pending.pop(cand)[:3]]
+        k = 0
+        while len(group) < cap and k < len(self._pending):
+            if g is not None and self._pending[k][4] == g:
+                group.append(self._pending.pop(k)[:3])
+            else:
+                k += 1
         self._busy[slot] = True
-        return req, fut, t, b, None, need
+        return group, b, plan, reserved
 
     # ---- device hooks (overridden by the scheduler's CPU test) ---------------------------
     def _device(self):
@@ -363,11 +466,19 @@ class SolveServer:
         return torch.cuda.Stream()
 
     def _run_request(self, slot, stream, req, b, plan):
+        """One request alone: (Result, plan)."""
+        res, plan = self._run_group(slot, stream, [req], b, plan)
+        return res[0], plan
+
+    def _run_group(self, slot, stream, reqs, b, plan):
+        """A group of requests of one plan key (one request, or up to the plan's capacity):
+        ([Result per request], plan)."""
         with torch.cuda.stream(stream):
-            if isinstance(req, ResistanceRequest):
-                res, plan = self._resistance(slot, stream, req, b, plan)
+            if isinstance(reqs[0], ResistanceRequest):
+                res, plan = self._resistance(slot, stream, reqs, b, plan)
             else:
-                res, plan = self._swimmer(stream, req, plan)
+                r, plan = self._swimmer(stream, reqs[0], plan)
+                res = [r]
             stream.synchronize()
         return res, plan
 
@@ -383,17 +494,30 @@ class SolveServer:
                     elif self._closed:
                         return
                     self._cv.wait(timeout=0.05)
-            req, fut, t_arr, b, plan, reserved = item
+            group, b, plan, reserved = item
+            reqs = [r for r, _, _ in group]
             t0 = time.perf_counter()
             try:
-                res, plan = self._run_request(slot, stream, req, b, plan)
-                res.t_arrival, res.t_start, res.t_done, res.slot = t_arr, t0, time.perf_counter(), slot
-                fut.set_result(res)
+                if len(group) == 1:
+                    res, plan = self._run_request(slot, stream, reqs[0], b, plan)
+                    res = [res]
+                else:
+                    res, plan = self._run_group(slot, stream, reqs, b, plan)
+                t1 = time.perf_counter()
+                for (req, fut, t_arr), r in zip(group, res):
+                    if isinstance(r, Exception):
+                        fut.set_exception(r)
+                        continue
+                    r.t_arrival, r.t_start, r.t_done, r.slot, r.batch = t_arr, t0, t1, slot, len(group)
+                    fut.set_result(r)
                 with self._cv:
+                    self.stats["groups"][len(group)] = self.stats["groups"].get(len(group), 0) + 1
                     if plan is not None:  # back into the pool, counted against the budget
-                        if reserved:
-                            plan.nbytes = reserved
-                        plan.key = self._key(req, b)
+                        if reserved:  # built for this group: count what it holds
+                            nb = getattr(plan, "nbytes", None) or reserved
+                            self._used += nb - reserved
+                            plan.nbytes = nb
+                        plan.key = self._key(reqs[0], b)
                         self._free.setdefault(plan.key, []).append(plan)
                         self._lru.append(plan)
                     else:
@@ -401,7 +525,9 @@ class SolveServer:
             except Exception as e:  # noqa: BLE001 - delivered to the caller
                 with self._cv:
                     self._used -= reserved if reserved else getattr(plan, "nbytes", 0)
-                fut.set_exception(e)
+                for _, fut, _ in group:
+                    if not fut.done():
+                        fut.set_exception(e)
             finally:
                 with self._cv:
                     self._busy[slot] = False
@@ -413,20 +539,31 @@ class SolveServer:
             return self.lu
         return self._tuned.get((kernel_params(req.kernel)[0], b))
 
-    def _resistance(self, slot, stream, req, b, plan):
+    def _resistance(self, slot, stream, reqs, b, plan):
+        """Resistance requests of one plan key: one (batched) factorization of the group, then
+        each system's refinement.  A request whose system fails gets its exception in place of
+        a Result."""
         dev = torch.device("cuda", self._dev)
-        X = torch.as_tensor(np.ascontiguousarray(req.points, dtype=np.float64)).to(dev, non_blocking=True)
-        U = torch.as_tensor(np.ascontiguousarray(req.velocities, dtype=np.float64)).to(dev, non_blocking=True)
-        N = X.shape[0]
-        e = torch.full((N,), float(req.eps), dtype=torch.float64, device=dev) if np.ndim(req.eps) == 0 else \
-            torch.as_tensor(np.asarray(req.eps, dtype=np.float64)).to(dev)
+        items, Us = [], []
+        for req in reqs:
+            X = torch.as_tensor(np.ascontiguousarray(req.points, dtype=np.float64)).to(dev, non_blocking=True)
+            U = torch.as_tensor(np.ascontiguousarray(req.velocities, dtype=np.float64)).to(dev, non_blocking=True)
+            N = X.shape[0]
+            e = torch.full((N,), float(req.eps), dtype=torch.float64, device=dev) if np.ndim(req.eps) == 0 else \
+                torch.as_tensor(np.asarray(req.eps, dtype=np.float64)).to(dev)
+            items.append((X, e))
+            Us.append(U)
+        req = reqs[0]
         if plan is None:
             lu = self._lu_for(req, b)
             if lu is None:  # autotune this bucket (precision x tile width), keep the fastest that converges
-                lu = self._autotune(req, b, stream, X, e, U)
+                lu = self._autotune(req, b, stream, items[0][0], items[0][1], Us[0])
                 with self._cv:
                     self._tuned[(kernel_params(req.kernel)[0], b)] = lu
-            plan = BucketPlan(req.kernel, b, req.mu, lu, stream, uniform=_uniform(req.eps))
+            uniform = _uniform(req.eps)
+            cap = max(len(reqs), self._cap(("res", kernel_params(req.kernel)[0], b, float(req.mu), lu, uniform), b))
+            plan = BucketPlan(req.kernel, b, req.mu, lu, stream, uniform=uniform, cap=cap)
+            plan.nbytes = self._need(req, b) * plan.cap
             with self._cv:
                 self.stats["plans_built"] += 1
             if self.graphs:
@@ -438,13 +575,29 @@ class SolveServer:
                     if plan.graph is None:
                         self.stats["capture_errors"].append(getattr(plan, "capture_error", "?"))
         plan.stream = stream  # a pooled plan runs on the stream of the slot that checked it out
-        plan.factor(X, e)
+        plan.factor_group(items)
         with self._cv:
             self.stats["graph_replays" if plan.graph is not None else "eager_factors"] += 1
-        F, it, outer, resid = plan.solve(U, self.rtol)
+        outs = []
+        if plan.irs and self.rtol * 1e-2 == plan.rtol_ir:
+            for z, U in enumerate(Us):  # every refinement queued, then the results in order
+                plan.launch_refinement(U, z)
+            for z, U in enumerate(Us):
+                try:
+                    outs.append(plan.refinement_result(U.shape[0], self.rtol, z))
+                except Exception as e:  # noqa: BLE001 - this request's own failure
+                    outs.append(e)
+        else:
+            for z, U in enumerate(Us):
+                try:
+                    outs.append(plan.solve(U, self.rtol, z=z))
+                except Exception as e:  # noqa: BLE001
+                    outs.append(e)
         # resid: the refinement's last ||U - K F|| / ||U|| with the FP64 K (padding rows are identity
         # with zero right-hand side, so this is the residual of the unpadded system)
-        return Result(F.cpu().numpy(), resid, 0, 0, 0, slot, b, plan.lu, outer), plan
+        res = [o if isinstance(o, Exception) else Result(o[0].cpu().numpy(), o[3], 0, 0, 0, slot, b, plan.lu, o[2])
+               for o in outs]
+        return res, plan
 
     def _autotune(self, req, b, stream, X, e, U):
         """Time factor + solve of this request for every candidate LU mode on one eager plan
@@ -573,16 +726,17 @@ def _poisson_run(srv, reqs, rate, seed):
             "max_residual": float(resid.max()) if len(resid) else None}
 
 
-def serve_run(n_requests=512, rate=200.0, slots=6, seed=0):
+def serve_run(n_requests=512, rate=200.0, slots=6, seed=0, batch=4):
     """A served run of the mixed workload at one arrival rate: p50 / p99 latency, solves/s and the
     server's counters (warm-up and per-bucket autotuning of the buckets in use happen first)."""
     reqs = make_requests(n_requests, seed=seed)
-    with SolveServer(slots=slots) as srv:
+    with SolveServer(slots=slots, batch=batch) as srv:
         _warm(srv, reqs)
         line = _poisson_run(srv, reqs, rate, int(rate))
         stats = dict(srv.stats)
     line["workload"] = (f"served mixed workload: {n_requests} requests (75% rigid bodies N log-uniform [256, 6144], "
-                        f"25% biflagellate swimmers), Poisson arrivals at {rate:g}/s, {slots} slots, HBM budget 150 GB")
+                        f"25% biflagellate swimmers), Poisson arrivals at {rate:g}/s, {slots} slots, groups of up to "
+                        f"{batch} same-bucket requests, HBM budget 150 GB")
     line["server_stats"] = {k: (v if not isinstance(v, list) else len(v)) for k, v in stats.items()}
     return line
 
@@ -600,9 +754,10 @@ def bench_serving(args):
     out = {"workload": f"served mixed workload: {n_req} requests (75% rigid bodies N log-uniform [256, 6144], "
                        "25% biflagellate swimmers), Poisson arrivals, HBM budget 150 GB", "rates": []}
     slots = getattr(args, "slots", 6)
+    batch = getattr(args, "batch", 4)
     rates = [float(r) for r in str(getattr(args, "rates", "50,200,800")).split(",")]
-    out["slots"] = slots
-    with SolveServer(slots=slots) as srv:
+    out["slots"], out["batch"] = slots, batch
+    with SolveServer(slots=slots, batch=batch) as srv:
         srv_stats = srv.stats
         # warm-up and autotuning of the buckets in use, outside the timed runs
         _warm(srv, reqs)

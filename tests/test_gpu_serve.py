@@ -74,3 +74,30 @@ def test_small_budget_still_serves_everything():
         res = [f.result(timeout=180) for f in [srv.submit(r) for r in reqs]]
     for r, x, ref in zip(reqs, res, refs):
         check(r, x, ref)
+
+
+def test_batched_groups_match_alone():
+    """Requests of one bucket (640 points) submitted together are factored in groups of up to
+    four, one replay of the batched graph per group; each result equals the request solved
+    alone, and the wall requests (another plan key) never share a group with the free ones."""
+    rng = np.random.default_rng(7)
+    reqs = []
+    for k in range(10):
+        N = int(rng.integers(520, 641))
+        pts = fibonacci_sphere(N) * np.array([rng.uniform(1, 2), 1, 1])
+        wall = k % 3 == 2
+        if wall:
+            pts = pts + [0, 0, -pts[:, 2].min() + rng.uniform(0.1, 1.0)]
+        eps = rng.uniform(0.2, 0.4) * mean_nn_spacing(pts)
+        U = np.tile(rng.normal(size=3), (N, 1))
+        reqs.append(ResistanceRequest(fl.WallStokeslet3D() if wall else fl.Stokeslet3D(), pts, U, eps))
+    refs = [alone(r) for r in reqs]
+    with SolveServer(slots=2, lu="tf32", batch=4) as srv:
+        res = [f.result(timeout=180) for f in [srv.submit(r) for r in reqs]]
+        stats = dict(srv.stats)
+    assert stats["capture_errors"] == [], stats
+    assert max(stats["groups"]) > 1, stats
+    for r, x, ref in zip(reqs, res, refs):
+        check(r, x, ref)
+        assert x.bucket == 640
+    assert any(x.batch > 1 for x in res)

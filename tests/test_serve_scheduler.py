@@ -1,5 +1,6 @@
 """Scheduling of the solve server, on the host only (device work replaced by fakes):
-admission by the HBM budget, eviction of idle plans, bucket affinity, no deadlock."""
+admission by the HBM budget, eviction of idle plans, bucket affinity, grouping of same-key
+requests for the batched graphs, no deadlock."""
 import threading
 import time
 
@@ -133,3 +134,53 @@ def test_autotuner_keeps_the_fastest_candidate_that_converges(monkeypatch):
         for k in resid:
             resid[k] = 1e-3
         assert srv._autotune(req, 512, _Stream(), None, None, None) == "tf32"
+
+
+class GroupServer(FakeServer):
+    """Records the groups the scheduler forms (device work replaced by a short sleep)."""
+
+    def __init__(self, *a, **k):
+        self.groups = []
+        super().__init__(*a, **k)
+
+    def _run_group(self, slot, stream, reqs, b, plan):
+        with self._cv:
+            self.groups.append([(self._group_key(r, b), b) for r in reqs])
+            if plan is None:
+                plan = _Plan(b, 0)
+                plan.cap = self._cap(self._key(reqs[0], b), b)
+        assert len(reqs) <= plan.cap
+        time.sleep(0.002)
+        return [Result(None, 0.0, 0, 0, 0, slot, b) for _ in reqs], plan
+
+    def _run_request(self, slot, stream, req, b, plan):
+        res, plan = self._run_group(slot, stream, [req], b, plan)
+        return res[0], plan
+
+
+def test_same_key_requests_are_grouped_up_to_the_batch():
+    """Requests submitted together are grouped by plan key (kernel, bucket, mu, LU mode, one
+    blob width), at most `batch` per group, only for buckets up to `batch_points`; every
+    request completes once, with its group size in the result."""
+    reqs = mix(160, 4, sizes=(300, 700, 3000))  # buckets 384, 768 and 3072 points
+    with GroupServer(slots=2, lu="tf32", batch=4, batch_points=2304) as srv:
+        futs = [srv.submit(r) for r in reqs]
+        res = [f.result(timeout=60) for f in futs]
+        groups, stats = srv.groups, dict(srv.stats)
+    assert len(res) == len(reqs)
+    sizes = [len(g) for g in groups]
+    assert sum(sizes) == len(reqs) and max(sizes) == 4
+    for g in groups:
+        assert len({k for k, _ in g}) == 1  # one plan key per group
+        if g[0][0] is None or g[0][1] > 2304:  # swimmers and large buckets run alone
+            assert len(g) == 1
+    assert sum(stats["groups"].get(k, 0) * k for k in stats["groups"]) == len(reqs)
+    assert {r.batch for r in res} >= {1, 4}
+
+
+def test_untuned_and_fp32_buckets_are_not_grouped():
+    reqs = mix(60, 5, sizes=(300,))
+    for lu in ("auto", "fp32"):
+        with GroupServer(slots=2, lu=lu, batch=4) as srv:
+            [f.result(timeout=60) for f in [srv.submit(r) for r in reqs]]
+            assert max(len(g) for g in srv.groups) == 1, lu
