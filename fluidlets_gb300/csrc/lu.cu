@@ -26,6 +26,7 @@
 // failure through a device flag instead of hanging.
 #include <cooperative_groups.h>
 #include <cuda.h>
+#include <cuda_bf16.h>
 
 #include <algorithm>
 
@@ -997,6 +998,30 @@ size_t tc_update_bytes(int64_t m, int64_t nc, int64_t K, int mode, int nb = 1);
 int tc_update(float *C, int64_t ldc, const float *Lp, int64_t ldl, const float *Ut, int64_t ldu, int64_t m,
               int64_t nc, int64_t K, int mode, void *work, size_t work_bytes, cudaStream_t st, int *err_dev,
               bool store = false, int tile = 0, int max_ctas = 0, const TcBatch &bt = TcBatch{});
+// the BF16 update from operands already rounded to BF16 (La, Ub: K-major __nv_bfloat16)
+int tc_update_bf16(float *C, int64_t ldc, const void *La, int64_t ldl, const void *Ub, int64_t ldu, int64_t m,
+                   int64_t nc, int64_t K, void *work, size_t work_bytes, cudaStream_t st, int *err_dev, int tile,
+                   int max_ctas, const TcBatch &bt);
+
+// BF16 copies of one step's finished panels for the BF16 trailing updates: blockIdx.y = 0
+// rounds the L panel (nr rows x 128, row stride lda) into Lb, 1 the K-major U panel (nr rows
+// x 128, row stride ldu) into Ub (row stride ldb); system blockIdx.z at + z (sA, sU, sB).
+__global__ void __launch_bounds__(256) panel_bf16_kernel(const float *L21, int64_t lda, const float *Ut, int64_t ldu,
+                                                         __nv_bfloat16 *Lb, __nv_bfloat16 *Ub, int64_t ldb,
+                                                         int64_t nr, int64_t sA, int64_t sU, int64_t sB) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, r = i >> 5;
+    if (r >= nr) return;
+    const int c4 = (int)(i & 31) * 4;
+    const int64_t z = blockIdx.z;
+    const float *src = blockIdx.y == 0 ? L21 + z * sA + r * lda : Ut + z * sU + r * ldu;
+    __nv_bfloat16 *dst = (blockIdx.y == 0 ? Lb : Ub) + z * sB + r * ldb;
+    const float4 v = *reinterpret_cast<const float4 *>(src + c4);
+    __nv_bfloat162 lo = __floats2bfloat162_rn(v.x, v.y), hi = __floats2bfloat162_rn(v.z, v.w);
+    uint2 w;
+    w.x = *reinterpret_cast<uint32_t *>(&lo);
+    w.y = *reinterpret_cast<uint32_t *>(&hi);
+    *reinterpret_cast<uint2 *>(dst + c4) = w;
+}
 
 static int sgemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, float alpha, const float *A, int64_t lda,
                  const float *B, int64_t ldb, float beta, float *C, int64_t ldc) {
@@ -1607,16 +1632,19 @@ extern "C" int64_t flg_lu_lowp_dinv_elems(int64_t n) { return 2 * ceil_div(std::
 // faster from n = 12,288 up and 2% slower at n = 4,608, so 512 below n = 8,192.
 static int64_t outer_width(int64_t n) { return (n >= 8192 ? 8 : 4) * (int64_t)kNB; }
 
-// scratch of nbat systems, system z's at + z * (kNB n, n kNB, n W) floats
+// scratch of nbat systems, system z's at + z * (kNB n, n kNB, n W) floats; BF16 mode: the
+// BF16 copies of the outer panel's L columns and of UtB (n W each per system) in PB
 template <class Ar>
 static void lowp_carve(Ar &ar, int64_t n, int nbat, int mode, float **U12, float **L21, float **UtB, char **tcw,
-                       size_t *tcb) {
+                       size_t *tcb, __nv_bfloat16 **PB) {
     *U12 = ar.template take<float>((size_t)nbat * kNB * n);
     *L21 = ar.template take<float>((size_t)nbat * n * kNB);
     const int64_t W = outer_width(n);
     *UtB = ar.template take<float>((size_t)nbat * n * W);
-    *tcb = (mode == FLG_LU_FP32) ? 0 : tc_update_bytes(n, n, W, mode, nbat);
+    // the panel products run in TF32 (no operand workspace); the BF16 updates read PB
+    *tcb = (mode == FLG_LU_FP32) ? 0 : tc_update_bytes(n, n, W, FLG_LU_TF32, nbat);
     *tcw = ar.template take<char>(*tcb);
+    *PB = mode == FLG_LU_BF16 ? ar.template take<__nv_bfloat16>((size_t)2 * nbat * n * W) : nullptr;
 }
 
 // precision part of an LU mode (the tile bits masked off)
@@ -1628,7 +1656,8 @@ extern "C" size_t flg_lu_factor_lowp_workspace(int64_t n, int mode) {
     float *a, *b, *d;
     char *w;
     size_t t;
-    lowp_carve(c, n, 1, mode, &a, &b, &d, &w, &t);
+    __nv_bfloat16 *pb;
+    lowp_carve(c, n, 1, mode, &a, &b, &d, &w, &t, &pb);
     return c.bytes() + 256;  // + the flags of flg_lu_factor_lowp, at the end
 }
 
@@ -1638,7 +1667,8 @@ extern "C" size_t flg_lu_factor_lowp_batched_workspace(int64_t n, int nbat, int 
     float *a, *b, *d;
     char *w;
     size_t t;
-    lowp_carve(c, n, std::max(nbat, 1), mode, &a, &b, &d, &w, &t);
+    __nv_bfloat16 *pb;
+    lowp_carve(c, n, std::max(nbat, 1), mode, &a, &b, &d, &w, &t, &pb);
     return c.bytes();
 }
 
@@ -1665,8 +1695,10 @@ static int lowp_factor(int64_t n, int nbat, float *A, int64_t ld, int64_t sA, in
     float *U12, *L21, *UtB;
     char *tcw;
     size_t tcb;
-    lowp_carve(ar, n, nbat, mode, &U12, &L21, &UtB, &tcw, &tcb);
-    FLG_REQUIRE(U12 && L21 && UtB && (tcb == 0 || tcw), "workspace too small for LU (%zu bytes)", work_bytes);
+    __nv_bfloat16 *PB;
+    lowp_carve(ar, n, nbat, mode, &U12, &L21, &UtB, &tcw, &tcb, &PB);
+    FLG_REQUIRE(U12 && L21 && UtB && (tcb == 0 || tcw) && (mode != FLG_LU_BF16 || PB),
+                "workspace too small for LU (%zu bytes)", work_bytes);
     // the tensor-core panels use the partial-block scratch: U12 for A12^T, L21 for Uinv^T
     float *T12 = U12, *UinvT = L21;
     int *dinfo = flags;  // [0] first bad pivot, [1] tensor-core wait timed out
@@ -1674,6 +1706,21 @@ static int lowp_factor(int64_t n, int nbat, float *A, int64_t ld, int64_t sA, in
     // per-system strides: the matrix, the block inverses, A12^T / Uinv^T scratch, U's K-major copy
     const int64_t sD = flg_lu_lowp_dinv_elems(n), sT = (int64_t)kNB * n, sUt = n * W;
     const TcBatch bA{nbat, sA, sA, sUt}, bU{nbat, sUt, sT, sD}, bL{nbat, sA, sA, sT};
+    // BF16 mode: each step's finished L and U panels are rounded once into LB (row r, column
+    // c - K0 of the outer panel at LB + r W + c - K0) and UB (laid out as UtB), and every
+    // trailing update of the outer panel reads them
+    __nv_bfloat16 *LB = PB, *UB = PB ? PB + (size_t)nbat * n * W : nullptr;
+    const TcBatch bB{nbat, sA, n * W, n * W};
+    int64_t K0 = 0;  // first column of the current outer panel
+    // C -= Lp Up^T (Lp inside A at columns [K0, E), Up inside UtB) over m x nc, depth K
+    auto upd = [&](float *C, const float *Lp, const float *Up, int64_t m, int64_t nc, int64_t K, int ctas) -> int {
+        if (mode == FLG_LU_BF16) {
+            const int64_t off = Lp - A, r = off / ld, c = off % ld;
+            return tc_update_bf16(C, ld, LB + r * W + (c - K0), W, UB + (Up - UtB), W, m, nc, K, tcw, tcb, st,
+                                  dinfo + 1, tile, ctas, bB);
+        }
+        return tc_update(C, ld, Lp, ld, Up, W, m, nc, K, mode, tcw, tcb, st, dinfo + 1, false, tile, ctas, bA);
+    };
     const size_t dsmem = kDiagSmem;
     static bool attr_set = false;  // set once, so a later call can be captured in a graph
     if (!attr_set) {
@@ -1726,7 +1773,7 @@ static int lowp_factor(int64_t n, int nbat, float *A, int64_t ld, int64_t sA, in
         pending = true;
         return FLG_OK;
     };
-    for (int64_t K0 = 0; K0 < n; K0 += W) {
+    for (K0 = 0; K0 < n; K0 += W) {
         const int64_t E = std::min<int64_t>(n, K0 + W);
         for (int64_t k0 = K0; k0 < E; k0 += kNB) {
             const int64_t k = k0 / kNB;
@@ -1770,6 +1817,11 @@ static int lowp_factor(int64_t n, int nbat, float *A, int64_t ld, int64_t sA, in
                     FLG_LAUNCH_CHECK();
                 }
                 FLG_CUDA(cudaStreamWaitEvent(st, side->ljoin, 0));
+                if (mode == FLG_LU_BF16) {  // both panels of this step, rounded once for every update
+                    panel_bf16_kernel<<<dim3((unsigned)ceil_div(nr * 32, 256), 2, nbat), 256, 0, st>>>(
+                        A21, ld, Ut, W, LB + c0 * W + (k0 - K0), UB + (Ut - UtB), W, nr, sA, sUt, n * W);
+                    FLG_LAUNCH_CHECK();
+                }
             } else if (nb == kNB) {
                 // U12 = Linv A12 (+ its K-major copy), L21 = A21 Uinv: one launch, in place
                 const int ntu = (int)ceil_div(nr, 32), ntl = (int)ceil_div(nr, 32);
@@ -1790,23 +1842,16 @@ static int lowp_factor(int64_t n, int nbat, float *A, int64_t ld, int64_t sA, in
                 if (n - c0 > kNB) {
                     // the next diagonal block first, then it factors beside the rest:
                     // rows > c0 + 128 x its columns, rows > k0 x columns (c0 + 128, E)
-                    FLG_TRY(tc_update(A22, ld, A21, ld, Ut, W, kNB, kNB, kNB, mode, tcw, tcb, st, dinfo + 1,
-                                      false, tile, 0, bA));
+                    FLG_TRY(upd(A22, A21, Ut, kNB, kNB, kNB, 0));
                     FLG_TRY(look_ahead(c0, Deferred{Ut, A12, nr}));
-                    FLG_TRY(tc_update(A22 + kNB * ld, ld, A21 + kNB * ld, ld, Ut, W, nr - kNB, kNB, kNB, mode,
-                                      tcw, tcb, st, dinfo + 1, false, tile, cap, bA));
-                    if (E > c0 + kNB)
-                        FLG_TRY(tc_update(A22 + kNB, ld, A21, ld, Ut + kNB * W, W, nr, E - c0 - kNB, kNB,
-                                          mode, tcw, tcb, st, dinfo + 1, false, tile, cap, bA));
+                    FLG_TRY(upd(A22 + kNB * ld, A21 + kNB * ld, Ut, nr - kNB, kNB, kNB, cap));
+                    if (E > c0 + kNB) FLG_TRY(upd(A22 + kNB, A21, Ut + kNB * W, nr, E - c0 - kNB, kNB, cap));
                 } else {
                     // rows > k0 x columns (k0, E)
-                    FLG_TRY(tc_update(A22, ld, A21, ld, Ut, W, nr, E - c0, kNB, mode, tcw, tcb, st, dinfo + 1,
-                                      false, tile, 0, bA));
+                    FLG_TRY(upd(A22, A21, Ut, nr, E - c0, kNB, 0));
                 }
                 // rows (k0, E) x columns >= E
-                if (n > E)
-                    FLG_TRY(tc_update(A + c0 * ld + E, ld, A21, ld, Ut + (E - c0) * W, W, E - c0, n - E,
-                                      kNB, mode, tcw, tcb, st, dinfo + 1, false, tile, pending ? cap : 0, bA));
+                if (n > E) FLG_TRY(upd(A + c0 * ld + E, A21, Ut + (E - c0) * W, E - c0, n - E, kNB, pending ? cap : 0));
             }
             prof_end(FLG_SLOT_LU_UPDATE, st);
         }
@@ -1815,16 +1860,12 @@ static int lowp_factor(int64_t n, int nbat, float *A, int64_t ld, int64_t sA, in
             float *C = A + E * ld + E, *Lp = A + E * ld + K0, *Up = UtB + (E - K0) * W;
             if (n - E > kNB) {
                 // the next outer panel's first diagonal block first, then it factors beside the rest
-                FLG_TRY(tc_update(C, ld, Lp, ld, Up, W, kNB, kNB, E - K0, mode, tcw, tcb, st, dinfo + 1, false,
-                                  tile, 0, bA));
+                FLG_TRY(upd(C, Lp, Up, kNB, kNB, E - K0, 0));
                 FLG_TRY(look_ahead(E, Deferred{}));
-                FLG_TRY(tc_update(C + kNB * ld, ld, Lp + kNB * ld, ld, Up, W, n - E - kNB, kNB, E - K0, mode,
-                                  tcw, tcb, st, dinfo + 1, false, tile, cap, bA));
-                FLG_TRY(tc_update(C + kNB, ld, Lp, ld, Up + kNB * W, W, n - E, n - E - kNB, E - K0, mode,
-                                  tcw, tcb, st, dinfo + 1, false, tile, cap, bA));
+                FLG_TRY(upd(C + kNB * ld, Lp + kNB * ld, Up, n - E - kNB, kNB, E - K0, cap));
+                FLG_TRY(upd(C + kNB, Lp, Up + kNB * W, n - E, n - E - kNB, E - K0, cap));
             } else {
-                FLG_TRY(tc_update(C, ld, Lp, ld, Up, W, n - E, n - E, E - K0, mode, tcw, tcb, st, dinfo + 1,
-                                  false, tile, 0, bA));
+                FLG_TRY(upd(C, Lp, Up, n - E, n - E, E - K0, 0));
             }
             prof_end(FLG_SLOT_LU_UPDATE, st);
         }

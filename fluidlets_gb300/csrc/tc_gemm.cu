@@ -416,6 +416,42 @@ static int tc_launch(const CUtensorMap &ma, const CUtensorMap &mb, const CUtenso
     return FLG_OK;
 }
 
+// The launch and the timeout check shared by both entry points below: C map, grid, flag.
+static int tc_run(const CUtensorMap &ma, const CUtensorMap &mb, float *C, int64_t ldc, int64_t m, int64_t nc,
+                  int64_t K, int mode, int bn, int sms, const TcBatch &bt, bool store, int *err, bool own_err,
+                  cudaStream_t st) {
+    const int nb = bt.count;
+    CUtensorMap mc;
+    FLG_TRY(make_c_map(&mc, C, m, nc, ldc, nb, bt.sC));
+    if (own_err) FLG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
+    const int nkb = (int)(K / (mode == FLG_LU_TF32 ? 32 : 64));
+    int rc;
+    if (mode == FLG_LU_TF32)
+        rc = bn == 128 ? tc_launch<FLG_LU_TF32, 128>(ma, mb, mc, m, nc, nkb, nb, store, err, sms, st)
+                       : tc_launch<FLG_LU_TF32, 256>(ma, mb, mc, m, nc, nkb, nb, store, err, sms, st);
+    else
+        rc = bn == 128 ? tc_launch<FLG_LU_BF16, 128>(ma, mb, mc, m, nc, nkb, nb, store, err, sms, st)
+                       : tc_launch<FLG_LU_BF16, 256>(ma, mb, mc, m, nc, nkb, nb, store, err, sms, st);
+    FLG_TRY(rc);
+    if (!own_err) return FLG_OK;
+    int herr = 0;
+    FLG_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    FLG_CUDA(cudaStreamSynchronize(st));
+    if (herr != 0) {
+        set_error("a bounded device wait timed out (tensor-core update, mbarrier)");
+        return FLG_ERR_TIMEOUT;
+    }
+    return FLG_OK;
+}
+
+static int tc_check_shape(int64_t m, int64_t nc, int64_t K, int tile, const TcBatch &bt) {
+    FLG_REQUIRE(m >= 0 && nc >= 0 && m < (1LL << 31) && nc < (1LL << 31), "bad tensor-core update shape");
+    FLG_REQUIRE(bt.count >= 1 && bt.count <= 65535, "bad batch count %d", bt.count);
+    FLG_REQUIRE(K > 0 && K % 128 == 0 && K <= (1 << 20), "tensor-core update depth must be a multiple of 128");
+    FLG_REQUIRE(tile == 0 || tile == 128 || tile == 256, "tile width must be 128 or 256 (or 0 to choose)");
+    return FLG_OK;
+}
+
 // err_dev: device flag raised on a timed-out wait.  When null, the flag lives in
 // the workspace and the call synchronizes to check it; the LU passes its own
 // flag and checks it once at the end of the factorization.  tile: 0 picks the
@@ -426,11 +462,8 @@ int tc_update(float *C, int64_t ldc, const float *Lp, int64_t ldl, const float *
               int64_t nc, int64_t K, int mode, void *work, size_t work_bytes, cudaStream_t st, int *err_dev,
               bool store, int tile, int max_ctas, const TcBatch &bt) {
     FLG_REQUIRE(mode == FLG_LU_TF32 || mode == FLG_LU_BF16, "tensor-core mode must be TF32 or BF16");
-    FLG_REQUIRE(m >= 0 && nc >= 0 && m < (1LL << 31) && nc < (1LL << 31), "bad tensor-core update shape");
-    FLG_REQUIRE(bt.count >= 1 && bt.count <= 65535, "bad batch count %d", bt.count);
+    FLG_TRY(tc_check_shape(m, nc, K, tile, bt));
     const int nb = bt.count;
-    FLG_REQUIRE(K > 0 && K % 128 == 0 && K <= (1 << 20), "tensor-core update depth must be a multiple of 128");
-    FLG_REQUIRE(tile == 0 || tile == 128 || tile == 256, "tile width must be 128 or 256 (or 0 to choose)");
     if (m == 0 || nc == 0) return FLG_OK;
     const int sms = max_ctas > 0 ? std::min(max_ctas, sm_count_of_current_device()) : sm_count_of_current_device();
     const int bn = tile ? tile : tc_pick_tile(m, nc, sms, nb);
@@ -438,7 +471,7 @@ int tc_update(float *C, int64_t ldc, const float *Lp, int64_t ldl, const float *
     int *own = ar.take<int>(1);
     int *err = err_dev ? err_dev : own;
     FLG_REQUIRE(err != nullptr && own != nullptr, "workspace too small for the tensor-core update");
-    CUtensorMap ma, mb, mc;
+    CUtensorMap ma, mb;
     if (mode == FLG_LU_TF32) {
         FLG_TRY(make_operand_map(&ma, Lp, m, K, ldl, mode, TC_BM, nb, bt.sL));
         FLG_TRY(make_operand_map(&mb, Ut, nc, K, ldu, mode, bn, nb, bt.sU));
@@ -454,26 +487,27 @@ int tc_update(float *C, int64_t ldc, const float *Lp, int64_t ldl, const float *
         FLG_TRY(make_operand_map(&ma, La, m, K, K, mode, TC_BM, nb, m * K));
         FLG_TRY(make_operand_map(&mb, Ub, nc, K, K, mode, bn, nb, nc * K));
     }
-    FLG_TRY(make_c_map(&mc, C, m, nc, ldc, nb, bt.sC));
-    if (!err_dev) FLG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
-    const int nkb = (int)(K / (mode == FLG_LU_TF32 ? 32 : 64));
-    int rc;
-    if (mode == FLG_LU_TF32)
-        rc = bn == 128 ? tc_launch<FLG_LU_TF32, 128>(ma, mb, mc, m, nc, nkb, nb, store, err, sms, st)
-                       : tc_launch<FLG_LU_TF32, 256>(ma, mb, mc, m, nc, nkb, nb, store, err, sms, st);
-    else
-        rc = bn == 128 ? tc_launch<FLG_LU_BF16, 128>(ma, mb, mc, m, nc, nkb, nb, store, err, sms, st)
-                       : tc_launch<FLG_LU_BF16, 256>(ma, mb, mc, m, nc, nkb, nb, store, err, sms, st);
-    FLG_TRY(rc);
-    if (err_dev) return FLG_OK;
-    int herr = 0;
-    FLG_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
-    FLG_CUDA(cudaStreamSynchronize(st));
-    if (herr != 0) {
-        set_error("a bounded device wait timed out (tensor-core update, mbarrier)");
-        return FLG_ERR_TIMEOUT;
-    }
-    return FLG_OK;
+    return tc_run(ma, mb, C, ldc, m, nc, K, mode, bn, sms, bt, store, err, err_dev == nullptr, st);
+}
+
+// The BF16 update with operands already rounded to BF16 (K-major, row strides ldl / ldu
+// elements, system strides bt.sL / bt.sU elements): no conversion launches.  C -= La Ub^T.
+int tc_update_bf16(float *C, int64_t ldc, const void *La, int64_t ldl, const void *Ub, int64_t ldu, int64_t m,
+                   int64_t nc, int64_t K, void *work, size_t work_bytes, cudaStream_t st, int *err_dev, int tile,
+                   int max_ctas, const TcBatch &bt) {
+    FLG_TRY(tc_check_shape(m, nc, K, tile, bt));
+    const int nb = bt.count;
+    if (m == 0 || nc == 0) return FLG_OK;
+    const int sms = max_ctas > 0 ? std::min(max_ctas, sm_count_of_current_device()) : sm_count_of_current_device();
+    const int bn = tile ? tile : tc_pick_tile(m, nc, sms, nb);
+    Arena ar(work, work_bytes);
+    int *own = ar.take<int>(1);
+    int *err = err_dev ? err_dev : own;
+    FLG_REQUIRE(err != nullptr && own != nullptr, "workspace too small for the tensor-core update");
+    CUtensorMap ma, mb;
+    FLG_TRY(make_operand_map(&ma, La, m, K, ldl, FLG_LU_BF16, TC_BM, nb, bt.sL));
+    FLG_TRY(make_operand_map(&mb, Ub, nc, K, ldu, FLG_LU_BF16, bn, nb, bt.sU));
+    return tc_run(ma, mb, C, ldc, m, nc, K, FLG_LU_BF16, bn, sms, bt, false, err, err_dev == nullptr, st);
 }
 
 }  // namespace flg
