@@ -555,20 +555,25 @@ __global__ void trsv_update_kernel(const double *LU, int64_t ld, double *B, int6
 // the identity to 128) in shared memory, in 32 x 32 sub-blocks, and builds the
 // inverses of its L and U factors alongside (they precondition the panels and
 // the solves).  With X = inv(L) and Y = inv(U) started at zero, step s:
-//   warp 0:  D[s][s] = L_ss U_ss (lane = row, the pivot row broadcast through
-//            shared memory); the same sweep solves Y[s][s] U_ss = I row by row
-//            with the broadcast pivot rows, and publishes each column of L_ss;
-//   warp 1:  X[s][s] = inv(L_ss) column by column (lane = column), following
+//   warp 0:  D[s][s] = L_ss U_ss (lane = row, the pivot row broadcast by warp
+//            shuffles); the same sweep solves Y[s][s] U_ss = I row by row with
+//            the broadcast pivot rows, and publishes each column of L_ss;
+//   warp 4:  X[s][s] = inv(L_ss) column by column (lane = column), following
 //            warp 0's published columns (bounded waits);
 //   stage 1: U panel D[s][t] = X[s][s] D[s][t], L panel D[t][s] = D[t][s] Y[s][s]
 //            (t > s); X[s][q] = X[s][s] X[s][q], Y[q][s] = Y[q][s] Y[s][s] (q < s);
 //   stage 2: D[t][u] -= D[t][s] D[s][u] (t, u > s);
 //            X[t][q] -= D[t][s] X[s][q] (t > s, q <= s);
 //            Y[q][u] -= Y[q][s] D[s][u] (q <= s, u > s).
-// Stage 2 looks ahead: warps 0 and 1 update D[s+1][s+1] alone and go on to step
-// s + 1, while the 8 warps of the two other schedulers do the rest of stage 2 and
-// store the block row s of D and X and the block column s of Y (no later step
-// changes them).
+// Stage 2 looks ahead: warps 0 and 4 update D[s+1][s+1] alone and go on to step
+// s + 1, while the 12 warps of the other three schedulers do the rest of stage 2
+// and store the block row s of D and X and the block column s of Y (no later step
+// changes them).  Warps 0 and 4 share scheduler 0 (warp w issues on scheduler
+// w % 4): the latency-bound 32 x 32 factorization keeps a scheduler without
+// block products.  The block products are bound by shared-memory bandwidth (one
+// 16-byte load per lane per 8 FMA); measured per 128 x 128 block: 38.5 us with
+// the pivot row through shared memory and stage 2 on two schedulers, 36.1 us
+// with shuffles and three (bit-identical results).
 // (X <- inv(L_s) X and Y <- Y inv(U_s) for the block-column / block-row factors
 // L = L_0 L_1 L_2 L_3, U = U_3 U_2 U_1 U_0.)  Every stage-1/2 product is a
 // 32 x 32 x 32 block product split into two warp tasks (16-row or 16-column
@@ -579,6 +584,7 @@ constexpr int kNS = kNB / kSB;   // sub-blocks per side (4)
 constexpr int kLD = kNB + 4;     // shared-memory row stride (floats)
 constexpr size_t kDiagSmem = 3 * (size_t)kNB * kLD * sizeof(float);
 constexpr int kPub = 4;                   // columns of L published per flag update
+constexpr int kLinvWarp = 4;              // the inverse-of-L warp: scheduler 0, beside the LU warp
 constexpr long long kDiagSpin = 1LL << 22;  // bounded wait of warp 1 on warp 0
 
 __device__ __forceinline__ float *sblk(float *M, int i, int j) { return M + i * kSB * kLD + j * kSB; }
@@ -592,11 +598,12 @@ __device__ __forceinline__ float rcp_approx(float x) {
 
 __device__ __forceinline__ int ld_volatile_s32(const int *p) { return *(const volatile int *)p; }
 
-// Warp 0: row-per-lane LU of P (pivot row through R) and, in the same sweep, Y = inv(U) by rows
-// (Y U = I solved left to right with the pivot rows already broadcast); publishes column j of L
-// (multipliers, zero on and above the diagonal) to Lc[j][0..32) for warp 1, kPub columns at a time.
-__device__ __forceinline__ void lu32_fused(float *P, float *Yb, float *R, float *Lc, int *flag, int flag0, int lane,
-                                           int row0, int nb, int64_t k0, int *info) {
+// Warp 0: row-per-lane LU of P (pivot row by shuffles from lane j) and, in the same sweep,
+// Y = inv(U) by rows (Y U = I solved left to right with the pivot rows already broadcast);
+// publishes column j of L (multipliers, zero on and above the diagonal) to Lc[j][0..32) for the
+// inverse warp, kPub columns at a time.
+__device__ __forceinline__ void lu32_fused(float *P, float *Yb, float *Lc, int *flag, int flag0, int lane, int row0,
+                                           int nb, int64_t k0, int *info) {
     float a[kSB], y[kSB];
 #pragma unroll
     for (int c4 = 0; c4 < kSB; c4 += 4) {
@@ -607,14 +614,7 @@ __device__ __forceinline__ void lu32_fused(float *P, float *Yb, float *R, float 
     unsigned bad = 0;
 #pragma unroll
     for (int j = 0; j < kSB; j++) {
-        float *Rb = R + (j & 1) * kSB;
-        if (lane == j) {
-#pragma unroll
-            for (int c4 = j & ~3; c4 < kSB; c4 += 4)
-                *reinterpret_cast<float4 *>(Rb + c4) = make_float4(a[c4], a[c4 + 1], a[c4 + 2], a[c4 + 3]);
-        }
-        __syncwarp();
-        const float piv = Rb[j];
+        const float piv = __shfl_sync(0xffffffffu, a[j], j);
         const bool ok = piv != 0.0f && isfinite(piv);
         bad |= (ok || row0 + j >= nb) ? 0u : (1u << j);
         const float rp = ok ? rcp_approx(piv) : 0.0f;
@@ -625,15 +625,10 @@ __device__ __forceinline__ void lu32_fused(float *P, float *Yb, float *R, float 
         if (lane > j) a[j] = l;
         Lc[j * kSB + lane] = l;
 #pragma unroll
-        for (int c4 = (j + 1) & ~3; c4 < kSB; c4 += 4) {
-            const float4 v = *reinterpret_cast<const float4 *>(Rb + c4);
-            const float u[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-            for (int q = 0; q < 4; q++)
-                if (c4 + q > j) {
-                    a[c4 + q] = fmaf(-l, u[q], a[c4 + q]);
-                    y[c4 + q] = fmaf(yj, u[q], y[c4 + q]);
-                }
+        for (int c = j + 1; c < kSB; c++) {
+            const float u = __shfl_sync(0xffffffffu, a[c], j);  // pivot row j, column c
+            a[c] = fmaf(-l, u, a[c]);
+            y[c] = fmaf(yj, u, y[c]);
         }
         if (j % kPub == kPub - 1) {
             __syncwarp();
@@ -651,7 +646,7 @@ __device__ __forceinline__ void lu32_fused(float *P, float *Yb, float *R, float 
     }
 }
 
-// Warp 1: X = inv(L) column `lane`, right-looking forward substitution over the published columns
+// Warp 4: X = inv(L) column `lane`, right-looking forward substitution over the published columns
 // of L (waits, bounded, for each group of kPub; on a timeout raises info[1] and stops).
 __device__ __forceinline__ void linv32_follow(const float *Lc, float *Xb, const int *flag, int flag0, int lane,
                                               int *info) {
@@ -774,7 +769,7 @@ __global__ void __launch_bounds__(512) diag_lowp_kernel(float *A, int64_t ld, in
         if (UinvT) UinvT += z * sT;
     }
     float *D = sm, *X = sm + kNB * kLD, *Y = sm + 2 * kNB * kLD;
-    __shared__ __align__(16) float R[2 * kSB], Lc[kSB * kSB];
+    __shared__ __align__(16) float Lc[kSB * kSB];
     __shared__ int flag;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, nthr = blockDim.x, nwarp = nthr >> 5;
     if (tid == 0) flag = 0;
@@ -808,9 +803,9 @@ __global__ void __launch_bounds__(512) diag_lowp_kernel(float *A, int64_t ld, in
     __syncthreads();
     for (int s = 0; s < kNS; s++) {
         const int m = kNS - 1 - s;
-        // factor D[s][s] (warp 0) and invert L_ss (warp 1); the other warps finish stage 2 of s - 1
-        if (warp == 0) lu32_fused(sblk(D, s, s), sblk(Y, s, s), R, Lc, &flag, s * kSB, lane, s * kSB, nb, k0, info);
-        else if (warp == 1) linv32_follow(Lc, sblk(X, s, s), &flag, s * kSB, lane, info);
+        // factor D[s][s] (warp 0) and invert L_ss (warp kLinvWarp); the other warps finish stage 2 of s - 1
+        if (warp == 0) lu32_fused(sblk(D, s, s), sblk(Y, s, s), Lc, &flag, s * kSB, lane, s * kSB, nb, k0, info);
+        else if (warp == kLinvWarp) linv32_follow(Lc, sblk(X, s, s), &flag, s * kSB, lane, info);
         __syncthreads();
         for (int t = warp; t < 2 * (2 * m + 2 * s); t += nwarp) {
             const int b = t >> 1, h = (t & 1) * 16;
@@ -830,18 +825,18 @@ __global__ void __launch_bounds__(512) diag_lowp_kernel(float *A, int64_t ld, in
         }
         __syncthreads();
         if (m == 0) break;
-        if (warp < 2) {
-            // look-ahead: the block the next factorization needs, D[s+1][s+1] -= D[s+1][s] D[s][s+1],
-            // then on to step s + 1 while the other warps finish stage 2
-            warp_mm<8, true>(sblk(D, s + 1, s) + warp * 16 * kLD, sblk(D, s, s + 1),
-                             sblk(D, s + 1, s + 1) + warp * 16 * kLD, lane);
+        if (warp == 0 || warp == kLinvWarp) {
+            // look-ahead: the block the next factorization needs, D[s+1][s+1] -= D[s+1][s] D[s][s+1]
+            // (a 16-row half each), then on to step s + 1 while the other warps finish stage 2
+            const int h = warp == 0 ? 0 : 16;
+            warp_mm<8, true>(sblk(D, s + 1, s) + h * kLD, sblk(D, s, s + 1), sblk(D, s + 1, s + 1) + h * kLD, lane);
             asm volatile("bar.sync 1, 64;" ::: "memory");
-        } else if ((warp & 3) >= 2) {
+        } else if ((warp & 3) != 0) {
             // the rest of stage 2 (m^2 - 1 blocks of D, m (s + 1) of X and of Y), then the stores of
-            // step s, on the 8 warps of the two schedulers that warps 0 and 1 do not use
-            const int w8 = (warp >> 2) * 2 + (warp & 1);
+            // step s, on the 12 warps of the three schedulers that warps 0 and kLinvWarp do not use
+            const int w12 = (warp >> 2) * 3 + (warp & 3) - 1;
             const int nD = m * m - 1, nX = m * (s + 1);
-            for (int t = w8; t < 2 * (nD + 2 * nX); t += 8) {
+            for (int t = w12; t < 2 * (nD + 2 * nX); t += 12) {
                 const int b = t >> 1, h = (t & 1) * 16;
                 if (b < nD) {
                     const int i = (b + 1) / m, j = (b + 1) - ((b + 1) / m) * m;
@@ -857,7 +852,7 @@ __global__ void __launch_bounds__(512) diag_lowp_kernel(float *A, int64_t ld, in
                                      lane);
                 }
             }
-            diag_store_step(s, D, X, Y, A, ld, k0, nb, v4, Linv, Uinv, UinvT, w8 * 32 + lane, 256);
+            diag_store_step(s, D, X, Y, A, ld, k0, nb, v4, Linv, Uinv, UinvT, w12 * 32 + lane, 12 * 32);
         }
     }
     diag_store_step(kNS - 1, D, X, Y, A, ld, k0, nb, v4, Linv, Uinv, UinvT, tid, nthr);
