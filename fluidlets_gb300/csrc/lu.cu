@@ -1098,20 +1098,15 @@ __device__ __forceinline__ void mbar_arrive1(uint64_t *bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-// the published float4 of a block (elements e .. e+3, those < n): the four loads are issued
-// together, then any still unset is polled until published
+// the published float4 of a block (elements e .. e+3, those < n; zeros beyond n): the four
+// loads are issued together, then those still unset are polled together until published
 __device__ __forceinline__ bool fetch4(const float *v, int64_t e, int64_t n, float4 &out, int *err) {
-    unsigned first[4];
+    const int cnt = (int)max((int64_t)0, min((int64_t)4, n - e));
+    unsigned u[4];
 #pragma unroll
-    for (int k = 0; k < 4; k++) first[k] = e + k < n ? ld_relaxed_u32(v + e + k) : 0u;
-    float f[4];
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-        unsigned u = first[k];
-        if (e + k < n && !wait_published(v + e + k, kUnset, first[k], &u, kWaitLimitNs, err)) return false;
-        f[k] = __uint_as_float(u);
-    }
-    out = make_float4(f[0], f[1], f[2], f[3]);
+    for (int k = 0; k < 4; k++) u[k] = k < cnt ? ld_relaxed_u32(v + e + k) : 0u;
+    if (!wait_published4(reinterpret_cast<const unsigned *>(v + e), cnt, kUnset, u, kWaitLimitNs, err)) return false;
+    out = make_float4(__uint_as_float(u[0]), __uint_as_float(u[1]), __uint_as_float(u[2]), __uint_as_float(u[3]));
     return true;
 }
 

@@ -14,7 +14,7 @@ namespace flg {
 
 struct SelftestWords {
     GridBar bar;       // the grid barrier: counter, error word
-    unsigned slot;     // a published value that nothing stores (preset to the unset pattern)
+    unsigned slot[4];  // published values that nothing stores (preset to the unset pattern)
     int err;           // error word of the poll and mbarrier cases
 };
 
@@ -23,10 +23,10 @@ __global__ void selftest_grid_kernel(SelftestWords *w, unsigned long long limit_
     grid_sync(&w->bar, gridDim.x + 1, limit_ns);
 }
 
-// one thread polls a value that nothing publishes
+// one thread polls four values that nothing publishes
 __global__ void selftest_poll_kernel(SelftestWords *w, unsigned long long limit_ns) {
-    unsigned v;
-    wait_published(&w->slot, 0xffffffffu, 0xffffffffu, &v, limit_ns, &w->err);
+    unsigned v[4] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu};
+    wait_published4(w->slot, 4, 0xffffffffu, v, limit_ns, &w->err);
 }
 
 // one thread waits on an mbarrier phase that no arrival completes (the tensor-core
@@ -55,7 +55,7 @@ extern "C" int flg_wait_selftest(int which, double limit_ms, void *work, size_t 
     cudaStream_t st = as_stream(stream);
     const unsigned long long limit_ns = (unsigned long long)(limit_ms * 1e6);
     FLG_CUDA(cudaMemsetAsync(w, 0, sizeof(SelftestWords), st));
-    FLG_CUDA(cudaMemsetAsync(&w->slot, 0xff, sizeof(unsigned), st));
+    FLG_CUDA(cudaMemsetAsync(w->slot, 0xff, sizeof(w->slot), st));
     if (which == 0) {
         void *args[] = {&w, (void *)&limit_ns};
         FLG_CUDA(cudaLaunchCooperativeKernel((void *)selftest_grid_kernel, dim3(2), dim3(32), args, 0, st));

@@ -35,26 +35,32 @@ __device__ __forceinline__ unsigned ld_relaxed_u32(const void *p) {
 }
 
 // ---- published-value poll ------------------------------------------------------------
-// Waits until the 32-bit word at p differs from `unset` (a producer stores the value
-// itself, relaxed, in place of a flag); *v receives it.  The first probe is the
-// caller's (`first`), so a value that already arrived costs no extra load.
-__device__ __forceinline__ bool wait_published(const void *p, unsigned unset, unsigned first, unsigned *v,
-                                               unsigned long long limit_ns, int *err) {
-    unsigned u = first;
-    if (u != unset) {
-        *v = u;
-        return true;
-    }
+// Waits until each of the `count` (<= 4) 32-bit words p[0..count) differs from `unset` (a
+// producer stores the value itself, relaxed, in place of a flag).  v[] holds the caller's
+// first probe of each word, so values that already arrived cost no extra load, and
+// receives the values.  The words still unset are reloaded together on every round: values
+// that arrive together cost one round trip, not one each.  The error word and the clock are
+// checked every 32 rounds (all waiting threads share the error word).
+__device__ __forceinline__ bool wait_published4(const unsigned *p, int count, unsigned unset, unsigned (&v)[4],
+                                                unsigned long long limit_ns, int *err) {
+    bool pending = false;
+#pragma unroll
+    for (int k = 0; k < 4; k++) pending |= k < count && v[k] == unset;
+    if (!pending) return true;
     const unsigned long long t0 = global_ns();
-    while ((u = ld_relaxed_u32(p)) == unset) {
-        if (*(volatile int *)err || global_ns() - t0 > limit_ns) {
+    for (unsigned round = 1;; round++) {
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            if (k < count && v[k] == unset) v[k] = ld_relaxed_u32(p + k);
+        pending = false;
+#pragma unroll
+        for (int k = 0; k < 4; k++) pending |= k < count && v[k] == unset;
+        if (!pending) return true;
+        if ((round & 31) == 0 && (*(volatile int *)err || global_ns() - t0 > limit_ns)) {
             atomicExch(err, 1);
-            *v = unset;
             return false;
         }
     }
-    *v = u;
-    return true;
 }
 
 // ---- grid barrier -------------------------------------------------------------------
