@@ -319,4 +319,82 @@ __device__ __forceinline__ void wall_far_acc(const WallFar &g, float f0, float f
     u[2] = fmaf(g.cz, f2, fmaf(g.dm, t1, fmaf(-g.dp, v, u[2])));
 }
 
+// ---- two targets in one register pair (packed FP32x2 arithmetic) -------------------
+// Blackwell's fma/add/sub/mul .f32x2 do two FP32 operations (one per 32-bit half, the same
+// rounding as the scalar instruction) in one issue slot; the FP32 pipe's lane rate is
+// unchanged, so an issue-bound pair loop gets the slots back for the pipe.  The wall
+// kernel's far loop runs its two targets per thread through them, the source values
+// arriving duplicated into both halves from shared memory; the special functions stay
+// scalar, one per half.  Each half computes exactly what wall_far_geo / wall_far_acc
+// compute for its target.
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 pk2(float lo, float hi) {
+    f32x2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ float lo2(f32x2 v) {
+    float lo, hi;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+    return lo;
+}
+__device__ __forceinline__ float hi2(f32x2 v) {
+    float lo, hi;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+    return hi;
+}
+__device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
+    f32x2 d;
+    asm("fma.rn.ftz.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ f32x2 add2(f32x2 a, f32x2 b) {
+    f32x2 d;
+    asm("add.rn.ftz.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f32x2 sub2(f32x2 a, f32x2 b) {
+    f32x2 d;
+    asm("sub.rn.ftz.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b) {
+    f32x2 d;
+    asm("mul.rn.ftz.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f32x2 neg2(f32x2 a) { return a ^ 0x8000000080000000ull; }  // both signs
+__device__ __forceinline__ f32x2 rsq2(f32x2 a) { return pk2(rsq(lo2(a)), rsq(hi2(a))); }
+__device__ __forceinline__ f32x2 rcp2(f32x2 a) { return pk2(rcp(lo2(a)), rcp(hi2(a))); }
+
+// u (x, y, z components, one target per half) += the far wall pair of the targets (tx, ty,
+// tz) with one source (sx, sy, h, e2 and the h-scaled strengths f0, f1, f2 in both halves);
+// unmasked (the caller knows no pair is near), without the factor 2 t.
+__device__ __forceinline__ void wall_far_pair2(f32x2 tx, f32x2 ty, f32x2 tz, f32x2 sx, f32x2 sy, f32x2 h, f32x2 e2,
+                                               f32x2 f0, f32x2 f1, f32x2 f2, f32x2 (&u)[3]) {
+    const f32x2 d0 = sub2(tx, sx), d1 = sub2(ty, sy), dm = sub2(tz, h), dp = add2(tz, h);
+    const f32x2 rq = fma2(d1, d1, fma2(d0, d0, e2));
+    const f32x2 QF = fma2(dm, dm, rq);
+    const f32x2 QI = fma2(dp, dp, rq);
+    const f32x2 sF = rsq2(QF), s = rsq2(QI);
+    const f32x2 p = mul2(sF, s), q = add2(sF, s);
+    const f32x2 Z1 = mul2(mul2(p, add2(p, p)), rcp2(q));
+    const f32x2 Z3 = mul2(Z1, fma2(q, q, neg2(p)));
+    const f32x2 s2 = mul2(s, s), s3 = mul2(s2, s), s5 = mul2(s3, s2);
+    const f32x2 base = sub2(fma2(e2, Z3, Z1), s3);
+    const f32x2 e2s5 = mul2(e2, s5);
+    const f32x2 three = 0x4040000040400000ull;  // 3.0f in both halves
+    const f32x2 cxy = fma2(e2s5, three, base), cz = fma2(e2s5, neg2(three), base);
+    const f32x2 s5x3 = mul2(three, s5);
+    const f32x2 D = fma2(d1, f1, mul2(d0, f0));
+    const f32x2 fdF = fma2(dm, f2, D);
+    const f32x2 P = fma2(dp, f2, neg2(D));
+    const f32x2 t1 = mul2(Z3, fdF);
+    const f32x2 v = mul2(s5x3, P);
+    const f32x2 Bxy = sub2(t1, v);
+    u[0] = fma2(d0, Bxy, fma2(cxy, f0, u[0]));
+    u[1] = fma2(d1, Bxy, fma2(cxy, f1, u[1]));
+    u[2] = fma2(cz, f2, fma2(dm, t1, fma2(neg2(dp), v, u[2])));
+}
+
 }  // namespace flg

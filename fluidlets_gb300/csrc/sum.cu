@@ -277,7 +277,11 @@ template <int KIND, int NF, bool CK, int TPT>
 __global__ void FLG_FAR_BOUNDS far_f32_kernel(FarArgs a) {
     constexpr int NQ = 1 + NF;
     constexpr int OUTW = (NF == 2 || CK) ? 6 : 3;
+    // the wall kernel's targets run the far loop two per register pair, in packed FP32x2
+    // arithmetic, from a copy of the tile with every source value duplicated into both halves
+    constexpr bool PACK = KIND == FLG_WALL && NF == 1 && !CK && TPT % 2 == 0;
     __shared__ float4 s_src[kF32Tile * NQ];
+    __shared__ ulonglong2 s_dup[PACK ? kF32Tile * 4 : 1];
     __shared__ float s_box[kF32Threads / 32][6];
     const int64_t base = (int64_t)blockIdx.x * (kF32Threads * TPT) + threadIdx.x;
     float tx[TPT], ty[TPT], tz[TPT], tz2[TPT];
@@ -332,6 +336,13 @@ __global__ void FLG_FAR_BOUNDS far_f32_kernel(FarArgs a) {
         __syncthreads();
 #pragma unroll
         for (int qd = 0; qd < NQ; qd++) s_src[threadIdx.x * NQ + qd] = pre[qd];
+        if constexpr (PACK) {  // {x, y} {h, e2} {f0, f1} {f2, thr}, each value in both halves
+            ulonglong2 *d = s_dup + threadIdx.x * 4;
+            d[0] = make_ulonglong2(pk2(pre[0].x, pre[0].x), pk2(pre[0].y, pre[0].y));
+            d[1] = make_ulonglong2(pk2(pre[0].z, pre[0].z), pk2(pre[0].w, pre[0].w));
+            d[2] = make_ulonglong2(pk2(pre[1].x, pre[1].x), pk2(pre[1].y, pre[1].y));
+            d[3] = make_ulonglong2(pk2(pre[1].z, pre[1].z), pk2(pre[1].w, pre[1].w));
+        }
         __syncthreads();
         {
             const int64_t j = jt + kF32Tile + threadIdx.x;
@@ -354,7 +365,30 @@ __global__ void FLG_FAR_BOUNDS far_f32_kernel(FarArgs a) {
             const float gz = fmaxf(0.0f, fmaxf(lo.z - bh[2], bl[2] - hi.z));
             far_tile = fmaf(gz, gz, fmaf(gy, gy, gx * gx)) > lo.w * (1.0f + 0x1p-10f);
         }
-        if (far_tile) {
+        if (PACK && far_tile) {
+            if constexpr (PACK) {
+                constexpr int H = TPT / 2;  // register pairs of targets: (0, 1), (2, 3), ...
+                f32x2 tx2[H], ty2[H], tz2p[H], u2[H][3];
+#pragma unroll
+                for (int h = 0; h < H; h++) {
+                    tx2[h] = pk2(tx[2 * h], tx[2 * h + 1]), ty2[h] = pk2(ty[2 * h], ty[2 * h + 1]);
+                    tz2p[h] = pk2(tz[2 * h], tz[2 * h + 1]);
+                    u2[h][0] = u2[h][1] = u2[h][2] = 0ull;
+                }
+#pragma unroll 2
+                for (int k = 0; k < kF32Tile; k++) {
+                    const ulonglong2 a0 = s_dup[4 * k], a1 = s_dup[4 * k + 1], a2 = s_dup[4 * k + 2];
+                    const f32x2 f2v = s_dup[4 * k + 3].x;
+#pragma unroll
+                    for (int h = 0; h < H; h++)
+                        wall_far_pair2(tx2[h], ty2[h], tz2p[h], a0.x, a0.y, a1.x, a1.y, a2.x, a2.y, f2v, u2[h]);
+                }
+#pragma unroll
+                for (int h = 0; h < H; h++)
+#pragma unroll
+                    for (int c = 0; c < 3; c++) u[2 * h][c] = lo2(u2[h][c]), u[2 * h + 1][c] = hi2(u2[h][c]);
+            }
+        } else if (far_tile) {
 #pragma unroll kFarUnroll
             for (int k = 0; k < kF32Tile; k++) {
                 const float4 p = s_src[k * NQ];
