@@ -492,6 +492,11 @@ def run_ours(args):
                     "note": "frac above counts canonical flops (106 per pair); the kernel issues fewer "
                             "instructions than that count implies, so its frac can exceed 1 while the "
                             "issue slots are not all used"}
+        lane_ops = prof_data.get("fma_lane_ops_per_pair")
+        if lane_ops:
+            # the FP32 pipe's lane rate (128 per SM per clock, packed FP32x2 or not)
+            executed["fma_lane_ops_per_pair"] = lane_ops
+            executed["fma_lane_frac"] = pairs / (far_avg_ms * 1e-3) * lane_ops / (sms * 128 * clocks["sm_mhz"] * 1e6)
     line = {
         "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
