@@ -94,6 +94,10 @@ SIGNATURES = {
                                            c_double, c_double, _P, c_int, c_int64, _P, _P, c_size_t, _P]),
     "flg_swimmer_constraints_dev": (c_int, [_P, c_int64, _P, _P, _P, c_int64, _P, c_int, c_int64, _P]),
     "flg_swimmer_graph_workspace": (c_size_t, [c_int64, c_int64, c_int]),
+    "flg_swimmer_batch_graph_workspace": (c_size_t, [c_int64, c_int64, c_int, c_int]),
+    "flg_swimmer_batch_graph_create": (c_int, [c_int, c_double, c_double, _P, c_int64, _P, _P, _P, c_int64, _P, c_int,
+                                               c_int, c_double, _P, _P, _P, c_int64, c_int, _P, _P, _P, c_size_t, _P,
+                                               POINTER(c_void_p)]),
     "flg_swimmer_graph_create": (c_int, [c_int, c_double, c_double, _P, c_int64, _P, _P, _P, c_int64, _P, c_int,
                                          c_double, _P, _P, _P, c_int64, c_int, _P, _P, _P, c_size_t, _P,
                                          POINTER(c_void_p)]),

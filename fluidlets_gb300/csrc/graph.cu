@@ -20,6 +20,9 @@
 // shape size (force and quadrature point counts), for the stages of swim():
 //   flg_nearest_neighbors -> flg_assemble_nearest_async ->
 //   flg_swimmer_constraints_dev -> FP32 copies -> flg_lu_factor_lowp_async.
+// flg_swimmer_batch_graph_create captures the same for a group of swimmer systems of
+// one shape size: each system's nearest map, assembly and constraint rows, then one
+// FP32 conversion pass over all of them and the batched tensor-core LU.
 #include <algorithm>
 
 #include "flg_common.cuh"
@@ -133,6 +136,40 @@ extern "C" int flg_swimmer_graph_create(int kind, double alpha_re, double alpha_
         FLG_TRY(flg_convert_f64_f32x2(n, n, A, n, K32, A32, ld32, stream));
         // the workspace is reused by the LU: the assembly is done with it by then (stream order)
         return flg_lu_factor_lowp_async(n, K32, ld32, mode, dinv, flags, work, work_bytes, stream);
+    };
+    return capture_graph(stream, seq, graph_exec);
+}
+
+extern "C" size_t flg_swimmer_batch_graph_workspace(int64_t N, int64_t Q, int nbat, int mode) {
+    return std::max(flg_assemble_nearest_workspace(Q, N), flg_lu_factor_lowp_batched_workspace(3 * N + 6, nbat, mode));
+}
+
+extern "C" int flg_swimmer_batch_graph_create(int kind, double alpha_re, double alpha_im, const double *x, int64_t N,
+                                              const double *x0, const double *X, const double *eps, int64_t Q,
+                                              int64_t *nearest, int recompute_nearest, int nbat, double mu_re,
+                                              double *A, float *A32, float *K32, int64_t ld32, int mode, float *dinv,
+                                              int *flags, void *work, size_t work_bytes, void *stream,
+                                              void **graph_exec) {
+    FLG_RANGE("flg_swimmer_batch_graph_create");
+    FLG_REQUIRE(N > 0 && Q >= 0 && nbat >= 1 && flags && A && K32 && dinv, "bad swimmer graph arguments");
+    const int64_t n = 3 * N + 6;
+    FLG_REQUIRE(ld32 >= n, "bad ld32");
+    FLG_REQUIRE(work_bytes >= flg_swimmer_batch_graph_workspace(N, Q, nbat, mode),
+                "workspace too small for the batched swimmer graph");
+    auto seq = [&]() -> int {
+        for (int z = 0; z < nbat; z++) {  // the small per-system stages, in turn on the one workspace
+            const double *xz = x + 3 * N * z, *Xz = X + 3 * Q * z;
+            int64_t *nz = nearest + Q * z;
+            double *Az = A + n * n * z;
+            if (recompute_nearest) FLG_TRY(flg_nearest_neighbors(Xz, Q, xz, N, nz, stream));
+            FLG_TRY(flg_assemble_nearest_async(kind, alpha_re, alpha_im, xz, N, Xz, nz, eps + Q * z, Q, N, mu_re, 0.0,
+                                               Az, FLG_F64, n, flags + 2 * nbat + z, work, work_bytes, stream));
+            FLG_TRY(flg_swimmer_constraints_dev(xz, N, x0 + 3 * z, Xz, nz, Q, Az, FLG_F64, n, stream));
+        }
+        // system z of A (n x n) and of the FP32 copies (n x ld32) are consecutive: one tall matrix
+        FLG_TRY(flg_convert_f64_f32x2(nbat * n, n, A, n, K32, A32, ld32, stream));
+        return flg_lu_factor_lowp_batched_async(n, nbat, K32, ld32, n * ld32, mode, dinv, flags, work, work_bytes,
+                                                stream);
     };
     return capture_graph(stream, seq, graph_exec);
 }

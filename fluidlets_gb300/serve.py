@@ -331,7 +331,7 @@ class SolveServer:
     graph.  Nothing waits for a group to fill."""
 
     def __init__(self, slots: int = 6, hbm_budget_gb: float = 150.0, rtol: float = 1e-10, graphs: bool = True,
-                 lu: str = "auto", lookahead: int = 16, batch: int = 4, batch_points: int = 2304):
+                 lu: str = "auto", lookahead: int = 16, batch: int = 4, batch_points: int = 1280):
         self.slots = slots
         self.budget = int(hbm_budget_gb * 2**30)
         self.rtol = rtol
@@ -392,15 +392,21 @@ class SolveServer:
     @staticmethod
     def _group_key(req, b):
         """Requests with equal group keys run on the same plan key (the LU mode is tuned per
-        kernel and bucket), so they can share a batched plan; None: never grouped."""
+        kernel and bucket; swimmers of one shape size, blob width and viscosity share one), so
+        they can share a batched plan."""
         if not isinstance(req, ResistanceRequest):
-            return None
+            kind = kernel_params(req.kernel if req.kernel is not None else Stokeslet3D())[0]
+            return ("swim", kind, len(req.shape.x), len(req.shape.X), float(req.eps), float(req.mu))
         return (kernel_params(req.kernel)[0], b, float(req.mu), _uniform(req.eps))
 
     def _cap(self, key, b):
-        """Systems per plan of this key: `batch` for tuned tensor-core resistance plans of at
-        most `batch_points` points, else 1."""
-        if key[0] != "res" or self.batch == 1 or b > self.batch_points:
+        """Systems per plan of this key: `batch` for swimmer plans (captured graphs) and for
+        tuned tensor-core resistance plans of at most `batch_points` points, else 1."""
+        if self.batch == 1:
+            return 1
+        if key[0] == "swim":
+            return self.batch if self.graphs else 1
+        if b > self.batch_points:
             return 1
         lu = key[4]
         return 1 if lu == "tune" or lu.startswith("fp32") else self.batch
@@ -422,8 +428,10 @@ class SolveServer:
 
     def _pick(self, slot):
         """Oldest admissible request, preferring one with a free plan within the look-ahead window,
-        plus pending requests of its group key up to the plan's capacity.
-        Returns ([(request, future, t_arrival)], bucket, plan or None, reserved bytes) or None."""
+        plus pending requests of its group key up to the plan's capacity.  A new plan holds as
+        many systems as the key allows (_cap) and the budget leaves room for.
+        Returns ([(request, future, t_arrival)], bucket, plan or None, reserved bytes, systems per
+        plan) or None."""
         cand = None
         for k, (req, fut, t, b, g) in enumerate(self._pending[: self.lookahead]):
             if self._free.get(self._key(req, b)):
@@ -435,12 +443,15 @@ class SolveServer:
         key = self._key(req, b)
         plan, reserved = None, 0
         if self._free.get(key):
-            plan = self._free[key].pop()
+            plan = max(self._free[key], key=lambda p: getattr(p, "cap", 1))
+            self._free[key].remove(plan)
             self._lru.remove(plan)
             cap = getattr(plan, "cap", 1)
         else:
-            cap = self._cap(key, b)
-            need = self._need(req, b) * cap
+            cap, need1 = self._cap(key, b), self._need(req, b)
+            while cap > 1 and self._used + need1 * cap > self.budget:
+                cap -= 1
+            need = need1 * cap
             if self._used + need > self.budget:
                 self._evict_free(need)
                 if self._used + need > self.budget and any(self._busy):
@@ -450,12 +461,12 @@ class SolveServer:
         group = [self._pending.pop(cand)[:3]]
         k = 0
         while len(group) < cap and k < len(self._pending):
-            if g is not None and self._pending[k][4] == g:
+            if self._pending[k][4] == g:
                 group.append(self._pending.pop(k)[:3])
             else:
                 k += 1
         self._busy[slot] = True
-        return group, b, plan, reserved
+        return group, b, plan, reserved, cap
 
     # ---- device hooks (overridden by the scheduler's CPU test) ---------------------------
     def _device(self):
@@ -465,20 +476,14 @@ class SolveServer:
         torch.cuda.set_device(self._dev)
         return torch.cuda.Stream()
 
-    def _run_request(self, slot, stream, req, b, plan):
-        """One request alone: (Result, plan)."""
-        res, plan = self._run_group(slot, stream, [req], b, plan)
-        return res[0], plan
-
-    def _run_group(self, slot, stream, reqs, b, plan):
-        """A group of requests of one plan key (one request, or up to the plan's capacity):
-        ([Result per request], plan)."""
+    def _run_group(self, slot, stream, reqs, b, plan, cap=1):
+        """A group of requests of one plan key (one request, or up to the plan's capacity; a new
+        plan holds `cap` systems): ([Result or exception per request], plan)."""
         with torch.cuda.stream(stream):
             if isinstance(reqs[0], ResistanceRequest):
-                res, plan = self._resistance(slot, stream, reqs, b, plan)
+                res, plan = self._resistance(slot, stream, reqs, b, plan, cap)
             else:
-                r, plan = self._swimmer(stream, reqs[0], plan)
-                res = [r]
+                res, plan = self._swimmers(stream, reqs, plan, cap)
             stream.synchronize()
         return res, plan
 
@@ -494,15 +499,11 @@ class SolveServer:
                     elif self._closed:
                         return
                     self._cv.wait(timeout=0.05)
-            group, b, plan, reserved = item
+            group, b, plan, reserved, cap = item
             reqs = [r for r, _, _ in group]
             t0 = time.perf_counter()
             try:
-                if len(group) == 1:
-                    res, plan = self._run_request(slot, stream, reqs[0], b, plan)
-                    res = [res]
-                else:
-                    res, plan = self._run_group(slot, stream, reqs, b, plan)
+                res, plan = self._run_group(slot, stream, reqs, b, plan, cap)
                 t1 = time.perf_counter()
                 for (req, fut, t_arr), r in zip(group, res):
                     if isinstance(r, Exception):
@@ -539,7 +540,7 @@ class SolveServer:
             return self.lu
         return self._tuned.get((kernel_params(req.kernel)[0], b))
 
-    def _resistance(self, slot, stream, reqs, b, plan):
+    def _resistance(self, slot, stream, reqs, b, plan, cap=1):
         """Resistance requests of one plan key: one (batched) factorization of the group, then
         each system's refinement.  A request whose system fails gets its exception in place of
         a Result."""
@@ -561,8 +562,7 @@ class SolveServer:
                 with self._cv:
                     self._tuned[(kernel_params(req.kernel)[0], b)] = lu
             uniform = _uniform(req.eps)
-            cap = max(len(reqs), self._cap(("res", kernel_params(req.kernel)[0], b, float(req.mu), lu, uniform), b))
-            plan = BucketPlan(req.kernel, b, req.mu, lu, stream, uniform=uniform, cap=cap)
+            plan = BucketPlan(req.kernel, b, req.mu, lu, stream, uniform=uniform, cap=max(cap, len(reqs)))
             plan.nbytes = self._need(req, b) * plan.cap
             with self._cv:
                 self.stats["plans_built"] += 1
@@ -623,34 +623,47 @@ class SolveServer:
             self.stats["tuned"][f"{kernel_params(req.kernel)[0]}:{b}"] = lu
         return lu
 
-    def _swimmer(self, stream, req, plan):
-        """The free-swimmer instant on a pooled SwimmerPlan of its shape size: one captured graph
-        (nearest map -> nearest-neighbour assembly -> constraint rows -> FP32 copies ->
-        tensor-core LU) replayed with this request's points, then FP64 GMRES-IR."""
+    def _swimmers(self, stream, reqs, plan, cap=1):
+        """Free-swimmer instants of one shape size on a pooled SwimmerPlan: one captured graph
+        of the group's systems (nearest maps -> nearest-neighbour assemblies -> constraint rows
+        -> FP32 copies -> batched tensor-core LU) replayed with the requests' points, then each
+        system's FP64 GMRES-IR.  A request whose system fails gets its exception."""
         from .swimming import SwimmerPlan, SwimState, swimming_problem
 
-        if not self.graphs:  # eager: the mixed-precision swimmer solve, no plan
-            st = swimming_problem(req.shape, req.x0, req.B, req.eps, req.mu, req.kernel, precision="mixed",
-                                  rtol=self.rtol)
-            return Result(st, float("nan"), 0, 0, 0, 0, 0, "tf32", 0), None
+        if not self.graphs:  # eager: the mixed-precision swimmer solve, no plan (groups of one)
+            out = []
+            for req in reqs:
+                st = swimming_problem(req.shape, req.x0, req.B, req.eps, req.mu, req.kernel, precision="mixed",
+                                      rtol=self.rtol)
+                out.append(Result(st, float("nan"), 0, 0, 0, 0, 0, "tf32", 0))
+            return out, None
+        req = reqs[0]
         kernel = Stokeslet3D() if req.kernel is None else req.kernel
-        x0 = np.asarray(req.x0, float)
-        B = np.asarray(req.B, float)
-        x = x0 + np.asarray(req.shape.x, float) @ B.T
-        X = x0 + np.asarray(req.shape.X, float) @ B.T
-        v = np.asarray(req.shape.v, float) @ B.T
-        N = len(x)
+        items, geo = [], []
+        for r in reqs:
+            x0 = np.asarray(r.x0, float)
+            B = np.asarray(r.B, float)
+            x = x0 + np.asarray(r.shape.x, float) @ B.T
+            X = x0 + np.asarray(r.shape.X, float) @ B.T
+            v = np.asarray(r.shape.v, float) @ B.T
+            rhs = np.zeros(3 * len(x) + 6)
+            rhs[:3 * len(x)] = v.ravel()
+            items.append((x, X, x0, rhs))
+            geo.append((x, X))
+        N = len(items[0][0])
         if plan is None:
-            plan = SwimmerPlan(kernel, N, len(X), req.eps, req.mu, stream=stream)
+            plan = SwimmerPlan(kernel, N, len(items[0][1]), req.eps, req.mu, stream=stream, cap=max(cap, len(reqs)))
+            plan.nbytes = self._need(req, 0) * plan.cap
             with self._cv:
                 self.stats["plans_built"] += 1
                 self.stats["captures"] += 1
-        rhs = np.zeros(3 * N + 6)
-        rhs[:3 * N] = v.ravel()
-        U, Om, F, nn = plan.solve(x, X, x0, rhs, rtol=self.rtol, stream=stream)
+        outs = plan.solve_group(items, rtol=self.rtol, stream=stream)
         with self._cv:
             self.stats["graph_replays"] += 1
-        return Result(SwimState(U, Om, F, x, X, nn), plan.last_residual, 0, 0, 0, 0, 0, "tf32", 0), plan
+        res = [o if isinstance(o, Exception) else
+               Result(SwimState(o[0], o[1], o[2], x, X, o[3]), o[4], 0, 0, 0, 0, 0, "tf32", 0)
+               for o, (x, X) in zip(outs, geo)]
+        return res, plan
 
 
 # ---- the served mixed workload ------------------------------------------------------

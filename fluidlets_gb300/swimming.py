@@ -91,100 +91,143 @@ def swimming_problem(shape: SwimmerShape, x0, B, eps, mu=1.0, kernel=None, neare
 
 
 class SwimmerPlan:
-    """Device buffers and a captured CUDA graph of the mixed-precision swimmer system for one
+    """Device buffers and captured CUDA graphs of the mixed-precision swimmer system for one
     shape size (N force points, Q quadrature points): nearest map -> nearest-neighbour
     assembly -> constraint rows -> FP32 copies -> tensor-core LU (``flg_swimmer_graph_create``).
     Each ``solve`` writes the stage's points into the buffers, replays the graph and refines
-    with FP64 GMRES-IR; ``swim(..., precision="mixed")`` keeps one plan for all stages."""
+    with FP64 GMRES-IR; ``swim(..., precision="mixed")`` keeps one plan for all stages.
 
-    def __init__(self, kernel, N, Q, eps, mu=1.0, lu="tf32", nearest=None, stream=None):
+    With cap > 1 the plan holds that many systems and replays, for a group of k <= cap
+    swimmers, one graph of k systems (``flg_swimmer_batch_graph_create``: each system's small
+    assembly stages, then one FP32 conversion and the batched tensor-core LU); each system is
+    then refined by its own captured refinement (``solve_group``)."""
+
+    def __init__(self, kernel, N, Q, eps, mu=1.0, lu="tf32", nearest=None, stream=None, cap=1):
         L = load()
         dev = dv.require_cuda()
         if complex(mu).imag != 0.0:
             raise ValueError("swimming needs a real viscosity")
         self.N, self.Q, self.n = N, Q, 3 * N + 6
         n = self.n
+        self.cap = c = 1 if lu.startswith("fp32") else max(1, int(cap))
         self.stream = torch.cuda.Stream(device=dev) if stream is None else stream
         self.last_residual = float("nan")
         f64 = dict(dtype=torch.float64, device=dev)
-        self.x = torch.zeros((N, 3), **f64)
-        self.X = torch.zeros((Q, 3), **f64)
-        self.x0 = torch.zeros(3, **f64)
-        self.e = torch.from_numpy(np.broadcast_to(np.asarray(eps, float), (Q,)).copy()).to(dev)
+        self.x = torch.zeros((c, N, 3), **f64)
+        self.X = torch.zeros((c, Q, 3), **f64)
+        self.x0 = torch.zeros((c, 3), **f64)
+        self.e = torch.from_numpy(np.broadcast_to(np.asarray(eps, float), (c, Q)).copy()).to(dev)
         self.fixed = nearest is not None
-        self.nn = (torch.from_numpy(np.asarray(nearest, np.int64)).to(dev) if self.fixed
-                   else torch.zeros(Q, dtype=torch.int64, device=dev))
-        self.A = torch.empty((n, n), **f64)
+        self.nn = (torch.from_numpy(np.broadcast_to(np.asarray(nearest, np.int64), (c, Q)).copy()).to(dev)
+                   if self.fixed else torch.zeros((c, Q), dtype=torch.int64, device=dev))
+        self.A = torch.empty((c, n, n), **f64)
         self.ld32 = (n + 31) // 32 * 32
-        self.K32 = torch.empty((n, self.ld32), dtype=torch.float32, device=dev)
-        self.A32 = torch.empty((n, self.ld32), dtype=torch.float32, device=dev)
-        self.dinv = torch.empty(L.flg_lu_lowp_dinv_elems(n), dtype=torch.float32, device=dev)
-        self.flags = torch.zeros(3, dtype=torch.int32, device=dev)
+        self.K32 = torch.empty((c, n, self.ld32), dtype=torch.float32, device=dev)
+        self.A32 = torch.empty((c, n, self.ld32), dtype=torch.float32, device=dev)
+        self.dinv = torch.empty((c, L.flg_lu_lowp_dinv_elems(n)), dtype=torch.float32, device=dev)
+        self.flags = torch.zeros(3 * c, dtype=torch.int32, device=dev)
         mode = lu_mode(lu)
-        wb = L.flg_swimmer_graph_workspace(N, Q, mode)
+        wb = (L.flg_swimmer_graph_workspace(N, Q, mode) if c == 1
+              else L.flg_swimmer_batch_graph_workspace(N, Q, c, mode))
         self.ws = dv.workspace(wb)
         kind, are, aim = kernel_params(kernel)
-        self.graph = ctypes.c_void_p(0)
+        self.graphs = {}
         st = ctypes.c_void_p(self.stream.cuda_stream)
         with torch.cuda.stream(self.stream):
-            check(L.flg_swimmer_graph_create(kind, are, aim, dv.ptr(self.x), N, dv.ptr(self.x0), dv.ptr(self.X),
-                                             dv.ptr(self.e), Q, dv.ptr(self.nn), 0 if self.fixed else 1,
-                                             float(complex(mu).real), dv.ptr(self.A), dv.ptr(self.A32),
-                                             dv.ptr(self.K32), self.ld32, mode, dv.ptr(self.dinv), dv.ptr(self.flags),
-                                             dv.ptr(self.ws), wb, st, ctypes.byref(self.graph)), "swimmer graph")
+            for k in range(1, c + 1):
+                h = ctypes.c_void_p(0)
+                head = (kind, are, aim, dv.ptr(self.x), N, dv.ptr(self.x0), dv.ptr(self.X), dv.ptr(self.e), Q,
+                        dv.ptr(self.nn), 0 if self.fixed else 1)
+                tail = (float(complex(mu).real), dv.ptr(self.A), dv.ptr(self.A32), dv.ptr(self.K32), self.ld32, mode,
+                        dv.ptr(self.dinv), dv.ptr(self.flags), dv.ptr(self.ws), wb, st, ctypes.byref(h))
+                if c == 1:
+                    check(L.flg_swimmer_graph_create(*head, *tail), "swimmer graph")
+                else:
+                    check(L.flg_swimmer_batch_graph_create(*head, k, *tail), "batched swimmer graph")
+                self.graphs[k] = h
         self.stream.synchronize()
-        # the refinement captured over fixed buffers (right-hand side b, solution sol)
+        # the refinement of each system captured over fixed buffers (right-hand side b, solution sol)
         from .core import IrGraph
 
-        self.b = torch.zeros(n, **f64)
-        self.sol = torch.zeros(n, **f64)
+        self.b = torch.zeros((c, n), **f64)
+        self.sol = torch.zeros((c, n), **f64)
         self.rtol = 1e-10
-        self.ir = IrGraph(self.A, self.A32, self.K32, self.ld32, self.dinv, self.b, self.sol, self.rtol * 1e-2,
-                          stream=self.stream)
+        self.irs = [IrGraph(self.A[z], self.A32[z], self.K32[z], self.ld32, self.dinv[z], self.b[z], self.sol[z],
+                            self.rtol * 1e-2, stream=self.stream) for z in range(c)]
         self.stream.synchronize()
+
+    @property
+    def graph(self):
+        return self.graphs.get(1)
 
     def solve(self, x, X, x0, rhs, rtol=1e-10, stream=None):
         """(U, Omega, forces, nearest) for world-frame force points x, quadrature points X,
         origin x0 and right-hand side rhs (3N + 6), on `stream` (default: the plan's own);
         the refinement's final FP64 residual is left in last_residual."""
-        L = load()
-        st = self.stream if stream is None else stream
-        with torch.cuda.stream(st):
-            self.x.copy_(torch.from_numpy(np.ascontiguousarray(x, float)))
-            self.X.copy_(torch.from_numpy(np.ascontiguousarray(X, float)))
-            self.x0.copy_(torch.from_numpy(np.asarray(x0, float)))
-            b = torch.from_numpy(np.ascontiguousarray(rhs, float)).to(self.x.device)
-            check(L.flg_graph_launch(self.graph, ctypes.c_void_p(st.cuda_stream)), "swimmer graph replay")
-            if rtol == self.rtol:  # the captured refinement: one synchronization for the whole solve
-                self.b.copy_(b)
-                self.ir.launch(st)
-                status, _, _, self.last_residual = self.ir.result(st)
-            fl = self.flags.cpu()
-            if int(fl[2]):
-                raise ValueError("nearest indices must lie in [0, n_force)")
-            if int(fl[1]):
-                raise RuntimeError("low-precision LU: a bounded device wait timed out")
-            if int(fl[0]):
-                raise np.linalg.LinAlgError(f"zero or non-finite pivot at row {int(fl[0]) - 1} in the low-precision LU")
-            if rtol == self.rtol:
-                from .core import _accept
+        out = self.solve_group([(x, X, x0, rhs)], rtol, stream)[0]
+        if isinstance(out, Exception):
+            raise out
+        U, Om, F, nn, self.last_residual = out
+        return U, Om, F, nn
 
-                _accept(status, self.last_residual, rtol, "GMRES-IR")
-                sol = self.sol
-            else:
-                sol, _, _, self.last_residual = _gmres_ir_dense_dev(self.A, self.K32, self.ld32, self.dinv, b,
-                                                                    rtol * 1e-2, 60, 200, required=rtol, A32=self.A32)
-            sol = dv.to_host(sol)
-            nn = self.nn.cpu().numpy()
+    def solve_group(self, items, rtol=1e-10, stream=None):
+        """Solve a group of k <= cap swimmer systems ((x, X, x0, rhs) each): one replay of the
+        k-system graph, then each system's refinement.  Returns, per system, (U, Omega, forces,
+        nearest, residual) or the exception of that system."""
+        L = load()
+        k = len(items)
+        if not 1 <= k <= self.cap:
+            raise ValueError(f"a group of {k} swimmers on a plan of {self.cap}")
+        st = self.stream if stream is None else stream
         N = self.N
-        return sol[3 * N:3 * N + 3], sol[3 * N + 3:], sol[:3 * N].reshape(N, 3), nn
+        out = []
+        with torch.cuda.stream(st):
+            bs = []
+            for z, (x, X, x0, rhs) in enumerate(items):
+                self.x[z].copy_(torch.from_numpy(np.ascontiguousarray(x, float)))
+                self.X[z].copy_(torch.from_numpy(np.ascontiguousarray(X, float)))
+                self.x0[z].copy_(torch.from_numpy(np.asarray(x0, float)))
+                bs.append(torch.from_numpy(np.ascontiguousarray(rhs, float)).to(self.x.device))
+            check(L.flg_graph_launch(self.graphs[k], ctypes.c_void_p(st.cuda_stream)), "swimmer graph replay")
+            graph_ir = rtol == self.rtol
+            if graph_ir:  # every refinement queued, then one synchronization per result
+                for z in range(k):
+                    self.b[z].copy_(bs[z])
+                    self.irs[z].launch(st)
+            fl = self.flags.cpu().numpy()
+            for z in range(k):
+                try:
+                    if fl[2 * k + z]:
+                        raise ValueError("nearest indices must lie in [0, n_force)")
+                    if fl[2 * z + 1] or fl[1]:
+                        raise RuntimeError("low-precision LU: a bounded device wait timed out")
+                    if fl[2 * z]:
+                        raise np.linalg.LinAlgError(
+                            f"zero or non-finite pivot at row {int(fl[2 * z]) - 1} in the low-precision LU")
+                    if graph_ir:
+                        from .core import _accept
+
+                        status, _, _, resid = self.irs[z].result(st)
+                        _accept(status, resid, rtol, "GMRES-IR")
+                        sol = self.sol[z]
+                    else:
+                        sol, _, _, resid = _gmres_ir_dense_dev(self.A[z], self.K32[z], self.ld32, self.dinv[z], bs[z],
+                                                               rtol * 1e-2, 60, 200, required=rtol, A32=self.A32[z])
+                    sol = dv.to_host(sol)
+                    nn = self.nn[z].cpu().numpy()
+                    out.append((sol[3 * N:3 * N + 3], sol[3 * N + 3:], sol[:3 * N].reshape(N, 3), nn, resid))
+                except Exception as e:  # noqa: BLE001 - this system's own failure
+                    out.append(e)
+        return out
 
     def close(self):
-        if getattr(self, "ir", None) is not None:
-            self.ir.close()
-        if self.graph:
-            load().flg_graph_destroy(self.graph)
-            self.graph = ctypes.c_void_p(0)
+        for ir in getattr(self, "irs", []):
+            ir.close()
+        self.irs = []
+        for h in getattr(self, "graphs", {}).values():
+            if h:
+                load().flg_graph_destroy(h)
+        self.graphs = {}
 
     def __del__(self):
         try:

@@ -372,6 +372,21 @@ int flg_swimmer_graph_create(int kind, double alpha_re, double alpha_im, const d
                              int recompute_nearest, double mu_re, double *A, float *A32, float *K32, int64_t ld32,
                              int mode, float *dinv, int *flags, void *work, size_t work_bytes, void *stream,
                              void **graph_exec);
+/* The batched form for a group of nbat swimmer systems of one shape size: system z has
+ * x + 3 N z, x0 + 3 z, X + 3 Q z, eps + Q z, nearest + Q z, A + z (3N+6)^2 (ld 3N+6), A32 / K32
+ * + z (3N+6) ld32, dinv + z flg_lu_lowp_dinv_elems(3N+6); flags holds 3 nbat ints: the LU
+ * flags of system z at flags[2 z], flags[2 z + 1] (as flg_lu_factor_lowp_batched_async) and its
+ * invalid-nearest-index flag at flags[2 nbat + z] (nbat = 1: the layout of
+ * flg_swimmer_graph_create).  One graph: each system's nearest map (when recompute_nearest),
+ * nearest-neighbour assembly and constraint rows, then one FP32 conversion pass over all
+ * systems and flg_lu_factor_lowp_batched_async (tensor-core modes).  Each system's factors are
+ * bit-identical to its own flg_swimmer_graph_create replay.  No counterpart in the reference. */
+size_t flg_swimmer_batch_graph_workspace(int64_t N, int64_t Q, int nbat, int mode);
+int flg_swimmer_batch_graph_create(int kind, double alpha_re, double alpha_im, const double *x, int64_t N,
+                                   const double *x0, const double *X, const double *eps, int64_t Q, int64_t *nearest,
+                                   int recompute_nearest, int nbat, double mu_re, double *A, float *A32, float *K32,
+                                   int64_t ld32, int mode, float *dinv, int *flags, void *work, size_t work_bytes,
+                                   void *stream, void **graph_exec);
 int flg_graph_launch(void *graph_exec, void *stream);
 int flg_graph_destroy(void *graph_exec);
 

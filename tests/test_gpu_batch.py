@@ -218,3 +218,45 @@ def test_batched_bucket_graph_matches_single_graphs_and_oracle():
             assert np.linalg.norm(F - ref) / np.linalg.norm(ref) < 1e-10, z
     finally:
         L.flg_graph_destroy(h)
+
+
+def test_batched_swimmer_graph_matches_single_plans():
+    """Three biflagellate swimmer instants (678 unknowns each) through one SwimmerPlan of three
+    systems (one batched graph, one refinement per system): each equals its own single-system
+    plan's solve and the plain FP64 swimmer solve."""
+    from fluidlets_gb300.geometry import biflagellate_shape
+    from fluidlets_gb300.swimming import SwimmerPlan
+
+    rng = np.random.default_rng(4)
+    items = []
+    for t in (0.1, 0.45, 0.8):
+        sh = biflagellate_shape(t, amplitude=0.08)
+        B = np.linalg.qr(rng.normal(size=(3, 3)))[0]
+        B *= np.sign(np.linalg.det(B))
+        x0 = rng.normal(size=3) * 0.1
+        x = x0 + sh.x @ B.T
+        X = x0 + sh.X @ B.T
+        rhs = np.zeros(3 * len(x) + 6)
+        rhs[:3 * len(x)] = (sh.v @ B.T).ravel()
+        items.append((sh, B, x0, (x, X, x0, rhs)))
+    N, Q = len(items[0][3][0]), len(items[0][3][1])
+    group = SwimmerPlan(fl.Stokeslet3D(), N, Q, 0.02, cap=3)
+    single = SwimmerPlan(fl.Stokeslet3D(), N, Q, 0.02)
+    try:
+        outs = group.solve_group([it[3] for it in items])
+        for (sh, B, x0, item), out in zip(items, outs):
+            assert not isinstance(out, Exception), out
+            U, Om, F, nn, resid = out
+            U1, Om1, F1, nn1 = single.solve(*item)
+            assert resid < 1e-10
+            assert np.array_equal(nn, nn1)
+            assert np.array_equal(U, U1) and np.array_equal(Om, Om1) and np.array_equal(F, F1)
+            ref = fl.swimming_problem(sh, x0, B, 0.02)
+            both, both_ref = np.concatenate([U, Om]), np.concatenate([ref.U, ref.Omega])
+            assert np.linalg.norm(both - both_ref) / np.linalg.norm(both_ref) < 1e-9
+        # a group of two on the same plan (the graph of two systems)
+        outs2 = group.solve_group([items[2][3], items[0][3]])
+        assert np.array_equal(outs2[0][0], outs[2][0]) and np.array_equal(outs2[1][2], outs[0][2])
+    finally:
+        group.close()
+        single.close()

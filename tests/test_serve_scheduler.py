@@ -31,19 +31,22 @@ class FakeServer(SolveServer):
     def _make_stream(self):
         return None
 
-    def _run_request(self, slot, stream, req, b, plan):
+    def _run_group(self, slot, stream, reqs, b, plan, cap=1):
         with self._lock2:
             self.concurrent += 1
             self.max_concurrent = max(self.max_concurrent, self.concurrent)
         with self._cv:
             self.peak = max(self.peak, self._used)
-            if isinstance(req, ResistanceRequest) and plan is None:
+            if plan is None:
                 plan = _Plan(b, 0)
-                self.switches += 1
+                plan.cap = cap
+                if isinstance(reqs[0], ResistanceRequest):
+                    self.switches += 1
+        assert len(reqs) <= plan.cap
         time.sleep(0.001)
         with self._lock2:
             self.concurrent -= 1
-        return Result(None, 0.0, 0, 0, 0, slot, b), plan
+        return [Result(None, 0.0, 0, 0, 0, slot, b) for _ in reqs], plan
 
 
 def mix(n, seed, sizes=(200, 700, 1500, 3000)):
@@ -143,19 +146,15 @@ class GroupServer(FakeServer):
         self.groups = []
         super().__init__(*a, **k)
 
-    def _run_group(self, slot, stream, reqs, b, plan):
+    def _run_group(self, slot, stream, reqs, b, plan, cap=1):
         with self._cv:
             self.groups.append([(self._group_key(r, b), b) for r in reqs])
             if plan is None:
                 plan = _Plan(b, 0)
-                plan.cap = self._cap(self._key(reqs[0], b), b)
+                plan.cap = cap
         assert len(reqs) <= plan.cap
         time.sleep(0.002)
         return [Result(None, 0.0, 0, 0, 0, slot, b) for _ in reqs], plan
-
-    def _run_request(self, slot, stream, req, b, plan):
-        res, plan = self._run_group(slot, stream, [req], b, plan)
-        return res[0], plan
 
 
 def test_same_key_requests_are_grouped_up_to_the_batch():
@@ -172,15 +171,28 @@ def test_same_key_requests_are_grouped_up_to_the_batch():
     assert sum(sizes) == len(reqs) and max(sizes) == 4
     for g in groups:
         assert len({k for k, _ in g}) == 1  # one plan key per group
-        if g[0][0] is None or g[0][1] > 2304:  # swimmers and large buckets run alone
+        if g[0][0][0] != "swim" and g[0][1] > 2304:  # large buckets run alone
             assert len(g) == 1
+    # swimmers of one shape size are grouped too
+    assert max(len(g) for g in groups if g[0][0][0] == "swim") > 1
     assert sum(stats["groups"].get(k, 0) * k for k in stats["groups"]) == len(reqs)
     assert {r.batch for r in res} >= {1, 4}
 
 
 def test_untuned_and_fp32_buckets_are_not_grouped():
-    reqs = mix(60, 5, sizes=(300,))
+    reqs = [r for r in mix(80, 5, sizes=(300,)) if isinstance(r, ResistanceRequest)]
     for lu in ("auto", "fp32"):
         with GroupServer(slots=2, lu=lu, batch=4) as srv:
             [f.result(timeout=60) for f in [srv.submit(r) for r in reqs]]
             assert max(len(g) for g in srv.groups) == 1, lu
+
+
+def test_group_capacity_shrinks_to_the_budget():
+    """A new plan holds up to `batch` systems, as many as the budget has room for: under a
+    budget of two and a half swimmer systems the groups hold at most two."""
+    shape = fl.SwimmerShape(np.zeros((50, 3)), np.zeros((50, 3)), np.zeros((200, 3)))
+    reqs = [SwimmerRequest(shape, np.zeros(3), np.eye(3), 0.1) for _ in range(40)]
+    one = SolveServer._need(reqs[0], 0)
+    with GroupServer(slots=1, batch=4, hbm_budget_gb=2.5 * one / 2**30) as srv:
+        [f.result(timeout=60) for f in [srv.submit(r) for r in reqs]]
+        assert 1 < max(len(g) for g in srv.groups) <= 2
