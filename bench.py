@@ -59,7 +59,8 @@ def parse():
     p.add_argument("--batch", type=int, default=4, help="most same-bucket requests per batched factorization "
                                                         "(serve workload)")
     # one hot-path operation at a chosen size, for profiler captures (no JSON line)
-    p.add_argument("--case", default=None, choices=["sum", "assemble", "lu", "resistance", "breakdown", "swim"],
+    p.add_argument("--case", default=None,
+                   choices=["sum", "assemble", "lu", "resistance", "breakdown", "swim", "lu_batch"],
                    help="run one operation at a chosen size for a profiler capture instead of the benchmark")
     p.add_argument("--kind", default="wall", choices=["stokeslet", "wall", "brinkman"])
     p.add_argument("--alpha", type=complex, default=0.0)
@@ -69,6 +70,7 @@ def parse():
     p.add_argument("--n", type=int, default=1536, help="points for the assemble / lu / resistance cases")
     p.add_argument("--lu", default="tf32")
     p.add_argument("--reps", type=int, default=2)
+    p.add_argument("--nbat", type=int, default=4, help="systems per group (lu_batch case)")
     return p.parse_args()
 
 
@@ -674,6 +676,8 @@ def run_case(a):
         torch.cuda.synchronize()
     elif a.case == "breakdown":
         case_breakdown(a, kern)
+    elif a.case == "lu_batch":
+        case_lu_batch(a, kern)
     elif a.case == "swim":
         case_swim(a)
     else:
@@ -692,6 +696,92 @@ def run_case(a):
                 core.resistance(kern, Xd, U, eps, precision=a.precision, lu=a.lu)
             torch.cuda.synchronize()
             print(f"{a.case} n={a.n}: {1e3 * (time.perf_counter() - t0):.2f} ms")
+
+
+def case_lu_batch(a, kern):
+    """A group of nbat resistance systems of one bucket (a.n points each, Fibonacci spheres of
+    slightly different radii): one replay of the batched bucket graph (assembly, FP32 copies,
+    batched tensor-core LU) against nbat replays of the single-system graph, one after another
+    on one stream and side by side on nbat streams; CUDA-event times per group."""
+    import ctypes
+
+    import torch
+
+    from fluidlets_gb300 import _device as dv
+    from fluidlets_gb300 import _lib
+    from fluidlets_gb300.geometry import fibonacci_sphere, mean_nn_spacing
+
+    L = _lib.load()
+    dev = torch.device("cuda")
+    code, nbat, n_cap = _lib.KIND[a.kind], a.nbat, a.n
+    n, ld32 = 3 * n_cap, (3 * n_cap + 31) // 32 * 32
+    mode = _lib.lu_mode(a.lu)
+    pts = np.stack([fibonacci_sphere(n_cap) * (1.0 + 0.05 * z) + ([0, 0, 1.5] if a.kind == "wall" else 0)
+                    for z in range(nbat)])
+    eps = np.stack([np.full(n_cap, 0.25 * mean_nn_spacing(pts[z])) for z in range(nbat)])
+    P, E = torch.tensor(pts, device=dev), torch.tensor(eps, device=dev)
+    NR = torch.full((nbat,), n_cap, dtype=torch.int64, device=dev)
+    bufs = dict(K=torch.empty((nbat, n, n), dtype=torch.float64, device=dev),
+                K32=torch.empty((nbat, n, ld32), dtype=torch.float32, device=dev),
+                A32=torch.empty((nbat, n, ld32), dtype=torch.float32, device=dev),
+                dinv=torch.empty((nbat, L.flg_lu_lowp_dinv_elems(n)), dtype=torch.float32, device=dev),
+                flags=torch.zeros(2 * nbat, dtype=torch.int32, device=dev))
+    streams = [torch.cuda.Stream() for _ in range(nbat)]
+    sp = [ctypes.c_void_p(s.cuda_stream) for s in streams]
+
+    def graph(z0, k, st):
+        wb = L.flg_lu_factor_lowp_batched_workspace(n, k, mode) if k > 1 else L.flg_lu_factor_lowp_workspace(n, mode)
+        ws = dv.workspace(wb)
+        h = ctypes.c_void_p(0)
+        args = (code, 0.0, 0.0, dv.ptr(P[z0]), dv.ptr(E[z0]), 1, dv.ptr(NR[z0:]), n_cap)
+        tail = (1.0, dv.ptr(bufs["K"][z0]), dv.ptr(bufs["A32"][z0]), dv.ptr(bufs["K32"][z0]), ld32, mode,
+                dv.ptr(bufs["dinv"][z0]), dv.ptr(bufs["flags"][2 * z0:]), dv.ptr(ws), wb, st, ctypes.byref(h))
+        _lib.check(L.flg_bucket_batch_graph_create(*args, k, *tail) if k > 1 else
+                   L.flg_bucket_graph_create(*args, *tail), "graph")
+        return h, ws
+
+    gb = graph(0, nbat, sp[0])
+    gs = [graph(z, 1, sp[z]) for z in range(nbat)]
+    torch.cuda.synchronize()
+
+    def timed(fn):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ms = []
+        for _ in range(max(a.reps, 3)):
+            e0.record(streams[0])
+            fn()
+            for s in streams[1:]:  # the other streams' work joins stream 0 before the end event
+                ev = torch.cuda.Event()
+                ev.record(s)
+                streams[0].wait_event(ev)
+            e1.record(streams[0])
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return min(ms)
+
+    def batched():
+        L.flg_graph_launch(gb[0], sp[0])
+
+    def sequential():
+        for z in range(nbat):
+            L.flg_graph_launch(gs[z][0], sp[0])
+
+    def side_by_side():
+        ev = torch.cuda.Event()
+        ev.record(streams[0])
+        for z in range(nbat):
+            streams[z].wait_event(ev)
+            L.flg_graph_launch(gs[z][0], sp[z])
+
+    tb, tq, tp = timed(batched), timed(sequential), timed(side_by_side)
+    assert not bufs["flags"].any()
+    print(f"[lu_batch {a.kind} {a.lu}] {nbat} systems of n = {n}: batched graph {tb:.3f} ms, "
+          f"{nbat} single graphs in turn {tq:.3f} ms, side by side on {nbat} streams {tp:.3f} ms")
+    for h, _ in [gb] + gs:
+        L.flg_graph_destroy(h)
 
 
 def case_swim(a):
