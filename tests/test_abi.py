@@ -68,6 +68,24 @@ def test_lu_workspace_does_not_depend_on_the_tile_width(lib):
             assert L.flg_lu_factor_lowp_workspace(n, lib.LU_MODE[prec + ":256"]) == base
 
 
+def test_batched_lu_workspace_scales_with_the_batch(lib):
+    """The batched LU's scratch is the single system's per system (the BF16 copies of the
+    panels included), across both outer-panel widths (512 columns below n = 8,192, 1,024 from
+    there); the batched swimmer graph's workspace covers its LU's."""
+    L = lib.load()
+    for n in (768, 4608, 8192, 12288):
+        for prec in ("tf32", "bf16"):
+            one = L.flg_lu_factor_lowp_batched_workspace(n, 1, lib.LU_MODE[prec])
+            assert one + 256 == L.flg_lu_factor_lowp_workspace(n, lib.LU_MODE[prec])
+            for k in (2, 4):
+                wk = L.flg_lu_factor_lowp_batched_workspace(n, k, lib.LU_MODE[prec])
+                assert k * one - 4096 <= wk <= k * one + 4096, (n, prec, k)
+    # 1,024-column outer panels double the K-major copy of U from n = 8,192 on
+    assert L.flg_lu_factor_lowp_batched_workspace(8192, 1, 0) > 1.4 * L.flg_lu_factor_lowp_batched_workspace(8064, 1, 0)
+    for k in (1, 3):
+        assert L.flg_swimmer_batch_graph_workspace(224, 896, k, 0) >= L.flg_lu_factor_lowp_batched_workspace(678, k, 0)
+
+
 def test_unknown_lu_name_is_a_value_error(lib):
     assert lib.lu_mode("bf16:128") == lib.LU_MODE["bf16:128"]
     for bad in ("tf16", "fp32:128", "tf32:64", None):
