@@ -338,7 +338,9 @@ class SolveServer:
         self.graphs = graphs
         self.lu = lu
         self.lookahead = lookahead
-        self.batch = max(1, int(batch))
+        if not 1 <= int(batch) <= 64:
+            raise ValueError(f"batch must lie in [1, 64] (systems per batched factorization), got {batch}")
+        self.batch = int(batch)
         self.batch_points = batch_points
         self._pending = []            # [(request, future, t_arrival, bucket, group key)]
         self._cv = threading.Condition()

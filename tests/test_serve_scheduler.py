@@ -196,3 +196,9 @@ def test_group_capacity_shrinks_to_the_budget():
     with GroupServer(slots=1, batch=4, hbm_budget_gb=2.5 * one / 2**30) as srv:
         [f.result(timeout=60) for f in [srv.submit(r) for r in reqs]]
         assert 1 < max(len(g) for g in srv.groups) <= 2
+
+
+def test_batch_size_is_checked():
+    for bad in (0, 65):
+        with pytest.raises(ValueError):
+            FakeServer(slots=1, batch=bad)
